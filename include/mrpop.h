@@ -1,0 +1,188 @@
+/*
+ * mrpop.h -- C ABI of the GB300-native batched edge validator for MR.POP.
+ *
+ * The reference planner has no library boundary for this path: edge checks are
+ * block-collective __device__ routines inlined into its planner kernels
+ *   fkcc_single_buffer<Robot>       src/planning/utils.cuh:447-534  (env + self)
+ *   fkcc_single_buffer_mr<Robot>    src/planning/utils.cuh:536-624  (one arm)
+ *   fkcc_single_buffer_drrt<Robot>  src/planning/utils.cuh:626-686  (self only)
+ * whose callers interpolate the edge first (pop_planner.cu:551-561 extend,
+ * :666-703 connect, roadmap_interior.cuh:219-234 roadmap edges,
+ * path_simplification.cu:85-129 B-spline, :155-200 shortcut).  This header is
+ * the batched, stream-ordered replacement: one call validates many edges.
+ *
+ * Conventions
+ *   - Every function returns an mrpop_status; nothing calls exit() (the
+ *     reference's cudaCheckError does, utils.cuh:265-274).
+ *   - Device entry points are asynchronous on the given cudaStream_t (passed as
+ *     void*; NULL = legacy default stream).  Pointers documented "device" must
+ *     be device-accessible for the whole call.
+ *   - Handles are immutable after creation and may be shared by threads; calls
+ *     on one handle from several host threads are safe.  The library keeps no
+ *     global device state except the per-device tables it sets up on first use.
+ *   - Configurations are float32, row-major [n_edges][dof] with dof = 7 * arms
+ *     (the layout of the reference's Robot::Configuration arrays,
+ *     Robots.hh:46-140).  Sample k (1..g) of an edge is q0 + k*(q1-q0)/g as the
+ *     reference computes it; sample 0 (the edge start) is never tested.
+ */
+#ifndef MRPOP_H
+#define MRPOP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MRPOP_OK = 0,
+    MRPOP_ERR_INVALID_ARGUMENT = 1,
+    MRPOP_ERR_CUDA = 2,
+    MRPOP_ERR_UNSUPPORTED = 3,
+    MRPOP_ERR_OUT_OF_MEMORY = 4,
+    MRPOP_ERR_DEVICE_TIMEOUT = 5, /* a bounded device wait gave up (see mrpop_scene_status) */
+} mrpop_status;
+
+/* Check selection and semantics (flags argument). */
+#define MRPOP_CHECK_ENV 0x1u   /* robot spheres vs scene obstacles                    */
+#define MRPOP_CHECK_SELF 0x2u  /* intra-arm pairs and, for composites, arm-vs-arm     */
+#define MRPOP_MODE_EXACT 0x10u /* every flagged sample gets the detailed check        */
+/* Without MRPOP_MODE_EXACT the verdicts are those of the reference's own check,
+ * including its proportional thread split (utils.cuh:476-517: samples whose share
+ * of 4*g threads rounds to zero get no detailed check) and, for composites, its
+ * detailed intra-arm row indexing (panda_four.cuh:388-413).
+ *   fkcc_single_buffer       == MRPOP_CHECK_ENV | MRPOP_CHECK_SELF, arm = -1
+ *   fkcc_single_buffer_drrt  == MRPOP_CHECK_SELF,                   arm = -1
+ *   fkcc_single_buffer_mr    == MRPOP_CHECK_ENV | MRPOP_CHECK_SELF, arm = robot_id */
+
+/* Edge segmentation rules (mrpop_validate_segments). */
+#define MRPOP_RULE_PLAIN 0    /* one segment: q_k = q0 + k*((q1-q0)/g)                       */
+#define MRPOP_RULE_CONNECT 1  /* n = int(|q1-q0|/range)+1, q_k = q + k*(vec/g), q += vec     */
+                              /*   (pop_planner.cu:666-703)                                  */
+#define MRPOP_RULE_BSPLINE 2  /* n = ceil(|q1-q0|/range), q_k += delta per segment           */
+                              /*   (path_simplification.cu:85-129)                           */
+#define MRPOP_RULE_SHORTCUT 3 /* n = ceil((|q1-q0|-0.001)/range), q_k += delta per segment   */
+                              /*   (path_simplification.cu:155-200)                          */
+
+#define MRPOP_MAX_ARMS 5
+#define MRPOP_MAX_GRANULARITY 64 /* the reference's MAX_GRANULARITY, pop_planner_state.cuh:13 */
+
+/*
+ * Scene description (host memory; the library copies it).  Records are packed
+ * float32 in the field order of the reference's shape structs
+ * (src/collision/shapes.hh:28-185, environment.hh:11-40):
+ *   sphere  {x, y, z, r}                                         4 floats
+ *   capsule {x1, y1, z1, xv, yv, zv, r, rdv}  rdv = 1/|v|^2      8 floats
+ *   cuboid  {x, y, z, a1x, a1y, a1z, a2x, a2y, a2z, a3x, a3y, a3z, h1, h2, h3}  15 floats
+ * z_capsules / z_cuboids use the z-aligned tests (utils.cuh:165-181, 208-228).
+ * cylinders are accepted and never tested, as in the reference (its scene loop
+ * utils.cuh:231-260 does not read Environment::cylinders).
+ */
+typedef struct {
+    const float *spheres;
+    uint32_t num_spheres;
+    const float *capsules;
+    uint32_t num_capsules;
+    const float *z_capsules;
+    uint32_t num_z_capsules;
+    const float *cylinders;
+    uint32_t num_cylinders;
+    const float *cuboids;
+    uint32_t num_cuboids;
+    const float *z_cuboids;
+    uint32_t num_z_cuboids;
+} mrpop_scene_desc;
+
+typedef struct mrpop_scene mrpop_scene;
+typedef struct mrpop_robotset mrpop_robotset;
+typedef struct mrpop_workspace mrpop_workspace;
+
+/* Replaces setup_environment_on_device (pop_planner.cu:69-161): copies the
+ * scene to the current device.  Synchronous. */
+mrpop_status mrpop_scene_create(const mrpop_scene_desc *desc, mrpop_scene **out);
+mrpop_status mrpop_scene_destroy(mrpop_scene *scene);
+/* Device-side status word of the scene (0 = fine; nonzero = a bounded wait in a
+ * kernel gave up; the kernel then reported its edges as invalid). Synchronous. */
+mrpop_status mrpop_scene_status(const mrpop_scene *scene, uint32_t *status_out);
+
+/* Arm bases.  base_T: n_arms row-major 4x4 transforms (host memory), or NULL
+ * for the reference's compiled-in layouts: identity for 1 arm
+ * (panda.cuh:78-83), quad_franka_base_transform for 4 (panda.cuh:16-40 ==
+ * panda_four.cuh:17-41), five_franka_base_transform for 5 (panda.cuh:42-73 ==
+ * panda_five.cuh:17-46).  The arms are Franka Pandas with the reference's
+ * sphere model (panda_multi_geometry.cuh). */
+mrpop_status mrpop_robotset_create(int n_arms, const float *base_T, mrpop_robotset **out);
+mrpop_status mrpop_robotset_destroy(mrpop_robotset *robots);
+
+/*
+ * Validate n_edges edges q0[e] -> q1[e] (device pointers, [n_edges][dof]).
+ *   arm < 0 : composite check over all arms, dof = 7 * n_arms
+ *   arm >= 0: single-arm check of arm `arm` (its base), dof = 7
+ * granularity: samples per edge, 1..64.
+ * Outputs (device): valid[e] = 1 if collision-free; first_hit[e] = the 1-based
+ * sample index of the first sample whose detailed check fired (-1 if valid).
+ * Replaces one fkcc_single_buffer* call per edge (see flags above).
+ */
+mrpop_status mrpop_validate_edges(const mrpop_scene *scene, const mrpop_robotset *robots,
+                                  const float *q0, const float *q1, int64_t n_edges,
+                                  int granularity, uint32_t flags, int arm, uint8_t *valid,
+                                  int32_t *first_hit, void *stream);
+
+/*
+ * Segmented edges (connect, B-spline and shortcut forms).  Each edge is split
+ * into n segments of `granularity` samples by `rule` with `range` (settings.range);
+ * segments are checked in order and checking stops at the first invalid one.
+ * first_hit = segment * granularity + sample (1-based), -1 if valid.
+ * n_seg_out (device, optional) receives each edge's segment count.
+ */
+mrpop_status mrpop_validate_segments(const mrpop_scene *scene, const mrpop_robotset *robots,
+                                     const float *q0, const float *q1, int64_t n_edges,
+                                     int granularity, int rule, float range, uint32_t flags,
+                                     int arm, uint8_t *valid, int32_t *first_hit,
+                                     int32_t *n_seg_out, void *stream);
+
+/*
+ * Host-buffer form for callers without device memory (the reference's host
+ * API, dRRT::solve in Planners.hh:57-64, hands host arrays across): copies
+ * q0/q1 from host memory, validates, copies valid/first_hit back and waits.
+ * The workspace owns pinned staging and device buffers and grows on demand.
+ */
+mrpop_status mrpop_workspace_create(mrpop_workspace **out);
+mrpop_status mrpop_workspace_destroy(mrpop_workspace *ws);
+mrpop_status mrpop_validate_edges_host(mrpop_workspace *ws, const mrpop_scene *scene,
+                                       const mrpop_robotset *robots, const float *q0,
+                                       const float *q1, int64_t n_edges, int granularity,
+                                       uint32_t flags, int arm, int rule, float range,
+                                       uint8_t *valid, int32_t *first_hit);
+
+/*
+ * Sphere centres of n single-arm configurations (device q [n][7], device out
+ * [n][spheres][3]); detailed = 0: the 11 broad-phase spheres, 1: the 59
+ * detailed spheres.  The same FK the validator runs (panda.cuh:598-669,
+ * 761-829 with the base of arm `arm`).
+ */
+mrpop_status mrpop_fk_spheres(const mrpop_robotset *robots, int arm, const float *q, int64_t n,
+                              int detailed, float *out, void *stream);
+
+/* Algorithmic flop count per edge (FMA = 2; the convention of the project's
+ * roofline) for the same arguments as mrpop_validate_segments; writes
+ * flops[e] (device, double).  Runs the validator with counting enabled. */
+mrpop_status mrpop_count_flops(const mrpop_scene *scene, const mrpop_robotset *robots,
+                               const float *q0, const float *q1, int64_t n_edges,
+                               int granularity, int rule, float range, uint32_t flags, int arm,
+                               double *flops, void *stream);
+
+/* The __cosf/__sinf values the validator uses for inputs x (device arrays). */
+mrpop_status mrpop_debug_trig(const float *x, int64_t n, float *cos_out, float *sin_out,
+                              void *stream);
+
+/* Last error message of the calling thread ("" if none). */
+const char *mrpop_last_error(void);
+/* Library version string. */
+const char *mrpop_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MRPOP_H */

@@ -1,0 +1,439 @@
+// api.cu -- C ABI of the GB300 edge validator (declared in include/mrpop.h).
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/mrpop.h"
+#include "launch.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+mrpop_status fail(mrpop_status st, const std::string &msg) {
+    g_last_error = msg;
+    return st;
+}
+
+mrpop_status cuda_fail(cudaError_t err, const char *what) {
+    return fail(MRPOP_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
+}
+
+#define MRPOP_CUDA(call, what)                                                                             \
+    do {                                                                                                   \
+        cudaError_t _e = (call);                                                                           \
+        if (_e != cudaSuccess) return cuda_fail(_e, what);                                                 \
+    } while (0)
+
+// Reference base layouts (row-major 4x4): panda.cuh:16-73.
+const float kQuadBase[4][16] = {
+    {-0.65122966f, -0.75888071f, 0.f, 0.40000000f, 0.75888071f, -0.65122966f, 0.f, -0.40000000f, 0.f, 0.f,
+     1.f, 0.15000000f, 0.f, 0.f, 0.f, 1.f},
+    {0.78999223f, -0.61311685f, 0.f, -0.40000000f, 0.61311685f, 0.78999223f, 0.f, -0.40000000f, 0.f, 0.f,
+     1.f, 0.15000000f, 0.f, 0.f, 0.f, 1.f},
+    {0.78999223f, 0.61311685f, 0.f, -0.40000000f, -0.61311685f, 0.78999223f, 0.f, 0.40000000f, 0.f, 0.f,
+     1.f, 0.15000000f, 0.f, 0.f, 0.f, 1.f},
+    {-0.65122966f, 0.75888071f, 0.f, 0.40000000f, -0.75888071f, -0.65122966f, 0.f, 0.40000000f, 0.f, 0.f,
+     1.f, 0.15000000f, 0.f, 0.f, 0.f, 1.f}};
+const float kFiveBase[5][16] = {
+    {0.00079633f, -0.99999968f, 0.f, 0.60000000f, 0.99999968f, 0.00079633f, 0.f, -0.70000000f, 0.f, 0.f, 1.f,
+     0.10000000f, 0.f, 0.f, 0.f, 1.f},
+    {0.00079633f, -0.99999968f, 0.f, 0.00000000f, 0.99999968f, 0.00079633f, 0.f, -0.70000000f, 0.f, 0.f, 1.f,
+     0.10000000f, 0.f, 0.f, 0.f, 1.f},
+    {0.00079633f, 0.99999968f, 0.f, 0.60000000f, -0.99999968f, 0.00079633f, 0.f, 0.70000000f, 0.f, 0.f, 1.f,
+     0.10000000f, 0.f, 0.f, 0.f, 1.f},
+    {0.00079633f, 0.99999968f, 0.f, 0.00000000f, -0.99999968f, 0.00079633f, 0.f, 0.70000000f, 0.f, 0.f, 1.f,
+     0.10000000f, 0.f, 0.f, 0.f, 1.f},
+    {1.00000000f, 0.00000000f, 0.f, -0.60000000f, 0.00000000f, 1.00000000f, 0.f, -0.20000000f, 0.f, 0.f, 1.f,
+     0.10000000f, 0.f, 0.f, 0.f, 1.f}};
+
+size_t warp_scratch_bytes() { return sizeof(mrpop::WarpScratch) * mrpop::kWarpsPerBlock; }
+
+// Largest staged scene: the block's dynamic shared memory stays below this.
+constexpr size_t kMaxDynSmem = 200 * 1024;
+
+}  // namespace
+
+struct mrpop_scene {
+    float4 *d_buf = nullptr;          // packed obstacles (float4 units)
+    unsigned int *d_status = nullptr; // bounded-wait error word
+    mrpop::SceneCounts counts{};
+    int total_f4 = 0;
+    double env_test_flops = 0.0;
+    int device = 0;
+};
+
+struct mrpop_robotset {
+    int n_arms = 0;
+    float base[mrpop::kMaxArms][12] = {};
+};
+
+struct mrpop_workspace {
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    float *d_q0 = nullptr, *d_q1 = nullptr;
+    uint8_t *d_valid = nullptr;
+    int32_t *d_first = nullptr;
+    size_t cap_cfg = 0, cap_edges = 0;
+};
+
+extern "C" {
+
+const char *mrpop_last_error(void) { return g_last_error.c_str(); }
+const char *mrpop_version(void) { return "mrpop-gb300 0.1.0 (sm_103a)"; }
+
+mrpop_status mrpop_scene_create(const mrpop_scene_desc *desc, mrpop_scene **out) {
+    if (!desc || !out) return fail(MRPOP_ERR_INVALID_ARGUMENT, "scene_create: null argument");
+    *out = nullptr;
+    auto need = [](const float *p, uint32_t n) { return n == 0 || p != nullptr; };
+    if (!need(desc->spheres, desc->num_spheres) || !need(desc->capsules, desc->num_capsules) ||
+        !need(desc->z_capsules, desc->num_z_capsules) || !need(desc->cuboids, desc->num_cuboids) ||
+        !need(desc->z_cuboids, desc->num_z_cuboids) || !need(desc->cylinders, desc->num_cylinders))
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "scene_create: null array with nonzero count");
+    mrpop::SceneCounts c{(int)desc->num_spheres, (int)desc->num_capsules, (int)desc->num_z_capsules,
+                         (int)desc->num_cuboids, (int)desc->num_z_cuboids};
+    const mrpop::SceneLayout L = mrpop::scene_layout(c);
+    if ((size_t)L.total * sizeof(float4) + warp_scratch_bytes() > kMaxDynSmem)
+        return fail(MRPOP_ERR_UNSUPPORTED, "scene_create: scene too large to stage in shared memory (" +
+                                               std::to_string(L.total * 16) + " bytes)");
+    std::vector<float4> h((size_t)L.total);
+    for (int i = 0; i < c.n_sph; i++) {
+        const float *s = desc->spheres + 4 * i;
+        h[L.sph + i] = make_float4(s[0], s[1], s[2], s[3]);
+    }
+    auto put_caps = [&](int off, const float *src, int n) {
+        for (int i = 0; i < n; i++) {
+            const float *s = src + 8 * i;
+            h[off + 2 * i] = make_float4(s[0], s[1], s[2], s[6]);     // x1 y1 z1 r
+            h[off + 2 * i + 1] = make_float4(s[3], s[4], s[5], s[7]); // xv yv zv rdv
+        }
+    };
+    put_caps(L.cap, desc->capsules, c.n_cap);
+    put_caps(L.zcap, desc->z_capsules, c.n_zcap);
+    auto put_cubs = [&](int off, const float *src, int n) {
+        for (int i = 0; i < n; i++) {
+            const float *s = src + 15 * i;
+            h[off + 4 * i] = make_float4(s[0], s[1], s[2], s[12]);    // centre, h1
+            h[off + 4 * i + 1] = make_float4(s[3], s[4], s[5], s[13]); // axis 1, h2
+            h[off + 4 * i + 2] = make_float4(s[6], s[7], s[8], s[14]); // axis 2, h3
+            h[off + 4 * i + 3] = make_float4(s[9], s[10], s[11], 0.f); // axis 3
+        }
+    };
+    put_cubs(L.cub, desc->cuboids, c.n_cub);
+    put_cubs(L.zcub, desc->z_cuboids, c.n_zcub);
+
+    mrpop_scene *sc = new (std::nothrow) mrpop_scene();
+    if (!sc) return fail(MRPOP_ERR_OUT_OF_MEMORY, "scene_create: host allocation");
+    sc->counts = c;
+    sc->total_f4 = L.total;
+    sc->env_test_flops = 27.0 * (c.n_cub + c.n_zcub) + 26.0 * (c.n_cap + c.n_zcap) + 11.0 * c.n_sph;
+    cudaGetDevice(&sc->device);
+    cudaError_t e = cudaMalloc(&sc->d_status, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemset(sc->d_status, 0, sizeof(unsigned int));
+    if (e == cudaSuccess && L.total > 0) e = cudaMalloc(&sc->d_buf, (size_t)L.total * sizeof(float4));
+    if (e == cudaSuccess && L.total > 0)
+        e = cudaMemcpy(sc->d_buf, h.data(), (size_t)L.total * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(sc->d_buf);
+        cudaFree(sc->d_status);
+        delete sc;
+        return cuda_fail(e, "scene_create");
+    }
+    *out = sc;
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_scene_destroy(mrpop_scene *scene) {
+    if (!scene) return MRPOP_OK;
+    cudaFree(scene->d_buf);
+    cudaFree(scene->d_status);
+    delete scene;
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_scene_status(const mrpop_scene *scene, uint32_t *status_out) {
+    if (!scene || !status_out) return fail(MRPOP_ERR_INVALID_ARGUMENT, "scene_status: null argument");
+    unsigned int v = 0;
+    MRPOP_CUDA(cudaMemcpy(&v, scene->d_status, sizeof(v), cudaMemcpyDeviceToHost), "scene_status");
+    *status_out = v;
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_robotset_create(int n_arms, const float *base_T, mrpop_robotset **out) {
+    if (!out) return fail(MRPOP_ERR_INVALID_ARGUMENT, "robotset_create: null out");
+    *out = nullptr;
+    if (n_arms < 1 || n_arms > MRPOP_MAX_ARMS)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "robotset_create: n_arms must be 1..5");
+    const float *src = base_T;
+    static const float kIdent[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    if (!src) {
+        if (n_arms == 1) src = kIdent;
+        else if (n_arms == 4) src = &kQuadBase[0][0];
+        else if (n_arms == 5) src = &kFiveBase[0][0];
+        else
+            return fail(MRPOP_ERR_INVALID_ARGUMENT,
+                        "robotset_create: the reference has no built-in layout for this arm count");
+    }
+    mrpop_robotset *r = new (std::nothrow) mrpop_robotset();
+    if (!r) return fail(MRPOP_ERR_OUT_OF_MEMORY, "robotset_create: host allocation");
+    r->n_arms = n_arms;
+    for (int a = 0; a < n_arms; a++)
+        for (int i = 0; i < 12; i++) r->base[a][i] = src[16 * a + i];
+    *out = r;
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_robotset_destroy(mrpop_robotset *robots) {
+    delete robots;
+    return MRPOP_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
+                           const float *q1, int64_t n_edges, int g, int rule, float range, uint32_t flags,
+                           int arm, uint8_t *valid, int32_t *first_hit, int32_t *n_seg_out, double *flops,
+                           cudaStream_t stream) {
+    if (!scene || !robots) return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: null scene or robots");
+    if (n_edges < 0) return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: n_edges < 0");
+    if (n_edges == 0) return MRPOP_OK;
+    if (!q0 || !q1 || ((!valid || !first_hit) && !flops))
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: null device pointer");
+    if (g < 1 || g > MRPOP_MAX_GRANULARITY)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: granularity must be 1..64");
+    if (rule < MRPOP_RULE_PLAIN || rule > MRPOP_RULE_SHORTCUT)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: unknown segmentation rule");
+    if (rule != MRPOP_RULE_PLAIN && !(range > 0.0f))
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: range must be > 0");
+    if (flags & ~(MRPOP_CHECK_ENV | MRPOP_CHECK_SELF | MRPOP_MODE_EXACT))
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: unknown flag bits");
+    if (arm >= robots->n_arms) return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: arm out of range");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != scene->device) return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: scene lives on another device");
+
+    mrpop::EdgeParams p{};
+    p.q0 = q0;
+    p.q1 = q1;
+    p.n_edges = n_edges;
+    p.g = g;
+    p.flags = (int)flags;
+    p.single = arm >= 0 ? 1 : 0;
+    p.rule = rule;
+    p.range = range;
+    p.valid = valid;
+    p.first_hit = first_hit;
+    p.n_seg_out = n_seg_out;
+    p.flops = flops;
+    p.scene = scene->d_buf;
+    p.sc = scene->counts;
+    p.status = scene->d_status;
+    p.env_test_flops = scene->env_test_flops;
+    const int A = arm >= 0 ? 1 : robots->n_arms;
+    for (int a = 0; a < A; a++)
+        for (int i = 0; i < 12; i++) p.base[a][i] = robots->base[arm >= 0 ? arm : a][i];
+    double fbp = A * (7.0 * 81.0 + 11.0 * 18.0);
+    if (flags & MRPOP_CHECK_ENV) fbp += A * 10.0 * scene->env_test_flops;
+    if (flags & MRPOP_CHECK_SELF) fbp += A * 21.0 * 11.0 + (A * (A - 1) / 2) * 121.0 * 11.0;
+    p.fbp = fbp;
+
+    // scratch outputs when only the tally is wanted
+    uint8_t *tmp_valid = nullptr;
+    int32_t *tmp_first = nullptr;
+    if (!valid || !first_hit) {
+        MRPOP_CUDA(cudaMallocAsync(&tmp_valid, (size_t)n_edges, stream), "validate: tally scratch");
+        MRPOP_CUDA(cudaMallocAsync(&tmp_first, (size_t)n_edges * 4, stream), "validate: tally scratch");
+        p.valid = tmp_valid;
+        p.first_hit = tmp_first;
+    }
+    const size_t smem = (size_t)scene->total_f4 * sizeof(float4) + warp_scratch_bytes();
+    cudaError_t err = mrpop::launch_validate(A, p, smem, stream);
+    if (tmp_valid) cudaFreeAsync(tmp_valid, stream);
+    if (tmp_first) cudaFreeAsync(tmp_first, stream);
+    if (err != cudaSuccess) return cuda_fail(err, "validate: launch");
+    return MRPOP_OK;
+}
+
+struct Base12 {
+    float m[12];
+};
+
+__global__ void fk_spheres_kernel(const float *q, long long n, int detailed, const Base12 base, float *out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    float b[12];
+    for (int i = 0; i < 12; i++) b[i] = base.m[i];
+    float qq[7];
+    for (int d = 0; d < 7; d++) qq[d] = q[t * 7 + d];
+    if (!detailed) {
+        float px[mrpop::kNumApprox], py[mrpop::kNumApprox], pz[mrpop::kNumApprox];
+        mrpop::fk_approx_arm(b, qq, px, py, pz);
+        for (int i = 0; i < mrpop::kNumApprox; i++) {
+            out[(t * mrpop::kNumApprox + i) * 3 + 0] = px[i];
+            out[(t * mrpop::kNumApprox + i) * 3 + 1] = py[i];
+            out[(t * mrpop::kNumApprox + i) * 3 + 2] = pz[i];
+        }
+        return;
+    }
+    // detailed: the narrow phase's run-time path (joint chain + placement)
+    float Tj[mrpop::kNumJoints][12];
+    mrpop::Xf T;
+    mrpop::load_base(T, b);
+    for (int i = 0; i < 12; i++) Tj[0][i] = T.m[i];
+    for (int j = 1; j < mrpop::kNumJoints; j++) {
+        mrpop::joint_step_rt(T, qq[j - 1], j);
+        for (int i = 0; i < 12; i++) Tj[j][i] = T.m[i];
+    }
+    for (int i = 0; i < mrpop::kNumDet; i++) {
+        const float3 p = mrpop::place_rt(Tj[mrpop::det_joint(i)], mrpop::c_det[i]);
+        out[(t * mrpop::kNumDet + i) * 3 + 0] = p.x;
+        out[(t * mrpop::kNumDet + i) * 3 + 1] = p.y;
+        out[(t * mrpop::kNumDet + i) * 3 + 2] = p.z;
+    }
+}
+
+__global__ void trig_kernel(const float *x, long long n, float *c, float *s) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const float v = x[t];
+    c[t] = __cosf(v);
+    s[t] = __sinf(v);
+}
+
+}  // namespace
+
+namespace mrpop {
+cudaError_t launch_validate(int arms, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream) {
+    switch (arms) {
+    case 1: return launch_validate_arms<1>(p, smem_bytes, stream);
+    case 2: return launch_validate_arms<2>(p, smem_bytes, stream);
+    case 3: return launch_validate_arms<3>(p, smem_bytes, stream);
+    case 4: return launch_validate_arms<4>(p, smem_bytes, stream);
+    case 5: return launch_validate_arms<5>(p, smem_bytes, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+}  // namespace mrpop
+
+extern "C" {
+
+mrpop_status mrpop_validate_edges(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
+                                  const float *q1, int64_t n_edges, int granularity, uint32_t flags, int arm,
+                                  uint8_t *valid, int32_t *first_hit, void *stream) {
+    return run_validator(scene, robots, q0, q1, n_edges, granularity, MRPOP_RULE_PLAIN, 0.0f, flags, arm, valid,
+                         first_hit, nullptr, nullptr, (cudaStream_t)stream);
+}
+
+mrpop_status mrpop_validate_segments(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
+                                     const float *q1, int64_t n_edges, int granularity, int rule, float range,
+                                     uint32_t flags, int arm, uint8_t *valid, int32_t *first_hit,
+                                     int32_t *n_seg_out, void *stream) {
+    return run_validator(scene, robots, q0, q1, n_edges, granularity, rule, range, flags, arm, valid, first_hit,
+                         n_seg_out, nullptr, (cudaStream_t)stream);
+}
+
+mrpop_status mrpop_count_flops(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
+                               const float *q1, int64_t n_edges, int granularity, int rule, float range,
+                               uint32_t flags, int arm, double *flops, void *stream) {
+    if (!flops) return fail(MRPOP_ERR_INVALID_ARGUMENT, "count_flops: null output");
+    return run_validator(scene, robots, q0, q1, n_edges, granularity, rule, range, flags, arm, nullptr, nullptr,
+                         nullptr, flops, (cudaStream_t)stream);
+}
+
+mrpop_status mrpop_fk_spheres(const mrpop_robotset *robots, int arm, const float *q, int64_t n, int detailed,
+                              float *out, void *stream) {
+    if (!robots || !q || !out) return fail(MRPOP_ERR_INVALID_ARGUMENT, "fk_spheres: null argument");
+    if (arm < 0 || arm >= robots->n_arms) return fail(MRPOP_ERR_INVALID_ARGUMENT, "fk_spheres: arm out of range");
+    if (n <= 0) return MRPOP_OK;
+    Base12 b;
+    for (int i = 0; i < 12; i++) b.m[i] = robots->base[arm][i];
+    const int tpb = 128;
+    fk_spheres_kernel<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, (cudaStream_t)stream>>>(q, n, detailed, b, out);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return cuda_fail(err, "fk_spheres: launch");
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_debug_trig(const float *x, int64_t n, float *cos_out, float *sin_out, void *stream) {
+    if (!x || !cos_out || !sin_out) return fail(MRPOP_ERR_INVALID_ARGUMENT, "debug_trig: null argument");
+    if (n <= 0) return MRPOP_OK;
+    const int tpb = 256;
+    trig_kernel<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, (cudaStream_t)stream>>>(x, n, cos_out, sin_out);
+    MRPOP_CUDA(cudaGetLastError(), "debug_trig: launch");
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_workspace_create(mrpop_workspace **out) {
+    if (!out) return fail(MRPOP_ERR_INVALID_ARGUMENT, "workspace_create: null out");
+    mrpop_workspace *w = new (std::nothrow) mrpop_workspace();
+    if (!w) return fail(MRPOP_ERR_OUT_OF_MEMORY, "workspace_create: host allocation");
+    cudaGetDevice(&w->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete w;
+        return cuda_fail(e, "workspace_create");
+    }
+    *out = w;
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_workspace_destroy(mrpop_workspace *ws) {
+    if (!ws) return MRPOP_OK;
+    cudaStreamSynchronize(ws->stream);
+    cudaFree(ws->d_q0);
+    cudaFree(ws->d_q1);
+    cudaFree(ws->d_valid);
+    cudaFree(ws->d_first);
+    cudaStreamDestroy(ws->stream);
+    delete ws;
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_validate_edges_host(mrpop_workspace *ws, const mrpop_scene *scene, const mrpop_robotset *robots,
+                                       const float *q0, const float *q1, int64_t n_edges, int granularity,
+                                       uint32_t flags, int arm, int rule, float range, uint8_t *valid,
+                                       int32_t *first_hit) {
+    if (!ws || !robots) return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate_edges_host: null argument");
+    if (n_edges <= 0) return n_edges == 0 ? MRPOP_OK : fail(MRPOP_ERR_INVALID_ARGUMENT, "n_edges < 0");
+    if (!q0 || !q1 || !valid || !first_hit)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate_edges_host: null host pointer");
+    const int dof = 7 * (arm >= 0 ? 1 : robots->n_arms);
+    const size_t ncfg = (size_t)n_edges * dof;
+    if (ncfg > ws->cap_cfg) {
+        cudaFree(ws->d_q0);
+        cudaFree(ws->d_q1);
+        ws->d_q0 = ws->d_q1 = nullptr;
+        ws->cap_cfg = 0;
+        MRPOP_CUDA(cudaMalloc(&ws->d_q0, ncfg * sizeof(float)), "validate_edges_host: alloc");
+        MRPOP_CUDA(cudaMalloc(&ws->d_q1, ncfg * sizeof(float)), "validate_edges_host: alloc");
+        ws->cap_cfg = ncfg;
+    }
+    if ((size_t)n_edges > ws->cap_edges) {
+        cudaFree(ws->d_valid);
+        cudaFree(ws->d_first);
+        ws->d_valid = nullptr;
+        ws->d_first = nullptr;
+        ws->cap_edges = 0;
+        MRPOP_CUDA(cudaMalloc(&ws->d_valid, (size_t)n_edges), "validate_edges_host: alloc");
+        MRPOP_CUDA(cudaMalloc(&ws->d_first, (size_t)n_edges * 4), "validate_edges_host: alloc");
+        ws->cap_edges = (size_t)n_edges;
+    }
+    cudaStream_t st = ws->stream;
+    MRPOP_CUDA(cudaMemcpyAsync(ws->d_q0, q0, ncfg * sizeof(float), cudaMemcpyHostToDevice, st), "H2D q0");
+    MRPOP_CUDA(cudaMemcpyAsync(ws->d_q1, q1, ncfg * sizeof(float), cudaMemcpyHostToDevice, st), "H2D q1");
+    mrpop_status s = run_validator(scene, robots, ws->d_q0, ws->d_q1, n_edges, granularity, rule, range, flags, arm,
+                                   ws->d_valid, ws->d_first, nullptr, nullptr, st);
+    if (s != MRPOP_OK) return s;
+    MRPOP_CUDA(cudaMemcpyAsync(valid, ws->d_valid, (size_t)n_edges, cudaMemcpyDeviceToHost, st), "D2H valid");
+    MRPOP_CUDA(cudaMemcpyAsync(first_hit, ws->d_first, (size_t)n_edges * 4, cudaMemcpyDeviceToHost, st),
+               "D2H first_hit");
+    MRPOP_CUDA(cudaStreamSynchronize(st), "validate_edges_host: sync");
+    return MRPOP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,605 @@
+// edge_kernel.cuh -- the batched edge validator (sm_103a).
+//
+// One warp owns one edge at a time (persistent grid, warp-strided over the
+// batch).  Lane L evaluates samples k = L+1 (+32) of the edge:
+//   broad phase  per lane: FK of every arm (FP32 FMA, __sinf/__cosf as the
+//                reference), the 11 broad-phase spheres per arm against the
+//                scene staged in shared memory (one bulk-async copy per CTA),
+//                the intra-arm pairs and the arm-vs-arm pairs; the result is a
+//                per-(arm, joint) flag word and per-sample sphere counts.
+//   decision     per warp: shuffle reductions give the edge totals; the
+//                reference's proportional 4g-thread split (utils.cuh:476-517)
+//                is evaluated exactly to pick the samples that get a detailed
+//                check (or every flagged sample in EXACT mode).
+//   narrow phase per warp, one sample at a time in increasing k: lanes rebuild
+//                the joint frames of that sample, place the 59 detailed
+//                spheres per arm in shared memory and split the flagged env and
+//                self tests over the lanes; a warp vote ends the edge at the
+//                first colliding sample.
+#pragma once
+#include "panda_model.cuh"
+
+namespace mrpop {
+
+constexpr int kWarpsPerBlock = 4;
+constexpr int kMaxArms = 5;
+constexpr int kMaxDof = 7 * kMaxArms;
+
+struct SceneCounts {
+    int n_sph, n_cap, n_zcap, n_cub, n_zcub;
+};
+
+// Float4 offsets of each obstacle class inside the packed scene buffer.
+struct SceneLayout {
+    int sph, cap, zcap, cub, zcub, total; // in float4 units
+};
+
+__host__ __device__ inline SceneLayout scene_layout(const SceneCounts &c) {
+    SceneLayout l;
+    l.sph = 0;
+    l.cap = l.sph + c.n_sph;
+    l.zcap = l.cap + 2 * c.n_cap;
+    l.cub = l.zcap + 2 * c.n_zcap;
+    l.zcub = l.cub + 4 * c.n_cub;
+    l.total = l.zcub + 4 * c.n_zcub;
+    return l;
+}
+
+struct EdgeParams {
+    const float *q0;
+    const float *q1;
+    long long n_edges;
+    int g;           // samples per segment
+    int flags;       // MRPOP_CHECK_* | MRPOP_MODE_EXACT
+    int single;      // 1: single-arm (fkcc_single_buffer_mr) semantics
+    int rule;        // MRPOP_RULE_*
+    float range;
+    uint8_t *valid;
+    int32_t *first_hit;
+    int32_t *n_seg_out;
+    double *flops;   // optional per-edge algorithmic flop tally
+    double fbp;      // broad-phase flops per sample (for the tally)
+    double env_test_flops;
+    const float4 *scene;
+    SceneCounts sc;
+    unsigned int *status;
+    float base[kMaxArms][12]; // row-major 3x4 per arm of this check
+};
+
+// Per-warp shared scratch.
+struct WarpScratch {
+    float base[kMaxDof];   // segment start (accumulated for CONNECT)
+    float stepg[kMaxDof];  // per-sample step (delta/g or vec/g)
+    float delta[kMaxDof];  // per-segment step (B-spline / shortcut accumulation)
+    float T[kMaxArms][kNumJoints][12];
+    float4 P[kMaxArms][kNumDet]; // detailed sphere centres (w = radius)
+};
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kEnvBit = 1, kSelfBit = 2, kExactBit = 16;
+constexpr int kRulePlain = 0, kRuleConnect = 1, kRuleBspline = 2, kRuleShortcut = 3;
+constexpr int kMaxSegments = 1 << 16;
+
+// ---------------------------------------------------------------------------
+// shared-memory staging of the scene: one bulk asynchronous copy (TMA engine)
+// completed on an mbarrier, with a bounded wait.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ bool stage_scene(float4 *dst, const float4 *src, uint32_t bytes,
+                                            uint64_t *bar, unsigned int *status) {
+    bool ok = true;
+    if (bytes == 0) return true;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                     "r"(bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_u32(dst)),
+            "l"(src), "r"(bytes), "r"(smem_u32(bar))
+            : "memory");
+    }
+    // bounded wait on phase 0
+    uint32_t done = 0;
+    for (int it = 0; it < (1 << 22) && !done; it++) {
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(smem_u32(bar))
+            : "memory");
+    }
+    if (!done) {
+        atomicOr(status, 1u);
+        ok = false;
+    }
+    return __syncthreads_and(ok);
+}
+
+// ---------------------------------------------------------------------------
+// scene queries against the staged copy (uniform loops: obstacle data is a
+// shared-memory broadcast, spheres live in registers)
+// ---------------------------------------------------------------------------
+// Broad phase: approx spheres 1..10 of one arm; returns a bitmask over sphere
+// index (bit i set = sphere i touches some obstacle).
+__device__ __forceinline__ uint32_t env_mask_approx(const float4 *S, const SceneLayout &L,
+                                                    const SceneCounts &C, const float (&px)[kNumApprox],
+                                                    const float (&py)[kNumApprox],
+                                                    const float (&pz)[kNumApprox]) {
+    uint32_t m = 0;
+    float rsq[kNumApprox];
+#pragma unroll
+    for (int i = 1; i < kNumApprox; i++) rsq[i] = __fmul_rn(c_approx[i].w, c_approx[i].w);
+    for (int o = 0; o < C.n_cub; o++) {
+        const float4 c0 = S[L.cub + 4 * o], c1 = S[L.cub + 4 * o + 1], c2 = S[L.cub + 4 * o + 2],
+                     c3 = S[L.cub + 4 * o + 3];
+#pragma unroll
+        for (int i = 1; i < kNumApprox; i++)
+            if (hit_cuboid(c0, c1, c2, c3, px[i], py[i], pz[i], rsq[i])) m |= 1u << i;
+    }
+    for (int o = 0; o < C.n_zcub; o++) {
+        const float4 c0 = S[L.zcub + 4 * o], c1 = S[L.zcub + 4 * o + 1], c2 = S[L.zcub + 4 * o + 2];
+#pragma unroll
+        for (int i = 1; i < kNumApprox; i++)
+            if (hit_zcuboid(c0, c1, c2, px[i], py[i], pz[i], rsq[i])) m |= 1u << i;
+    }
+    for (int o = 0; o < C.n_cap; o++) {
+        const float4 c0 = S[L.cap + 2 * o], c1 = S[L.cap + 2 * o + 1];
+#pragma unroll
+        for (int i = 1; i < kNumApprox; i++)
+            if (hit_capsule(c0, c1, px[i], py[i], pz[i], c_approx[i].w)) m |= 1u << i;
+    }
+    for (int o = 0; o < C.n_zcap; o++) {
+        const float4 c0 = S[L.zcap + 2 * o], c1 = S[L.zcap + 2 * o + 1];
+#pragma unroll
+        for (int i = 1; i < kNumApprox; i++)
+            if (hit_zcapsule(c0, c1, px[i], py[i], pz[i], c_approx[i].w)) m |= 1u << i;
+    }
+    for (int o = 0; o < C.n_sph; o++) {
+        const float4 c0 = S[L.sph + o];
+#pragma unroll
+        for (int i = 1; i < kNumApprox; i++)
+            if (hit_sphere_sphere(c0.x, c0.y, c0.z, c0.w, px[i], py[i], pz[i], c_approx[i].w)) m |= 1u << i;
+    }
+    return m;
+}
+
+// One sphere against the whole scene (narrow phase).
+__device__ __forceinline__ bool env_hit_one(const float4 *S, const SceneLayout &L, const SceneCounts &C,
+                                            float x, float y, float z, float r) {
+    const float rsq = __fmul_rn(r, r);
+    for (int o = 0; o < C.n_cub; o++)
+        if (hit_cuboid(S[L.cub + 4 * o], S[L.cub + 4 * o + 1], S[L.cub + 4 * o + 2], S[L.cub + 4 * o + 3], x, y,
+                       z, rsq))
+            return true;
+    for (int o = 0; o < C.n_zcub; o++)
+        if (hit_zcuboid(S[L.zcub + 4 * o], S[L.zcub + 4 * o + 1], S[L.zcub + 4 * o + 2], x, y, z, rsq))
+            return true;
+    for (int o = 0; o < C.n_cap; o++)
+        if (hit_capsule(S[L.cap + 2 * o], S[L.cap + 2 * o + 1], x, y, z, r)) return true;
+    for (int o = 0; o < C.n_zcap; o++)
+        if (hit_zcapsule(S[L.zcap + 2 * o], S[L.zcap + 2 * o + 1], x, y, z, r)) return true;
+    for (int o = 0; o < C.n_sph; o++) {
+        const float4 c0 = S[L.sph + o];
+        if (hit_sphere_sphere(c0.x, c0.y, c0.z, c0.w, x, y, z, r)) return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// FK of one arm for one sample: approx sphere centres in registers
+// ---------------------------------------------------------------------------
+template <int I>
+__device__ __forceinline__ void place_approx(const Xf &T, float (&px)[kNumApprox], float (&py)[kNumApprox],
+                                             float (&pz)[kNumApprox]) {
+    px[I] = place_coord<I, false>(T, 0);
+    py[I] = place_coord<I, false>(T, 1);
+    pz[I] = place_coord<I, false>(T, 2);
+}
+
+__device__ __forceinline__ void fk_approx_arm(const float *base12, const float (&q)[7], float (&px)[kNumApprox],
+                                              float (&py)[kNumApprox], float (&pz)[kNumApprox]) {
+    Xf T;
+    load_base(T, base12);
+    place_approx<0>(T, px, py, pz);
+    joint_step<1>(T, q[0]);
+    place_approx<1>(T, px, py, pz);
+    joint_step<2>(T, q[1]);
+    place_approx<2>(T, px, py, pz);
+    joint_step<3>(T, q[2]);
+    place_approx<3>(T, px, py, pz);
+    joint_step<4>(T, q[3]);
+    place_approx<4>(T, px, py, pz);
+    joint_step<5>(T, q[4]);
+    place_approx<5>(T, px, py, pz);
+    joint_step<6>(T, q[5]);
+    place_approx<6>(T, px, py, pz);
+    joint_step<7>(T, q[6]);
+    place_approx<7>(T, px, py, pz);
+    place_approx<8>(T, px, py, pz);
+    place_approx<9>(T, px, py, pz);
+    place_approx<10>(T, px, py, pz);
+}
+
+// Joint values of arm `a` for sample k of segment `seg` (call-site formulas,
+// see the rule constants).
+__device__ __forceinline__ void sample_q(const WarpScratch &W, int rule, int seg, int a, int k, float (&q)[7]) {
+    const float fk = (float)k;
+#pragma unroll
+    for (int d = 0; d < 7; d++) {
+        const int i = 7 * a + d;
+        float v = __fmaf_rn(fk, W.stepg[i], W.base[i]);
+        if (rule == kRuleBspline || rule == kRuleShortcut)
+            for (int s = 0; s < seg; s++) v = __fadd_rn(v, W.delta[i]);
+        q[d] = v;
+    }
+}
+
+// Broad phase of one sample: env / self flag words (bit 8a+j) and counts.
+template <int A>
+__device__ __forceinline__ void broad_sample(const EdgeParams &P, const WarpScratch &W, const float4 *S,
+                                             const SceneLayout &L, int seg, int k, uint64_t &envw,
+                                             uint64_t &selfw) {
+    envw = 0;
+    selfw = 0;
+    const bool do_env = P.flags & kEnvBit, do_self = P.flags & kSelfBit;
+#pragma unroll 1
+    for (int b = 0; b < A; b++) {
+        float q[7];
+        sample_q(W, P.rule, seg, P.single ? 0 : b, k, q);
+        float px[kNumApprox], py[kNumApprox], pz[kNumApprox];
+        fk_approx_arm(P.base[b], q, px, py, pz);
+        if (do_env) {
+            const uint32_t m = env_mask_approx(S, L, P.sc, px, py, pz);
+            uint32_t jm = 0;
+#pragma unroll
+            for (int i = 1; i < kNumApprox; i++)
+                if (m >> i & 1u) jm |= 1u << approx_joint(i);
+            envw |= (uint64_t)jm << (8 * b);
+        }
+        if (do_self) {
+            uint32_t jm = 0;
+            // intra-arm rows (panda_multi_geometry.cuh:133-139)
+#define MRPOP_INTRA(s1, j)                                                                                 \
+    if (hit_sphere_sphere(px[s1], py[s1], pz[s1], c_approx[s1].w, px[j], py[j], pz[j], c_approx[j].w))    \
+        jm |= 1u << approx_joint(s1);
+#pragma unroll
+            for (int j = 5; j <= 10; j++) { MRPOP_INTRA(0, j) MRPOP_INTRA(1, j) }
+            MRPOP_INTRA(2, 5)
+#pragma unroll
+            for (int j = 7; j <= 10; j++) { MRPOP_INTRA(2, j) MRPOP_INTRA(5, j) }
+#undef MRPOP_INTRA
+            selfw |= (uint64_t)jm << (8 * b);
+            // arm-vs-arm against every lower arm a < b; flags go to arm a
+            // (panda_four.cuh:178-214)
+#pragma unroll 1
+            for (int a = 0; a < b; a++) {
+                float qa[7];
+                sample_q(W, P.rule, seg, a, k, qa);
+                float ax[kNumApprox], ay[kNumApprox], az[kNumApprox];
+                fk_approx_arm(P.base[a], qa, ax, ay, az);
+                uint32_t am = 0;
+#pragma unroll
+                for (int i = 0; i < kNumApprox; i++) {
+                    bool h = false;
+#pragma unroll
+                    for (int j = 0; j < kNumApprox; j++)
+                        h |= hit_sphere_sphere(ax[i], ay[i], az[i], c_approx[i].w, px[j], py[j], pz[j], c_approx[j].w);
+                    if (h) am |= 1u << approx_joint(i);
+                }
+                selfw |= (uint64_t)am << (8 * a);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ int flag_count(uint64_t w) {
+    int n = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const uint64_t col = (w >> j) & 0x0101010101ull; // joint j of arms 0..4
+        n += det_count(j) * __popcll(col);
+    }
+    return n;
+}
+
+// reference thread split (utils.cuh:478-497): share of 4g threads, truncated
+__device__ __forceinline__ int ref_share(int cnt, int total, int g) {
+    if (total == 0) return 0; // 0/0 is NaN on the device; its int conversion is 0
+    return __float2int_rz(__fmul_rn(__fdiv_rn((float)cnt, (float)total), (float)(4 * g)));
+}
+
+// dense narrow-phase tally for one sample (per the flop convention)
+__device__ __forceinline__ double narrow_flops(const EdgeParams &P, int A, uint64_t envw, uint64_t selfw,
+                                               bool de, bool ds) {
+    double f = 0.0;
+    const bool quirk = !P.single && !(P.flags & kExactBit);
+    for (int a = 0; a < A; a++) {
+        const uint32_t em = de ? (uint32_t)(envw >> (8 * a)) & 0xffu : 0u;
+        const uint32_t sm = ds ? (uint32_t)(selfw >> (8 * a)) & 0xffu : 0u;
+        for (int j = 0; j < 8; j++) {
+            if ((em | sm) >> j & 1u) f += 18.0 * det_count(j);
+            if (em >> j & 1u) f += P.env_test_flops * (j == 0 ? 0 : det_count(j));
+        }
+        if (sm) {
+            for (int r = 0; r < kDetRows; r++) {
+                const int idx = quirk ? r : det_row_first(r);
+                if (sm >> det_joint(idx) & 1u) f += 11.0 * (det_row_hi(r) - det_row_lo(r) + 1);
+            }
+            for (int j = 0; j < 8; j++)
+                if (sm >> j & 1u) f += 11.0 * kNumDet * (A - 1 - a) * det_count(j);
+        }
+    }
+    return f;
+}
+
+// ---------------------------------------------------------------------------
+// narrow phase of one sample (whole warp)
+// ---------------------------------------------------------------------------
+template <int A>
+__device__ __noinline__ bool narrow_sample(const EdgeParams &P, WarpScratch &W, const float4 *S,
+                                           const SceneLayout &L, const float4 *det_tab, int seg, int k,
+                                           uint64_t envw, uint64_t selfw, bool de, bool ds) {
+    const int lane = threadIdx.x & 31;
+    // joint frames of every arm
+    if (lane < A) {
+        float q[7];
+        sample_q(W, P.rule, seg, P.single ? 0 : lane, k, q);
+        Xf T;
+        load_base(T, P.base[lane]);
+#pragma unroll
+        for (int i = 0; i < 12; i++) W.T[lane][0][i] = T.m[i];
+#pragma unroll
+        for (int j = 1; j < kNumJoints; j++) {
+            joint_step_rt(T, q[j - 1], j);
+#pragma unroll
+            for (int i = 0; i < 12; i++) W.T[lane][j][i] = T.m[i];
+        }
+    }
+    __syncwarp();
+    for (int idx = lane; idx < A * kNumDet; idx += 32) {
+        const int a = idx / kNumDet, i = idx - a * kNumDet;
+        const float4 s = det_tab[i];
+        const float3 p = place_rt(W.T[a][det_joint(i)], s);
+        W.P[a][i] = make_float4(p.x, p.y, p.z, s.w);
+    }
+    __syncwarp();
+    bool hit = false;
+    if (de) {
+        for (int idx = lane; idx < A * kNumDet; idx += 32) {
+            const int a = idx / kNumDet, i = idx - a * kNumDet;
+            if (i > 0 && (envw >> (8 * a + det_joint(i)) & 1ull)) {
+                const float4 p = W.P[a][i];
+                hit |= env_hit_one(S, L, P.sc, p.x, p.y, p.z, p.w);
+            }
+        }
+        if (__any_sync(kFull, hit)) return true;
+    }
+    if (ds) {
+        const bool quirk = !P.single && !(P.flags & kExactBit);
+        const int rows = A * kDetRows + A * kNumDet;
+        for (int idx = lane; idx < rows; idx += 32) {
+            if (idx < A * kDetRows) {
+                const int a = idx / kDetRows, r = idx - a * kDetRows;
+                const int s1 = det_row_first(r);
+                const int pi = quirk ? r : s1; // composite robots read sphere r (panda_four.cuh:390-401)
+                if (!(selfw >> (8 * a + det_joint(pi)) & 1ull)) continue;
+                const float4 p = W.P[a][pi];
+                const float r1 = W.P[a][s1].w;
+                for (int j = det_row_lo(r); j <= det_row_hi(r); j++) {
+                    const float4 o = W.P[a][j];
+                    hit |= hit_sphere_sphere(p.x, p.y, p.z, r1, o.x, o.y, o.z, o.w);
+                }
+            } else {
+                const int t = idx - A * kDetRows;
+                const int a = t / kNumDet, i = t - a * kNumDet;
+                if (!(selfw >> (8 * a + det_joint(i)) & 1ull)) continue;
+                const float4 p = W.P[a][i];
+                for (int b = a + 1; b < A; b++)
+                    for (int j = 0; j < kNumDet; j++) {
+                        const float4 o = W.P[b][j];
+                        hit |= hit_sphere_sphere(p.x, p.y, p.z, p.w, o.x, o.y, o.z, o.w);
+                    }
+            }
+        }
+        if (__any_sync(kFull, hit)) return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// the kernel
+// ---------------------------------------------------------------------------
+template <int A, int SPL>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
+    validate_kernel(const __grid_constant__ EdgeParams P) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ float4 det_tab[kNumDet];
+
+    const SceneLayout L = scene_layout(P.sc);
+    float4 *S = reinterpret_cast<float4 *>(smem_raw);
+    WarpScratch *Wall = reinterpret_cast<WarpScratch *>(smem_raw + (size_t)L.total * sizeof(float4));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    WarpScratch &W = Wall[warp];
+
+    for (int i = threadIdx.x; i < kNumDet; i += blockDim.x) det_tab[i] = c_det[i];
+    const bool staged = stage_scene(S, P.scene, (uint32_t)(L.total * sizeof(float4)), &bar, P.status);
+
+    const int g = P.g;
+    const int dof = 7 * (P.single ? 1 : A);
+    const long long nwarps = (long long)gridDim.x * kWarpsPerBlock;
+
+    for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps) {
+        if (!staged) {
+            if (lane == 0) {
+                P.valid[e] = 0;
+                P.first_hit[e] = -2;
+            }
+            continue;
+        }
+        // edge set-up: per-dof segment start and steps in warp scratch
+        const float *qa = P.q0 + e * dof, *qb = P.q1 + e * dof;
+        float diff0 = 0.f, diff1 = 0.f;
+        if (lane < dof) diff0 = __fsub_rn(qb[lane], qa[lane]);
+        if (lane + 32 < dof) diff1 = __fsub_rn(qb[lane + 32], qa[lane + 32]);
+        int nseg = 1;
+        bool too_many = false;
+        if (P.rule != kRulePlain) {
+            // |q1 - q0| with the reference's sequential FMA chain (utils.cuh:123-133)
+            float acc = 0.0f;
+            for (int d = 0; d < dof; d++) {
+                const float v = __shfl_sync(kFull, d < 32 ? diff0 : diff1, d & 31);
+                acc = __fmaf_rn(v, v, acc);
+            }
+            const float dist = __fsqrt_rn(acc);
+            float n;
+            if (P.rule == kRuleConnect) n = truncf(__fdiv_rn(dist, P.range)) + 1.0f;
+            else if (P.rule == kRuleBspline) n = ceilf(__fdiv_rn(dist, P.range));
+            else n = ceilf(__fdiv_rn(__fsub_rn(dist, 0.001f), P.range));
+            if (n > (float)kMaxSegments) too_many = true;
+            else nseg = (int)n; // may be <= 0: no segment is checked (the reference's loop runs 0 times)
+        }
+        for (int d = lane; d < dof; d += 32) {
+            const float df = d < 32 ? diff0 : diff1;
+            W.base[d] = P.q0[e * dof + d];
+            if (P.rule == kRulePlain) {
+                W.stepg[d] = __fdiv_rn(df, (float)g);
+                W.delta[d] = 0.0f;
+            } else {
+                const float step = __fdiv_rn(df, (float)nseg);
+                W.delta[d] = step;
+                W.stepg[d] = __fdiv_rn(step, (float)g);
+            }
+        }
+        __syncwarp();
+
+        int first = 0;
+        double tally = 0.0;
+        const int nseg_run = too_many ? 0 : nseg;
+        for (int seg = 0; seg < nseg_run && first == 0; seg++) {
+            // ---- broad phase: this lane's samples
+            uint64_t envw[SPL], selfw[SPL];
+            int envc[SPL], selfc[SPL];
+            int tot_env = 0, tot_self = 0;
+#pragma unroll
+            for (int s = 0; s < SPL; s++) {
+                const int k = lane + 1 + 32 * s;
+                envw[s] = selfw[s] = 0;
+                if (k <= g) broad_sample<A>(P, W, S, L, seg, k, envw[s], selfw[s]);
+                envc[s] = flag_count(envw[s]);
+                selfc[s] = flag_count(selfw[s]);
+                tot_env += envc[s];
+                tot_self += selfc[s];
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                tot_env += __shfl_xor_sync(kFull, tot_env, o);
+                tot_self += __shfl_xor_sync(kFull, tot_self, o);
+            }
+            if (P.flops) tally += P.fbp * g;
+            if (tot_env == 0 && tot_self == 0) {
+                if (P.rule == kRuleConnect) {
+                    __syncwarp();
+                    for (int d = lane; d < dof; d += 32) W.base[d] = __fadd_rn(W.base[d], W.delta[d]);
+                    __syncwarp();
+                }
+                continue;
+            }
+            // ---- decision: which samples get the detailed check
+            uint64_t cand_env = 0, cand_self = 0;
+            const bool exact = P.flags & kExactBit;
+            if (exact) {
+#pragma unroll
+                for (int s = 0; s < SPL; s++) {
+                    const uint64_t be = __ballot_sync(kFull, envc[s] > 0);
+                    const uint64_t bs = __ballot_sync(kFull, selfc[s] > 0);
+                    cand_env |= be << (32 * s);
+                    cand_self |= bs << (32 * s);
+                }
+            } else {
+                int de[SPL], ds[SPL], sum_e = 0, sum_s = 0;
+#pragma unroll
+                for (int s = 0; s < SPL; s++) {
+                    const int k = lane + 1 + 32 * s;
+                    de[s] = k <= g ? ref_share(envc[s], tot_env, g) : 0;
+                    ds[s] = k <= g ? ref_share(selfc[s], tot_self, g) : 0;
+                    sum_e += de[s];
+                    sum_s += ds[s];
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    sum_e += __shfl_xor_sync(kFull, sum_e, o);
+                    sum_s += __shfl_xor_sync(kFull, sum_s, o);
+                }
+#pragma unroll
+                for (int s = 0; s < SPL; s++) {
+                    const int k = lane + 1 + 32 * s;
+                    if (k == g) { // the remainder goes to the last sample
+                        de[s] += 4 * g - sum_e;
+                        ds[s] += 4 * g - sum_s;
+                    }
+                    const uint64_t be = __ballot_sync(kFull, tot_env > 0 && de[s] > 0);
+                    const uint64_t bs = __ballot_sync(kFull, tot_self > 0 && ds[s] > 0);
+                    cand_env |= be << (32 * s);
+                    cand_self |= bs << (32 * s);
+                }
+            }
+            if (P.flops) {
+                double f = 0.0;
+#pragma unroll
+                for (int s = 0; s < SPL; s++) {
+                    const int bit = lane + 32 * s;
+                    const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
+                    if (dE || dS) f += narrow_flops(P, P.single ? 1 : A, envw[s], selfw[s], dE, dS);
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) f += __shfl_xor_sync(kFull, f, o);
+                tally += f;
+            }
+            // ---- narrow phase, samples in increasing order
+            uint64_t cand = cand_env | cand_self;
+            while (cand) {
+                const int bit = __ffsll((long long)cand) - 1;
+                cand &= cand - 1;
+                const int src = bit & 31, slot = bit >> 5;
+                uint64_t ew = 0, sw = 0;
+#pragma unroll
+                for (int s = 0; s < SPL; s++) {
+                    const uint64_t e2 = __shfl_sync(kFull, envw[s], src);
+                    const uint64_t s2 = __shfl_sync(kFull, selfw[s], src);
+                    if (s == slot) {
+                        ew = e2;
+                        sw = s2;
+                    }
+                }
+                const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
+                if (narrow_sample<A>(P, W, S, L, det_tab, seg, bit + 1, ew, sw, dE, dS)) {
+                    first = seg * g + bit + 1;
+                    break;
+                }
+            }
+            if (P.rule == kRuleConnect) {
+                __syncwarp();
+                for (int d = lane; d < dof; d += 32) W.base[d] = __fadd_rn(W.base[d], W.delta[d]);
+                __syncwarp();
+            }
+        }
+        if (lane == 0) {
+            P.valid[e] = (first == 0 && !too_many) ? 1 : 0;
+            P.first_hit[e] = too_many ? -2 : (first ? first : -1);
+            if (P.n_seg_out) P.n_seg_out[e] = nseg;
+            if (P.flops) P.flops[e] = tally;
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace mrpop

@@ -1,0 +1,279 @@
+"""Python host binding of the C ABI (include/mrpop.h) over ctypes.
+
+Device buffers are torch CUDA tensors (PyTorch is used for device memory and
+streams only); host-buffer calls take numpy arrays.  Every call goes through
+the compiled library: there is no Python or CPU fallback, and a missing
+library raises at load time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+CHECK_ENV = 0x1
+CHECK_SELF = 0x2
+MODE_EXACT = 0x10
+RULE_PLAIN, RULE_CONNECT, RULE_BSPLINE, RULE_SHORTCUT = 0, 1, 2, 3
+MAX_ARMS = 5
+MAX_GRANULARITY = 64
+
+STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "CUDA", 3: "UNSUPPORTED", 4: "OUT_OF_MEMORY", 5: "DEVICE_TIMEOUT"}
+
+EXPORTED = [
+    "mrpop_scene_create", "mrpop_scene_destroy", "mrpop_scene_status", "mrpop_robotset_create",
+    "mrpop_robotset_destroy", "mrpop_validate_edges", "mrpop_validate_segments", "mrpop_workspace_create",
+    "mrpop_workspace_destroy", "mrpop_validate_edges_host", "mrpop_fk_spheres", "mrpop_count_flops",
+    "mrpop_debug_trig", "mrpop_last_error", "mrpop_version",
+]
+
+
+class MrpopError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"mrpop {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [
+        ("spheres", C.c_void_p), ("num_spheres", C.c_uint32),
+        ("capsules", C.c_void_p), ("num_capsules", C.c_uint32),
+        ("z_capsules", C.c_void_p), ("num_z_capsules", C.c_uint32),
+        ("cylinders", C.c_void_p), ("num_cylinders", C.c_uint32),
+        ("cuboids", C.c_void_p), ("num_cuboids", C.c_uint32),
+        ("z_cuboids", C.c_void_p), ("num_z_cuboids", C.c_uint32),
+    ]
+
+
+_LIBS: dict[str, C.CDLL] = {}
+
+
+def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
+    """Load (not build) the compiled library; raises if it is missing."""
+    p = Path(path) if path else _build.lib_path(variant)
+    key = str(p)
+    if key in _LIBS:
+        return _LIBS[key]
+    if not p.exists():
+        raise FileNotFoundError(f"mrpop CUDA library not built: {p} (run __graft_entry__.build())")
+    lib = C.CDLL(str(p))
+    vp, i64, i32, u32, f32 = C.c_void_p, C.c_int64, C.c_int, C.c_uint32, C.c_float
+    sig = {
+        "mrpop_scene_create": [C.POINTER(SceneDesc), C.POINTER(vp)],
+        "mrpop_scene_destroy": [vp],
+        "mrpop_scene_status": [vp, C.POINTER(C.c_uint32)],
+        "mrpop_robotset_create": [i32, vp, C.POINTER(vp)],
+        "mrpop_robotset_destroy": [vp],
+        "mrpop_validate_edges": [vp, vp, vp, vp, i64, i32, u32, i32, vp, vp, vp],
+        "mrpop_validate_segments": [vp, vp, vp, vp, i64, i32, i32, f32, u32, i32, vp, vp, vp, vp],
+        "mrpop_workspace_create": [C.POINTER(vp)],
+        "mrpop_workspace_destroy": [vp],
+        "mrpop_validate_edges_host": [vp, vp, vp, vp, vp, i64, i32, u32, i32, i32, f32, vp, vp],
+        "mrpop_fk_spheres": [vp, i32, vp, i64, i32, vp, vp],
+        "mrpop_count_flops": [vp, vp, vp, vp, i64, i32, i32, f32, u32, i32, vp, vp],
+        "mrpop_debug_trig": [vp, i64, vp, vp, vp],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    lib.mrpop_last_error.restype = C.c_char_p
+    lib.mrpop_last_error.argtypes = []
+    lib.mrpop_version.restype = C.c_char_p
+    lib.mrpop_version.argtypes = []
+    _LIBS[key] = lib
+    return lib
+
+
+def _check(lib: C.CDLL, status: int) -> None:
+    if status != 0:
+        raise MrpopError(status, lib.mrpop_last_error().decode())
+
+
+def _f32(a, cols: int) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, cols))
+    return a
+
+
+@dataclass
+class SceneArrays:
+    """Obstacles as packed float32 records (field order of include/mrpop.h)."""
+    spheres: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.float32))
+    capsules: np.ndarray = field(default_factory=lambda: np.zeros((0, 8), np.float32))
+    z_capsules: np.ndarray = field(default_factory=lambda: np.zeros((0, 8), np.float32))
+    cylinders: np.ndarray = field(default_factory=lambda: np.zeros((0, 8), np.float32))
+    cuboids: np.ndarray = field(default_factory=lambda: np.zeros((0, 15), np.float32))
+    z_cuboids: np.ndarray = field(default_factory=lambda: np.zeros((0, 15), np.float32))
+
+    def __post_init__(self):
+        self.spheres = _f32(self.spheres, 4)
+        self.capsules = _f32(self.capsules, 8)
+        self.z_capsules = _f32(self.z_capsules, 8)
+        self.cylinders = _f32(self.cylinders, 8)
+        self.cuboids = _f32(self.cuboids, 15)
+        self.z_cuboids = _f32(self.z_cuboids, 15)
+
+    def counts(self) -> dict:
+        return {k: len(getattr(self, k)) for k in
+                ("spheres", "capsules", "z_capsules", "cylinders", "cuboids", "z_cuboids")}
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data if a.size else None
+
+
+class Scene:
+    """Device-resident scene (mrpop_scene)."""
+
+    def __init__(self, arrays: SceneArrays, lib: C.CDLL | None = None):
+        self.lib = lib or library()
+        self.arrays = arrays
+        d = SceneDesc(_ptr(arrays.spheres), len(arrays.spheres), _ptr(arrays.capsules), len(arrays.capsules),
+                      _ptr(arrays.z_capsules), len(arrays.z_capsules), _ptr(arrays.cylinders),
+                      len(arrays.cylinders), _ptr(arrays.cuboids), len(arrays.cuboids),
+                      _ptr(arrays.z_cuboids), len(arrays.z_cuboids))
+        h = C.c_void_p()
+        _check(self.lib, self.lib.mrpop_scene_create(C.byref(d), C.byref(h)))
+        self.handle = h
+
+    def status(self) -> int:
+        v = C.c_uint32()
+        _check(self.lib, self.lib.mrpop_scene_status(self.handle, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.mrpop_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RobotSet:
+    """Arm bases (mrpop_robotset); base: (n, 4, 4) row-major or None (built-in)."""
+
+    def __init__(self, n_arms: int, base: np.ndarray | None = None, lib: C.CDLL | None = None):
+        self.lib = lib or library()
+        self.n_arms = n_arms
+        self.base = None if base is None else np.ascontiguousarray(np.asarray(base, np.float32).reshape(n_arms, 16))
+        h = C.c_void_p()
+        _check(self.lib, self.lib.mrpop_robotset_create(n_arms, None if self.base is None else self.base.ctypes.data,
+                                                         C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.mrpop_robotset_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return C.c_void_p(stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream))
+
+
+def validate(scene: Scene, robots: RobotSet, q0, q1, granularity: int, flags: int = CHECK_ENV | CHECK_SELF,
+             arm: int = -1, rule: int = RULE_PLAIN, range_: float = 0.0, valid=None, first_hit=None,
+             n_seg=None, stream=None):
+    """Validate edges held in CUDA tensors q0/q1 [n, dof]; returns (valid u8, first_hit i32[, n_seg])."""
+    import torch
+    lib = scene.lib
+    n = q0.shape[0]
+    dev = q0.device
+    assert q0.is_cuda and q1.is_cuda and q0.dtype == torch.float32 and q0.is_contiguous() and q1.is_contiguous()
+    if valid is None:
+        valid = torch.empty(n, dtype=torch.uint8, device=dev)
+    if first_hit is None:
+        first_hit = torch.empty(n, dtype=torch.int32, device=dev)
+    st = _stream_ptr(stream)
+    if rule == RULE_PLAIN and n_seg is None:
+        _check(lib, lib.mrpop_validate_edges(scene.handle, robots.handle, q0.data_ptr(), q1.data_ptr(), n,
+                                             granularity, flags, arm, valid.data_ptr(), first_hit.data_ptr(), st))
+        return valid, first_hit
+    if n_seg is None:
+        n_seg = torch.empty(n, dtype=torch.int32, device=dev)
+    _check(lib, lib.mrpop_validate_segments(scene.handle, robots.handle, q0.data_ptr(), q1.data_ptr(), n,
+                                            granularity, rule, float(range_), flags, arm, valid.data_ptr(),
+                                            first_hit.data_ptr(), n_seg.data_ptr(), st))
+    return valid, first_hit, n_seg
+
+
+def count_flops(scene: Scene, robots: RobotSet, q0, q1, granularity: int, flags: int = CHECK_ENV | CHECK_SELF,
+                arm: int = -1, rule: int = RULE_PLAIN, range_: float = 0.0, stream=None):
+    import torch
+    out = torch.empty(q0.shape[0], dtype=torch.float64, device=q0.device)
+    _check(scene.lib, scene.lib.mrpop_count_flops(scene.handle, robots.handle, q0.data_ptr(), q1.data_ptr(),
+                                                  q0.shape[0], granularity, rule, float(range_), flags, arm,
+                                                  out.data_ptr(), _stream_ptr(stream)))
+    return out
+
+
+def fk_spheres(robots: RobotSet, arm: int, q, detailed: bool, stream=None):
+    import torch
+    n = q.shape[0]
+    ns = 59 if detailed else 11
+    out = torch.empty((n, ns, 3), dtype=torch.float32, device=q.device)
+    _check(robots.lib, robots.lib.mrpop_fk_spheres(robots.handle, arm, q.data_ptr(), n, int(detailed),
+                                                   out.data_ptr(), _stream_ptr(stream)))
+    return out
+
+
+def debug_trig(x, lib: C.CDLL | None = None, stream=None):
+    import torch
+    lib = lib or library()
+    c = torch.empty_like(x)
+    s = torch.empty_like(x)
+    _check(lib, lib.mrpop_debug_trig(x.data_ptr(), x.numel(), c.data_ptr(), s.data_ptr(), _stream_ptr(stream)))
+    return c, s
+
+
+class Workspace:
+    """Host-buffer path (mrpop_validate_edges_host)."""
+
+    def __init__(self, lib: C.CDLL | None = None):
+        self.lib = lib or library()
+        h = C.c_void_p()
+        _check(self.lib, self.lib.mrpop_workspace_create(C.byref(h)))
+        self.handle = h
+
+    def validate(self, scene: Scene, robots: RobotSet, q0: np.ndarray, q1: np.ndarray, granularity: int,
+                 flags: int = CHECK_ENV | CHECK_SELF, arm: int = -1, rule: int = RULE_PLAIN, range_: float = 0.0,
+                 valid: np.ndarray | None = None, first_hit: np.ndarray | None = None):
+        n = q0.shape[0]
+        assert q0.dtype == np.float32 and q0.flags.c_contiguous and q1.flags.c_contiguous
+        if valid is None:
+            valid = np.empty(n, np.uint8)
+        if first_hit is None:
+            first_hit = np.empty(n, np.int32)
+        _check(self.lib, self.lib.mrpop_validate_edges_host(self.handle, scene.handle, robots.handle, q0.ctypes.data,
+                                                            q1.ctypes.data, n, granularity, flags, arm, rule,
+                                                            float(range_), valid.ctypes.data,
+                                                            first_hit.ctypes.data))
+        return valid, first_hit
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.mrpop_workspace_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
