@@ -1,0 +1,369 @@
+#!/usr/bin/env python3
+"""Benchmark: edge-samples validated per second on one GB300.
+
+Workload (default): the 4-arm composite configuration -- four Pandas at the
+corners of a 1.0 m square facing the centre, 65536 edges of 28 DOF with
+|dq| <= 1.5 rad, 32 samples per edge, a 51-box bin-picking scene, checks of
+arm-vs-environment and every arm-vs-arm pair with the reference's verdict
+semantics.  Seeded synthetic inputs (no dataset exists for this path).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
+
+A step validates the whole batch once.  `value` is device-timed throughput
+with inputs resident in HBM (L2 flushed before every step); `e2e` is the same
+metric through the host-buffer C ABI call (host->device copy of the edges and
+device->host copy of the verdicts inside the timed region).  Under torchrun
+each rank validates its own copy of the batch (independent edges, no
+collective); value = all ranks' samples / slowest rank's time.
+The reference arm runs the reference's own CUDA edge check
+(fkcc_single_buffer<Panda_four>, compiled from the reference sources into
+oracle/_ref) on the same inputs, or the CPU restatement when that build is
+absent.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "edge-samples validated/s"
+UNIT = "edge-samples/s"
+L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
+    ap.add_argument("--workload", choices=["config1", "config2", "config3"], default="config2")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+        time.sleep(0.3)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows for n, v in zip(names, r[5:9]) if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_setup():
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def load_workload(pkg, name):
+    W = pkg.workloads
+    return {"config1": W.config1, "config2": W.config2, "config3": W.config3}[name]()
+
+
+def workload_config(wl, extra):
+    sc = wl.scene
+    n_obst = int(len(sc.spheres) + len(sc.capsules) + len(sc.z_capsules) + len(sc.cuboids) + len(sc.z_cuboids))
+    cfg = {"workload": wl.name, "edges": int(len(wl.q0)), "granularity": wl.granularity,
+           "arms": int(len(wl.bases)) if wl.arm < 0 else 1, "dof": int(wl.q0.shape[1]), "obstacles": n_obst,
+           "checks": "env+self" if wl.flags & 3 == 3 else ("self" if wl.flags & 2 else "env"),
+           "semantics": "reference verdicts (thread split included)", "l2": "flushed (256 MiB write) before every step"}
+    cfg.update(extra)
+    return cfg
+
+
+def cpu_baseline(orc, wl, n_edges: int):
+    """The CPU restatement on all host threads over the first n_edges edges."""
+    threads = orc.max_threads()
+    sub0, sub1 = wl.q0[:n_edges], wl.q1[:n_edges]
+    orc.validate(wl.scene, wl.bases, sub0[:64], sub1[:64], wl.granularity, wl.flags, wl.arm, threads=threads)
+    t = time.perf_counter()
+    orc.validate(wl.scene, wl.bases, sub0, sub1, wl.granularity, wl.flags, wl.arm, threads=threads)
+    dt = time.perf_counter() - t
+    return {"value": n_edges * wl.granularity / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {n_edges} of the {len(wl.q0)} edges, oracle/edge_oracle.c (FP32 restatement of the "
+                      f"reference check), OpenMP over edges, {dt:.2f} s wall"}
+
+
+def fp32_peak(pkg, torch) -> float:
+    """Measured FP32 FMA issue rate of this GPU in TFLOP/s (best of 3)."""
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, iters = sms * 8, 4000
+    scratch = torch.zeros(blocks, device="cuda")
+    pkg.mrpop.fp32_peak_probe(blocks, 200, scratch)
+    best = 0.0
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        fl = pkg.mrpop.fp32_peak_probe(blocks, iters, scratch)
+        e.record()
+        torch.cuda.synchronize()
+        best = max(best, fl / (s.elapsed_time(e) * 1e-3) / 1e12)
+    return best
+
+
+def committed_traffic(workload: str):
+    """DRAM bytes per launch from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / f"validate_{workload}.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return d.get("dram_bytes_per_launch")
+        except Exception:
+            return None
+    return None
+
+
+def run_mine(args, world, rank, local):
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    lib = pkg.build.lib_path()
+    if not lib.exists():
+        pkg.build.build()
+    pkg.library()
+    wl = load_workload(pkg, args.workload)
+    scene = pkg.Scene(wl.scene)
+    robots = pkg.RobotSet(len(wl.bases), wl.bases)
+    q0 = torch.from_numpy(wl.q0).cuda()
+    q1 = torch.from_numpy(wl.q1).cuda()
+    n = len(wl.q0)
+    samples = n * wl.granularity
+    valid = torch.empty(n, dtype=torch.uint8, device="cuda")
+    first = torch.empty(n, dtype=torch.int32, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        pkg.validate(scene, robots, q0, q1, wl.granularity, wl.flags, wl.arm, valid=valid, first_hit=first)
+
+    flops_launch = float(pkg.count_flops(scene, robots, q0, q1, wl.granularity, wl.flags, wl.arm).sum().item())
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    for s, e in ev:
+        flush.zero_()
+        s.record(stream)
+        step()
+        e.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    step_ms = [s.elapsed_time(e) for s, e in ev]
+    t_total = max_over_ranks(sum(step_ms) / 1e3, world)
+    value = world * samples * args.steps / t_total
+    launch_s = sum(step_ms) / len(step_ms) / 1e3
+    assert scene.status() == 0, "device status word set during the bench"
+
+    peak = fp32_peak(pkg, torch)
+    achieved = flops_launch / launch_s / 1e12
+    traffic = committed_traffic(args.workload)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
+        "config": workload_config(wl, {"parallelism": f"replica x{world}, independent edge batches"}),
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "measured: FP32 FMA loop (mrpop_fp32_peak_probe) timed in this run",
+                     "achieved_basis": f"{flops_launch:.4g} algorithmic flops per launch (FMA=2, per-test costs "
+                                       f"of the flop convention, dense narrow tally) / CUDA-event launch time"},
+        "clocks": clk,
+    }
+    if not args.no_e2e:
+        ws = pkg.Workspace()
+        hq0 = torch.from_numpy(wl.q0).pin_memory()
+        hq1 = torch.from_numpy(wl.q1).pin_memory()
+        hv = torch.empty(n, dtype=torch.uint8).pin_memory()
+        hf = torch.empty(n, dtype=torch.int32).pin_memory()
+        a0, a1, av, af = hq0.numpy(), hq1.numpy(), hv.numpy(), hf.numpy()
+        for _ in range(2):
+            ws.validate(scene, robots, a0, a1, wl.granularity, wl.flags, wl.arm, valid=av, first_hit=af)
+        barrier(world)
+        t = time.perf_counter()
+        for _ in range(args.steps):
+            ws.validate(scene, robots, a0, a1, wl.granularity, wl.flags, wl.arm, valid=av, first_hit=af)
+        dt = max_over_ranks(time.perf_counter() - t, world)
+        out["e2e"] = {"value": world * samples * args.steps / dt, "unit": UNIT,
+                      "h2d_bytes_per_step": int(a0.nbytes + a1.nbytes), "d2h_bytes_per_step": int(av.nbytes + af.nbytes),
+                      "path": "mrpop_validate_edges_host (pinned host buffers, copies and sync inside)"}
+        assert np.array_equal(av, valid.cpu().numpy())
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        out["cpu_baseline"] = cpu_baseline(orc, wl, min(n, 4096))
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def run_reference(args, world, rank, local):
+    if rank != 0:
+        return
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    from oracle import oracle as orc
+    from oracle import ref_runner
+    wl = load_workload(pkg, args.workload)
+    n = len(wl.q0)
+    samples = n * wl.granularity
+    out = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded generators)", "impl": "reference"}
+    if ref_runner.available() and args.workload in ("config1", "config2", "config3"):
+        R = ref_runner.RefHarness()
+        kind = R.KIND_SINGLE if wl.arm >= 0 else R.KIND_COMPOSITE
+        arms = len(wl.bases)
+        if kind == R.KIND_COMPOSITE:
+            R.set_bases(arms, wl.bases)
+        env = R.make_env(wl.scene)
+        q0 = torch.from_numpy(wl.q0).cuda()
+        q1 = torch.from_numpy(wl.q1).cuda()
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        blocks = sms * 8
+        flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+        res = (torch.empty(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda"))
+
+        def step():
+            R.validate(env, q0, q1, wl.granularity, kind, 0, 0.0, arms if kind == R.KIND_COMPOSITE else 1,
+                       max(wl.arm, 0), blocks=blocks, out=res)
+
+        for _ in range(args.warmup):
+            flush.zero_()
+            step()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        clocks = ClockSampler(local)
+        clocks.start()
+        torch.cuda.synchronize()
+        for s, e in ev:
+            flush.zero_()
+            s.record()
+            step()
+            e.record()
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        t = sum(s.elapsed_time(e) for s, e in ev) / 1e3
+        value = samples * args.steps / t
+        out.update({"value": value, "ms_per_step": t / args.steps * 1e3, "clocks": clk, "gpu_launches": args.steps,
+                    "config": workload_config(wl, {"parallelism": "single GPU", "launch": f"{blocks} blocks x "
+                                                                                         f"{4 * wl.granularity} threads, one edge per block at a time"}),
+                    "cpu_baseline": {"value": value, "unit": UNIT, "cores": None, "kind": "reference",
+                                     "sample": "the reference's own CUDA edge check (fkcc_single_buffer*, "
+                                               "utils.cuh:447-686) compiled from its sources for sm_103a and run "
+                                               "on this GB300 over the full workload"}})
+    else:
+        threads = orc.max_threads()
+        m = min(n, 4096)
+        orc.validate(wl.scene, wl.bases, wl.q0[:64], wl.q1[:64], wl.granularity, wl.flags, wl.arm, threads=threads)
+        times = []
+        for _ in range(max(1, min(args.steps, 3))):
+            t = time.perf_counter()
+            orc.validate(wl.scene, wl.bases, wl.q0[:m], wl.q1[:m], wl.granularity, wl.flags, wl.arm, threads=threads)
+            times.append(time.perf_counter() - t)
+        value = m * wl.granularity / (sum(times) / len(times))
+        out.update({"value": value, "ms_per_step": None, "gpu_launches": 0,
+                    "config": workload_config(wl, {"parallelism": f"{threads} host threads"}),
+                    "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                     "sample": f"reference build absent: CPU restatement over the first {m} edges"}})
+    out["e2e"] = {"value": out["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    try:
+        if args.impl == "reference":
+            run_reference(args, world, rank, local)
+        else:
+            run_mine(args, world, rank, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            if dist.is_initialized():
+                dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

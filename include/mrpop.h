@@ -177,6 +177,12 @@ mrpop_status mrpop_count_flops(const mrpop_scene *scene, const mrpop_robotset *r
 mrpop_status mrpop_debug_trig(const float *x, int64_t n, float *cos_out, float *sin_out,
                               void *stream);
 
+/* Measurement utility: launches `blocks` x 256 threads of an FP32 FMA loop
+ * (scratch: >= blocks floats of device memory) and reports its flop count, so
+ * a caller can time the FP32 issue peak that bounds the validator.  No
+ * counterpart in the reference. */
+mrpop_status mrpop_fp32_peak_probe(int blocks, int iters, float *scratch, double *flops_out, void *stream);
+
 /* Last error message of the calling thread ("" if none). */
 const char *mrpop_last_error(void);
 /* Library version string. */

@@ -1,4 +1,5 @@
 // api.cu -- C ABI of the GB300 edge validator (declared in include/mrpop.h).
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -124,6 +125,44 @@ mrpop_status mrpop_scene_create(const mrpop_scene_desc *desc, mrpop_scene **out)
     };
     put_cubs(L.cub, desc->cuboids, c.n_cub);
     put_cubs(L.zcub, desc->z_cuboids, c.n_zcub);
+    // bounding spheres (culling only; exact tests decide every verdict)
+    const double margin = mrpop::kCullMargin;
+    auto bound = [&](double x, double y, double z, double r) {
+        return make_float4((float)x, (float)y, (float)z, (float)(r * 1.002 + margin));
+    };
+    auto unit = [](double x, double y, double z) { return std::fabs(std::sqrt(x * x + y * y + z * z) - 1.0) < 1e-3; };
+    for (int k = 0; k < 2; k++) {
+        const float *src = k ? desc->z_cuboids : desc->cuboids;
+        const int n = k ? c.n_zcub : c.n_cub, off = k ? L.b_zcub : L.b_cub;
+        for (int i = 0; i < n; i++) {
+            const float *b = src + 15 * i;
+            bool ortho;
+            if (k == 0)
+                ortho = unit(b[3], b[4], b[5]) && unit(b[6], b[7], b[8]) && unit(b[9], b[10], b[11]) &&
+                        std::fabs((double)b[3] * b[6] + (double)b[4] * b[7] + (double)b[5] * b[8]) < 1e-3 &&
+                        std::fabs((double)b[3] * b[9] + (double)b[4] * b[10] + (double)b[5] * b[11]) < 1e-3 &&
+                        std::fabs((double)b[6] * b[9] + (double)b[7] * b[10] + (double)b[8] * b[11]) < 1e-3;
+            else
+                ortho = unit(b[3], b[4], 0.0) && unit(b[6], b[7], 0.0) &&
+                        std::fabs((double)b[3] * b[6] + (double)b[4] * b[7]) < 1e-3;
+            const double hr = std::sqrt((double)b[12] * b[12] + (double)b[13] * b[13] + (double)b[14] * b[14]);
+            h[off + i] = bound(b[0], b[1], b[2], ortho ? hr : 1e18);
+        }
+    }
+    for (int k = 0; k < 2; k++) {
+        const float *src = k ? desc->z_capsules : desc->capsules;
+        const int n = k ? c.n_zcap : c.n_cap, off = k ? L.b_zcap : L.b_cap;
+        for (int i = 0; i < n; i++) {
+            const float *b = src + 8 * i;
+            const double vx = k ? 0.0 : b[3], vy = k ? 0.0 : b[4], vz = b[5];
+            const double len = std::sqrt(vx * vx + vy * vy + vz * vz);
+            h[off + i] = bound(b[0] + 0.5 * vx, b[1] + 0.5 * vy, b[2] + 0.5 * vz, 0.5 * len + b[6]);
+        }
+    }
+    for (int i = 0; i < c.n_sph; i++) {
+        const float *b = desc->spheres + 4 * i;
+        h[L.b_sph + i] = bound(b[0], b[1], b[2], b[3]);
+    }
 
     mrpop_scene *sc = new (std::nothrow) mrpop_scene();
     if (!sc) return fail(MRPOP_ERR_OUT_OF_MEMORY, "scene_create: host allocation");
@@ -234,6 +273,14 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
     p.sc = scene->counts;
     p.status = scene->d_status;
     p.env_test_flops = scene->env_test_flops;
+    for (int j = 0; j < mrpop::kNumJoints; j++) {
+        double r = 0.0;
+        for (int i = mrpop::kDetFirst[j]; i < mrpop::kDetFirst[j + 1]; i++) {
+            const mrpop::SphereDef &d = mrpop::kDet[i];
+            r = std::fmax(r, std::sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z) + d.r);
+        }
+        p.group_r[j] = (float)(r * 1.001 + mrpop::kCullMargin);
+    }
     const int A = arm >= 0 ? 1 : robots->n_arms;
     for (int a = 0; a < A; a++)
         for (int i = 0; i < 12; i++) p.base[a][i] = robots->base[arm >= 0 ? arm : a][i];
@@ -271,12 +318,12 @@ __global__ void fk_spheres_kernel(const float *q, long long n, int detailed, con
     float qq[7];
     for (int d = 0; d < 7; d++) qq[d] = q[t * 7 + d];
     if (!detailed) {
-        float px[mrpop::kNumApprox], py[mrpop::kNumApprox], pz[mrpop::kNumApprox];
-        mrpop::fk_approx_arm(b, qq, px, py, pz);
+        mrpop::ArmSpheres s;
+        mrpop::fk_approx_arm(b, qq, s);
         for (int i = 0; i < mrpop::kNumApprox; i++) {
-            out[(t * mrpop::kNumApprox + i) * 3 + 0] = px[i];
-            out[(t * mrpop::kNumApprox + i) * 3 + 1] = py[i];
-            out[(t * mrpop::kNumApprox + i) * 3 + 2] = pz[i];
+            out[(t * mrpop::kNumApprox + i) * 3 + 0] = s.x[i];
+            out[(t * mrpop::kNumApprox + i) * 3 + 1] = s.y[i];
+            out[(t * mrpop::kNumApprox + i) * 3 + 2] = s.z[i];
         }
         return;
     }

@@ -13,25 +13,38 @@
 //                check (or every flagged sample in EXACT mode).
 //   narrow phase per warp, one sample at a time in increasing k: lanes rebuild
 //                the joint frames of that sample, place the 59 detailed
-//                spheres per arm in shared memory and split the flagged env and
-//                self tests over the lanes; a warp vote ends the edge at the
-//                first colliding sample.
+//                spheres per arm in shared memory, then split the flagged env
+//                tests and self rows (compacted into dense work lists) over the
+//                lanes; a warp vote ends the edge at the first colliding sample.
+// Culling: every obstacle carries a bounding sphere (1 mm margin) and every
+// arm / joint group a bounding sphere computed from its own sphere set; an
+// exact test is skipped only where the bounds prove it cannot fire, so the
+// set of tests that can fire -- and therefore every verdict -- is unchanged.
 #pragma once
 #include "panda_model.cuh"
 
 namespace mrpop {
 
+#ifndef MRPOP_MIN_BLOCKS
+#define MRPOP_MIN_BLOCKS 4
+#endif
 constexpr int kWarpsPerBlock = 4;
 constexpr int kMaxArms = 5;
 constexpr int kMaxDof = 7 * kMaxArms;
+constexpr float kCullMargin = 1e-3f;   // metres added to every bounding radius
+constexpr float kApproxMaxR = 0.176f;  // largest broad-phase sphere radius
 
 struct SceneCounts {
     int n_sph, n_cap, n_zcap, n_cub, n_zcub;
 };
 
-// Float4 offsets of each obstacle class inside the packed scene buffer.
+// Float4 offsets inside the packed scene buffer: obstacle records by class,
+// then one bounding sphere {cx, cy, cz, radius + margin} per obstacle in the
+// order cuboids, z-cuboids, capsules, z-capsules, spheres.
 struct SceneLayout {
-    int sph, cap, zcap, cub, zcub, total; // in float4 units
+    int sph, cap, zcap, cub, zcub;
+    int b_cub, b_zcub, b_cap, b_zcap, b_sph;
+    int total;
 };
 
 __host__ __device__ inline SceneLayout scene_layout(const SceneCounts &c) {
@@ -41,7 +54,12 @@ __host__ __device__ inline SceneLayout scene_layout(const SceneCounts &c) {
     l.zcap = l.cap + 2 * c.n_cap;
     l.cub = l.zcap + 2 * c.n_zcap;
     l.zcub = l.cub + 4 * c.n_cub;
-    l.total = l.zcub + 4 * c.n_zcub;
+    l.b_cub = l.zcub + 4 * c.n_zcub;
+    l.b_zcub = l.b_cub + c.n_cub;
+    l.b_cap = l.b_zcub + c.n_zcub;
+    l.b_zcap = l.b_cap + c.n_cap;
+    l.b_sph = l.b_zcap + c.n_zcap;
+    l.total = l.b_sph + c.n_sph;
     return l;
 }
 
@@ -63,16 +81,27 @@ struct EdgeParams {
     const float4 *scene;
     SceneCounts sc;
     unsigned int *status;
-    float base[kMaxArms][12]; // row-major 3x4 per arm of this check
+    float group_r[kNumJoints];  // bounding radius of each joint's detailed spheres (+margin)
+    float base[kMaxArms][12];   // row-major 3x4 per arm of this check
 };
 
-// Per-warp shared scratch.
+// Per-warp shared scratch.  The broad-phase and narrow-phase parts are never
+// live at the same time and share storage.
 struct WarpScratch {
     float base[kMaxDof];   // segment start (accumulated for CONNECT)
     float stepg[kMaxDof];  // per-sample step (delta/g or vec/g)
     float delta[kMaxDof];  // per-segment step (B-spline / shortcut accumulation)
-    float T[kMaxArms][kNumJoints][12];
-    float4 P[kMaxArms][kNumDet]; // detailed sphere centres (w = radius)
+    union {
+        struct {
+            float4 armbs[kMaxArms][32];     // per-lane arm bounding sphere
+            float cur[kNumApprox][3][32];   // per-lane approx spheres of the current arm
+            float low[kNumApprox][3][32];   // per-lane approx spheres of a lower arm
+        } broad;
+        struct {
+            float T[kMaxArms][kNumJoints][12];
+            float4 P[kMaxArms][kNumDet];     // detailed sphere centres (w = radius)
+        } narrow;
+    };
 };
 
 constexpr unsigned kFull = 0xffffffffu;
@@ -88,8 +117,8 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ bool stage_scene(float4 *dst, const float4 *src, uint32_t bytes,
-                                            uint64_t *bar, unsigned int *status) {
+__device__ __forceinline__ bool stage_scene(float4 *dst, const float4 *src, uint32_t bytes, uint64_t *bar,
+                                            unsigned int *status) {
     bool ok = true;
     if (bytes == 0) return true;
     if (threadIdx.x == 0) {
@@ -98,8 +127,7 @@ __device__ __forceinline__ bool stage_scene(float4 *dst, const float4 *src, uint
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-                     "r"(bytes)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                      : "memory");
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -107,7 +135,6 @@ __device__ __forceinline__ bool stage_scene(float4 *dst, const float4 *src, uint
             "l"(src), "r"(bytes), "r"(smem_u32(bar))
             : "memory");
     }
-    // bounded wait on phase 0
     uint32_t done = 0;
     for (int it = 0; it < (1 << 22) && !done; it++) {
         asm volatile(
@@ -123,109 +150,47 @@ __device__ __forceinline__ bool stage_scene(float4 *dst, const float4 *src, uint
     return __syncthreads_and(ok);
 }
 
-// ---------------------------------------------------------------------------
-// scene queries against the staged copy (uniform loops: obstacle data is a
-// shared-memory broadcast, spheres live in registers)
-// ---------------------------------------------------------------------------
-// Broad phase: approx spheres 1..10 of one arm; returns a bitmask over sphere
-// index (bit i set = sphere i touches some obstacle).
-__device__ __forceinline__ uint32_t env_mask_approx(const float4 *S, const SceneLayout &L,
-                                                    const SceneCounts &C, const float (&px)[kNumApprox],
-                                                    const float (&py)[kNumApprox],
-                                                    const float (&pz)[kNumApprox]) {
-    uint32_t m = 0;
-    float rsq[kNumApprox];
-#pragma unroll
-    for (int i = 1; i < kNumApprox; i++) rsq[i] = __fmul_rn(c_approx[i].w, c_approx[i].w);
-    for (int o = 0; o < C.n_cub; o++) {
-        const float4 c0 = S[L.cub + 4 * o], c1 = S[L.cub + 4 * o + 1], c2 = S[L.cub + 4 * o + 2],
-                     c3 = S[L.cub + 4 * o + 3];
-#pragma unroll
-        for (int i = 1; i < kNumApprox; i++)
-            if (hit_cuboid(c0, c1, c2, c3, px[i], py[i], pz[i], rsq[i])) m |= 1u << i;
-    }
-    for (int o = 0; o < C.n_zcub; o++) {
-        const float4 c0 = S[L.zcub + 4 * o], c1 = S[L.zcub + 4 * o + 1], c2 = S[L.zcub + 4 * o + 2];
-#pragma unroll
-        for (int i = 1; i < kNumApprox; i++)
-            if (hit_zcuboid(c0, c1, c2, px[i], py[i], pz[i], rsq[i])) m |= 1u << i;
-    }
-    for (int o = 0; o < C.n_cap; o++) {
-        const float4 c0 = S[L.cap + 2 * o], c1 = S[L.cap + 2 * o + 1];
-#pragma unroll
-        for (int i = 1; i < kNumApprox; i++)
-            if (hit_capsule(c0, c1, px[i], py[i], pz[i], c_approx[i].w)) m |= 1u << i;
-    }
-    for (int o = 0; o < C.n_zcap; o++) {
-        const float4 c0 = S[L.zcap + 2 * o], c1 = S[L.zcap + 2 * o + 1];
-#pragma unroll
-        for (int i = 1; i < kNumApprox; i++)
-            if (hit_zcapsule(c0, c1, px[i], py[i], pz[i], c_approx[i].w)) m |= 1u << i;
-    }
-    for (int o = 0; o < C.n_sph; o++) {
-        const float4 c0 = S[L.sph + o];
-#pragma unroll
-        for (int i = 1; i < kNumApprox; i++)
-            if (hit_sphere_sphere(c0.x, c0.y, c0.z, c0.w, px[i], py[i], pz[i], c_approx[i].w)) m |= 1u << i;
-    }
-    return m;
-}
-
-// One sphere against the whole scene (narrow phase).
-__device__ __forceinline__ bool env_hit_one(const float4 *S, const SceneLayout &L, const SceneCounts &C,
-                                            float x, float y, float z, float r) {
-    const float rsq = __fmul_rn(r, r);
-    for (int o = 0; o < C.n_cub; o++)
-        if (hit_cuboid(S[L.cub + 4 * o], S[L.cub + 4 * o + 1], S[L.cub + 4 * o + 2], S[L.cub + 4 * o + 3], x, y,
-                       z, rsq))
-            return true;
-    for (int o = 0; o < C.n_zcub; o++)
-        if (hit_zcuboid(S[L.zcub + 4 * o], S[L.zcub + 4 * o + 1], S[L.zcub + 4 * o + 2], x, y, z, rsq))
-            return true;
-    for (int o = 0; o < C.n_cap; o++)
-        if (hit_capsule(S[L.cap + 2 * o], S[L.cap + 2 * o + 1], x, y, z, r)) return true;
-    for (int o = 0; o < C.n_zcap; o++)
-        if (hit_zcapsule(S[L.zcap + 2 * o], S[L.zcap + 2 * o + 1], x, y, z, r)) return true;
-    for (int o = 0; o < C.n_sph; o++) {
-        const float4 c0 = S[L.sph + o];
-        if (hit_sphere_sphere(c0.x, c0.y, c0.z, c0.w, x, y, z, r)) return true;
-    }
-    return false;
+__device__ __forceinline__ bool near3(float x, float y, float z, float4 b, float r) {
+    const float dx = x - b.x, dy = y - b.y, dz = z - b.z;
+    const float rr = r + b.w;
+    return dx * dx + dy * dy + dz * dz < rr * rr;
 }
 
 // ---------------------------------------------------------------------------
-// FK of one arm for one sample: approx sphere centres in registers
+// FK of one arm for one sample: approx sphere centres
 // ---------------------------------------------------------------------------
+struct ArmSpheres {
+    float x[kNumApprox], y[kNumApprox], z[kNumApprox];
+};
+
 template <int I>
-__device__ __forceinline__ void place_approx(const Xf &T, float (&px)[kNumApprox], float (&py)[kNumApprox],
-                                             float (&pz)[kNumApprox]) {
-    px[I] = place_coord<I, false>(T, 0);
-    py[I] = place_coord<I, false>(T, 1);
-    pz[I] = place_coord<I, false>(T, 2);
+__device__ __forceinline__ void place_approx(const Xf &T, ArmSpheres &s) {
+    s.x[I] = place_coord<I, false>(T, 0);
+    s.y[I] = place_coord<I, false>(T, 1);
+    s.z[I] = place_coord<I, false>(T, 2);
 }
 
-__device__ __forceinline__ void fk_approx_arm(const float *base12, const float (&q)[7], float (&px)[kNumApprox],
-                                              float (&py)[kNumApprox], float (&pz)[kNumApprox]) {
+__device__ __forceinline__ void fk_approx_arm(const float *base12, const float (&q)[7], ArmSpheres &s) {
     Xf T;
     load_base(T, base12);
-    place_approx<0>(T, px, py, pz);
+    place_approx<0>(T, s);
     joint_step<1>(T, q[0]);
-    place_approx<1>(T, px, py, pz);
+    place_approx<1>(T, s);
     joint_step<2>(T, q[1]);
-    place_approx<2>(T, px, py, pz);
+    place_approx<2>(T, s);
     joint_step<3>(T, q[2]);
-    place_approx<3>(T, px, py, pz);
+    place_approx<3>(T, s);
     joint_step<4>(T, q[3]);
-    place_approx<4>(T, px, py, pz);
+    place_approx<4>(T, s);
     joint_step<5>(T, q[4]);
-    place_approx<5>(T, px, py, pz);
+    place_approx<5>(T, s);
     joint_step<6>(T, q[5]);
-    place_approx<6>(T, px, py, pz);
+    place_approx<6>(T, s);
     joint_step<7>(T, q[6]);
-    place_approx<7>(T, px, py, pz);
-    place_approx<8>(T, px, py, pz);
-    place_approx<9>(T, px, py, pz);
-    place_approx<10>(T, px, py, pz);
+    place_approx<7>(T, s);
+    place_approx<8>(T, s);
+    place_approx<9>(T, s);
+    place_approx<10>(T, s);
 }
 
 // Joint values of arm `a` for sample k of segment `seg` (call-site formulas,
@@ -242,60 +207,192 @@ __device__ __forceinline__ void sample_q(const WarpScratch &W, int rule, int seg
     }
 }
 
-// Broad phase of one sample: env / self flag words (bit 8a+j) and counts.
+// FK of arm `qarm`'s joint values (base12) for this lane's sample; writes the
+// 11 centres into the lane's column of dst and returns a conservative bounding
+// sphere of the arm's approx spheres (w = radius).
+static __device__ __noinline__ float4 fk_approx_lane(const float *base12, const WarpScratch &W, int rule, int seg,
+                                                     int qarm, int k, float (*dst)[3][32], int lane) {
+    float q[7];
+    sample_q(W, rule, seg, qarm, k, q);
+    ArmSpheres s;
+    fk_approx_arm(base12, q, s);
+    float lx = s.x[0], hx = s.x[0], ly = s.y[0], hy = s.y[0], lz = s.z[0], hz = s.z[0];
+#pragma unroll
+    for (int i = 0; i < kNumApprox; i++) {
+        dst[i][0][lane] = s.x[i];
+        dst[i][1][lane] = s.y[i];
+        dst[i][2][lane] = s.z[i];
+        lx = fminf(lx, s.x[i]);
+        hx = fmaxf(hx, s.x[i]);
+        ly = fminf(ly, s.y[i]);
+        hy = fmaxf(hy, s.y[i]);
+        lz = fminf(lz, s.z[i]);
+        hz = fmaxf(hz, s.z[i]);
+    }
+    const float cx = 0.5f * (lx + hx), cy = 0.5f * (ly + hy), cz = 0.5f * (lz + hz);
+    float r2 = 0.f;
+#pragma unroll
+    for (int i = 0; i < kNumApprox; i++) {
+        const float dx = s.x[i] - cx, dy = s.y[i] - cy, dz = s.z[i] - cz;
+        r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
+    }
+    return make_float4(cx, cy, cz, sqrtf(r2) * 1.0001f + kApproxMaxR + 1e-4f);
+}
+
+// ---------------------------------------------------------------------------
+// broad phase: approx spheres 1..10 of one arm (lane column `lane` of sp)
+// against the scene.  Returns a bitmask over sphere index (bit i = sphere i
+// touches some obstacle).  Each obstacle is first tested against every lane's
+// arm bound (warp vote), then against each sphere's bound (warp OR); exact
+// tests run, for the whole warp, only for spheres some lane cannot rule out.
+// ---------------------------------------------------------------------------
+template <typename ExactFn>
+__device__ __forceinline__ void env_obstacle(const float (*sp)[3][32], int lane, float4 cb, float4 ob, uint32_t &m,
+                                             ExactFn exact) {
+    if (!__any_sync(kFull, near3(cb.x, cb.y, cb.z, ob, cb.w))) return;
+    uint32_t q = 0;
+#pragma unroll
+    for (int i = 1; i < kNumApprox; i++)
+        if (near3(sp[i][0][lane], sp[i][1][lane], sp[i][2][lane], ob, c_approx[i].w)) q |= 1u << i;
+    q = __reduce_or_sync(kFull, q);
+    while (q) {
+        const int i = __ffs(q) - 1;
+        q &= q - 1;
+        if (exact(sp[i][0][lane], sp[i][1][lane], sp[i][2][lane], c_approx[i].w)) m |= 1u << i;
+    }
+}
+
+static __device__ __noinline__ uint32_t env_mask_approx(const float4 *S, const SceneLayout &L, const SceneCounts &C,
+                                                        const float (*sp)[3][32], int lane, float4 cb) {
+    uint32_t m = 0;
+    for (int o = 0; o < C.n_cub; o++) {
+        const float4 *r = S + L.cub + 4 * o;
+        env_obstacle(sp, lane, cb, S[L.b_cub + o], m, [&](float x, float y, float z, float rad) {
+            return hit_cuboid(r[0], r[1], r[2], r[3], x, y, z, __fmul_rn(rad, rad));
+        });
+    }
+    for (int o = 0; o < C.n_zcub; o++) {
+        const float4 *r = S + L.zcub + 4 * o;
+        env_obstacle(sp, lane, cb, S[L.b_zcub + o], m, [&](float x, float y, float z, float rad) {
+            return hit_zcuboid(r[0], r[1], r[2], x, y, z, __fmul_rn(rad, rad));
+        });
+    }
+    for (int o = 0; o < C.n_cap; o++) {
+        const float4 *r = S + L.cap + 2 * o;
+        env_obstacle(sp, lane, cb, S[L.b_cap + o], m,
+                     [&](float x, float y, float z, float rad) { return hit_capsule(r[0], r[1], x, y, z, rad); });
+    }
+    for (int o = 0; o < C.n_zcap; o++) {
+        const float4 *r = S + L.zcap + 2 * o;
+        env_obstacle(sp, lane, cb, S[L.b_zcap + o], m,
+                     [&](float x, float y, float z, float rad) { return hit_zcapsule(r[0], r[1], x, y, z, rad); });
+    }
+    for (int o = 0; o < C.n_sph; o++) {
+        const float4 c0 = S[L.sph + o];
+        env_obstacle(sp, lane, cb, S[L.b_sph + o], m, [&](float x, float y, float z, float rad) {
+            return hit_sphere_sphere(c0.x, c0.y, c0.z, c0.w, x, y, z, rad);
+        });
+    }
+    return m;
+}
+
+// One sphere against the whole scene (narrow phase), with per-obstacle bounds.
+static __device__ __noinline__ bool env_hit_one(const float4 *S, const SceneLayout &L, const SceneCounts &C, float x,
+                                                float y, float z, float r) {
+    const float rsq = __fmul_rn(r, r);
+    for (int o = 0; o < C.n_cub; o++)
+        if (near3(x, y, z, S[L.b_cub + o], r) &&
+            hit_cuboid(S[L.cub + 4 * o], S[L.cub + 4 * o + 1], S[L.cub + 4 * o + 2], S[L.cub + 4 * o + 3], x, y, z,
+                       rsq))
+            return true;
+    for (int o = 0; o < C.n_zcub; o++)
+        if (near3(x, y, z, S[L.b_zcub + o], r) &&
+            hit_zcuboid(S[L.zcub + 4 * o], S[L.zcub + 4 * o + 1], S[L.zcub + 4 * o + 2], x, y, z, rsq))
+            return true;
+    for (int o = 0; o < C.n_cap; o++)
+        if (near3(x, y, z, S[L.b_cap + o], r) && hit_capsule(S[L.cap + 2 * o], S[L.cap + 2 * o + 1], x, y, z, r))
+            return true;
+    for (int o = 0; o < C.n_zcap; o++)
+        if (near3(x, y, z, S[L.b_zcap + o], r) && hit_zcapsule(S[L.zcap + 2 * o], S[L.zcap + 2 * o + 1], x, y, z, r))
+            return true;
+    for (int o = 0; o < C.n_sph; o++) {
+        const float4 c0 = S[L.sph + o];
+        if (near3(x, y, z, S[L.b_sph + o], r) && hit_sphere_sphere(c0.x, c0.y, c0.z, c0.w, x, y, z, r)) return true;
+    }
+    return false;
+}
+
+// Broad-phase intra-arm rows (panda_multi_geometry.cuh:133-139) as 21 pairs.
+static __constant__ uint8_t c_intra_pairs[21][2] = {
+    {0, 5}, {0, 6}, {0, 7}, {0, 8}, {0, 9}, {0, 10}, {1, 5}, {1, 6}, {1, 7}, {1, 8}, {1, 9},
+    {1, 10}, {2, 5}, {2, 7}, {2, 8}, {2, 9}, {2, 10}, {5, 7}, {5, 8}, {5, 9}, {5, 10}};
+
+// Broad phase of one sample (every lane of the warp calls it; lanes past the
+// segment's last sample evaluate sample g and discard the result).
 template <int A>
-__device__ __forceinline__ void broad_sample(const EdgeParams &P, const WarpScratch &W, const float4 *S,
-                                             const SceneLayout &L, int seg, int k, uint64_t &envw,
-                                             uint64_t &selfw) {
+__device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W, const float4 *S,
+                                             const SceneLayout &L, int seg, int k, uint64_t &envw, uint64_t &selfw) {
+    const int lane = threadIdx.x & 31;
     envw = 0;
     selfw = 0;
     const bool do_env = P.flags & kEnvBit, do_self = P.flags & kSelfBit;
+    auto &cur = W.broad.cur;
+    auto &low = W.broad.low;
 #pragma unroll 1
     for (int b = 0; b < A; b++) {
-        float q[7];
-        sample_q(W, P.rule, seg, P.single ? 0 : b, k, q);
-        float px[kNumApprox], py[kNumApprox], pz[kNumApprox];
-        fk_approx_arm(P.base[b], q, px, py, pz);
+        const float4 cb = fk_approx_lane(P.base[b], W, P.rule, seg, P.single ? 0 : b, k, cur, lane);
         if (do_env) {
-            const uint32_t m = env_mask_approx(S, L, P.sc, px, py, pz);
+            const uint32_t m = env_mask_approx(S, L, P.sc, cur, lane, cb);
             uint32_t jm = 0;
 #pragma unroll
             for (int i = 1; i < kNumApprox; i++)
                 if (m >> i & 1u) jm |= 1u << approx_joint(i);
             envw |= (uint64_t)jm << (8 * b);
         }
-        if (do_self) {
-            uint32_t jm = 0;
-            // intra-arm rows (panda_multi_geometry.cuh:133-139)
-#define MRPOP_INTRA(s1, j)                                                                                 \
-    if (hit_sphere_sphere(px[s1], py[s1], pz[s1], c_approx[s1].w, px[j], py[j], pz[j], c_approx[j].w))    \
-        jm |= 1u << approx_joint(s1);
-#pragma unroll
-            for (int j = 5; j <= 10; j++) { MRPOP_INTRA(0, j) MRPOP_INTRA(1, j) }
-            MRPOP_INTRA(2, 5)
-#pragma unroll
-            for (int j = 7; j <= 10; j++) { MRPOP_INTRA(2, j) MRPOP_INTRA(5, j) }
-#undef MRPOP_INTRA
-            selfw |= (uint64_t)jm << (8 * b);
-            // arm-vs-arm against every lower arm a < b; flags go to arm a
-            // (panda_four.cuh:178-214)
+        if (!do_self) continue;
+        uint32_t jm = 0;
 #pragma unroll 1
-            for (int a = 0; a < b; a++) {
-                float qa[7];
-                sample_q(W, P.rule, seg, a, k, qa);
-                float ax[kNumApprox], ay[kNumApprox], az[kNumApprox];
-                fk_approx_arm(P.base[a], qa, ax, ay, az);
-                uint32_t am = 0;
+        for (int t = 0; t < 21; t++) {
+            const int s1 = c_intra_pairs[t][0], s2 = c_intra_pairs[t][1];
+            if (hit_sphere_sphere(cur[s1][0][lane], cur[s1][1][lane], cur[s1][2][lane], c_approx[s1].w,
+                                  cur[s2][0][lane], cur[s2][1][lane], cur[s2][2][lane], c_approx[s2].w))
+                jm |= 1u << approx_joint(s1);
+        }
+        selfw |= (uint64_t)jm << (8 * b);
+        if (A == 1) continue;
+        W.broad.armbs[b][lane] = cb;
+        // arm-vs-arm against every lower arm a < b; flags go to arm a
+        // (panda_four.cuh:178-214).  Pairs whose bounds are apart in every
+        // lane are skipped; otherwise arm a's spheres are rebuilt.
+#pragma unroll 1
+        for (int a = 0; a < b; a++) {
+            const float4 ca = W.broad.armbs[a][lane];
+            if (!__any_sync(kFull, near3(cb.x, cb.y, cb.z, ca, cb.w))) continue;
+            fk_approx_lane(P.base[a], W, P.rule, seg, a, k, low, lane);
+            uint32_t qa = 0, qb = 0;
 #pragma unroll
-                for (int i = 0; i < kNumApprox; i++) {
-                    bool h = false;
-#pragma unroll
-                    for (int j = 0; j < kNumApprox; j++)
-                        h |= hit_sphere_sphere(ax[i], ay[i], az[i], c_approx[i].w, px[j], py[j], pz[j], c_approx[j].w);
-                    if (h) am |= 1u << approx_joint(i);
-                }
-                selfw |= (uint64_t)am << (8 * a);
+            for (int i = 0; i < kNumApprox; i++) {
+                if (near3(low[i][0][lane], low[i][1][lane], low[i][2][lane], cb, c_approx[i].w)) qa |= 1u << i;
+                if (near3(cur[i][0][lane], cur[i][1][lane], cur[i][2][lane], ca, c_approx[i].w)) qb |= 1u << i;
             }
+            qa = __reduce_or_sync(kFull, qa);
+            qb = __reduce_or_sync(kFull, qb);
+            uint32_t am = 0;
+            while (qa) {
+                const int i = __ffs(qa) - 1;
+                qa &= qa - 1;
+                const float ax = low[i][0][lane], ay = low[i][1][lane], az = low[i][2][lane], ar = c_approx[i].w;
+                bool h = false;
+                uint32_t qj = qb;
+                while (qj) {
+                    const int j = __ffs(qj) - 1;
+                    qj &= qj - 1;
+                    h |= hit_sphere_sphere(ax, ay, az, ar, cur[j][0][lane], cur[j][1][lane], cur[j][2][lane],
+                                           c_approx[j].w);
+                }
+                if (h) am |= 1u << approx_joint(i);
+            }
+            selfw |= (uint64_t)am << (8 * a);
         }
     }
 }
@@ -317,8 +414,8 @@ __device__ __forceinline__ int ref_share(int cnt, int total, int g) {
 }
 
 // dense narrow-phase tally for one sample (per the flop convention)
-__device__ __forceinline__ double narrow_flops(const EdgeParams &P, int A, uint64_t envw, uint64_t selfw,
-                                               bool de, bool ds) {
+__device__ __forceinline__ double narrow_flops(const EdgeParams &P, int A, uint64_t envw, uint64_t selfw, bool de,
+                                               bool ds) {
     double f = 0.0;
     const bool quirk = !P.single && !(P.flags & kExactBit);
     for (int a = 0; a < A; a++) {
@@ -343,10 +440,37 @@ __device__ __forceinline__ double narrow_flops(const EdgeParams &P, int A, uint6
 // ---------------------------------------------------------------------------
 // narrow phase of one sample (whole warp)
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t joint_sphere_mask(uint32_t jm) {
+    uint64_t m = 0;
+#pragma unroll
+    for (int j = 0; j < kNumJoints; j++)
+        if (jm >> j & 1u) m |= ((1ull << det_count(j)) - 1ull) << det_first(j);
+    return m;
+}
+
+// position of the n-th (0-based) set bit of m
+__device__ __forceinline__ int nth_bit(uint64_t m, int n) {
+    const uint32_t lo = (uint32_t)m;
+    const int pl = __popc(lo);
+    if (n < pl) return (int)__fns(lo, 0, n + 1);
+    return 32 + (int)__fns((uint32_t)(m >> 32), 0, n - pl + 1);
+}
+
+// bit r set: detailed self row r is checked for an arm with self flags sm
+__device__ __forceinline__ uint32_t row_mask(uint32_t sm, bool quirk) {
+    uint32_t m = 0;
+#pragma unroll
+    for (int r = 0; r < kDetRows; r++) {
+        const int pi = quirk ? r : det_row_first(r);
+        if (sm >> det_joint(pi) & 1u) m |= 1u << r;
+    }
+    return m;
+}
+
 template <int A>
-__device__ __noinline__ bool narrow_sample(const EdgeParams &P, WarpScratch &W, const float4 *S,
-                                           const SceneLayout &L, const float4 *det_tab, int seg, int k,
-                                           uint64_t envw, uint64_t selfw, bool de, bool ds) {
+__device__ __noinline__ bool narrow_sample(const EdgeParams &P, WarpScratch &W, const float4 *S, const SceneLayout &L,
+                                           const float4 *det_tab, int seg, int k, uint64_t envw, uint64_t selfw,
+                                           bool de, bool ds) {
     const int lane = threadIdx.x & 31;
     // joint frames of every arm
     if (lane < A) {
@@ -355,58 +479,98 @@ __device__ __noinline__ bool narrow_sample(const EdgeParams &P, WarpScratch &W, 
         Xf T;
         load_base(T, P.base[lane]);
 #pragma unroll
-        for (int i = 0; i < 12; i++) W.T[lane][0][i] = T.m[i];
+        for (int i = 0; i < 12; i++) W.narrow.T[lane][0][i] = T.m[i];
 #pragma unroll
         for (int j = 1; j < kNumJoints; j++) {
             joint_step_rt(T, q[j - 1], j);
 #pragma unroll
-            for (int i = 0; i < 12; i++) W.T[lane][j][i] = T.m[i];
+            for (int i = 0; i < 12; i++) W.narrow.T[lane][j][i] = T.m[i];
         }
     }
     __syncwarp();
     for (int idx = lane; idx < A * kNumDet; idx += 32) {
         const int a = idx / kNumDet, i = idx - a * kNumDet;
         const float4 s = det_tab[i];
-        const float3 p = place_rt(W.T[a][det_joint(i)], s);
-        W.P[a][i] = make_float4(p.x, p.y, p.z, s.w);
+        const float3 p = place_rt(W.narrow.T[a][det_joint(i)], s);
+        W.narrow.P[a][i] = make_float4(p.x, p.y, p.z, s.w);
     }
     __syncwarp();
     bool hit = false;
     if (de) {
-        for (int idx = lane; idx < A * kNumDet; idx += 32) {
-            const int a = idx / kNumDet, i = idx - a * kNumDet;
-            if (i > 0 && (envw >> (8 * a + det_joint(i)) & 1ull)) {
-                const float4 p = W.P[a][i];
-                hit |= env_hit_one(S, L, P.sc, p.x, p.y, p.z, p.w);
-            }
+        // dense list of (arm, sphere) with the env flag on the sphere's joint
+        uint64_t m[A];
+        int total = 0;
+#pragma unroll
+        for (int a = 0; a < A; a++) {
+            m[a] = joint_sphere_mask((uint32_t)(envw >> (8 * a)) & 0xffu) & ~1ull; // sphere 0 is never env-tested
+            total += __popcll(m[a]);
+        }
+        for (int t = lane; t < total; t += 32) {
+            int a = 0, u = t;
+#pragma unroll
+            for (int aa = 0; aa < A - 1; aa++)
+                if (a == aa && u >= __popcll(m[aa])) {
+                    u -= __popcll(m[aa]);
+                    a = aa + 1;
+                }
+            const int i = nth_bit(m[a], u);
+            const float4 p = W.narrow.P[a][i];
+            hit |= env_hit_one(S, L, P.sc, p.x, p.y, p.z, p.w);
         }
         if (__any_sync(kFull, hit)) return true;
     }
     if (ds) {
         const bool quirk = !P.single && !(P.flags & kExactBit);
-        const int rows = A * kDetRows + A * kNumDet;
-        for (int idx = lane; idx < rows; idx += 32) {
-            if (idx < A * kDetRows) {
-                const int a = idx / kDetRows, r = idx - a * kDetRows;
+        uint32_t rm[A];
+        uint64_t cm[A];
+        int n_rows = 0, n_cross = 0;
+#pragma unroll
+        for (int a = 0; a < A; a++) {
+            const uint32_t sm = (uint32_t)(selfw >> (8 * a)) & 0xffu;
+            rm[a] = row_mask(sm, quirk);
+            cm[a] = (a < A - 1) ? joint_sphere_mask(sm) : 0ull;
+            n_rows += __popc(rm[a]);
+            n_cross += __popcll(cm[a]) * (A - 1 - a);
+        }
+        const int total = n_rows + n_cross;
+        for (int t = lane; t < total; t += 32) {
+            if (t < n_rows) {
+                int a = 0, u = t;
+#pragma unroll
+                for (int aa = 0; aa < A - 1; aa++)
+                    if (a == aa && u >= __popc(rm[aa])) {
+                        u -= __popc(rm[aa]);
+                        a = aa + 1;
+                    }
+                const int r = (int)__fns(rm[a], 0, u + 1);
                 const int s1 = det_row_first(r);
                 const int pi = quirk ? r : s1; // composite robots read sphere r (panda_four.cuh:390-401)
-                if (!(selfw >> (8 * a + det_joint(pi)) & 1ull)) continue;
-                const float4 p = W.P[a][pi];
-                const float r1 = W.P[a][s1].w;
+                const float4 p = W.narrow.P[a][pi];
+                const float r1 = W.narrow.P[a][s1].w;
                 for (int j = det_row_lo(r); j <= det_row_hi(r); j++) {
-                    const float4 o = W.P[a][j];
+                    const float4 o = W.narrow.P[a][j];
                     hit |= hit_sphere_sphere(p.x, p.y, p.z, r1, o.x, o.y, o.z, o.w);
                 }
             } else {
-                const int t = idx - A * kDetRows;
-                const int a = t / kNumDet, i = t - a * kNumDet;
-                if (!(selfw >> (8 * a + det_joint(i)) & 1ull)) continue;
-                const float4 p = W.P[a][i];
-                for (int b = a + 1; b < A; b++)
-                    for (int j = 0; j < kNumDet; j++) {
-                        const float4 o = W.P[b][j];
+                int u = t - n_rows, a = 0;
+#pragma unroll
+                for (int aa = 0; aa < A - 1; aa++)
+                    if (a == aa && u >= __popcll(cm[aa]) * (A - 1 - aa)) {
+                        u -= __popcll(cm[aa]) * (A - 1 - aa);
+                        a = aa + 1;
+                    }
+                const int others = A - 1 - a;
+                const int i = nth_bit(cm[a], u / others);
+                const int b = a + 1 + u % others;
+                const float4 p = W.narrow.P[a][i];
+                for (int j = 0; j < kNumJoints; j++) {
+                    const float *Tj = W.narrow.T[b][j];
+                    if (!near3(p.x, p.y, p.z, make_float4(Tj[3], Tj[7], Tj[11], P.group_r[j]), p.w)) continue;
+                    for (int s2 = det_first(j); s2 < det_first(j + 1); s2++) {
+                        const float4 o = W.narrow.P[b][s2];
                         hit |= hit_sphere_sphere(p.x, p.y, p.z, p.w, o.x, o.y, o.z, o.w);
                     }
+                }
             }
         }
         if (__any_sync(kFull, hit)) return true;
@@ -418,8 +582,7 @@ __device__ __noinline__ bool narrow_sample(const EdgeParams &P, WarpScratch &W, 
 // the kernel
 // ---------------------------------------------------------------------------
 template <int A, int SPL>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
-    validate_kernel(const __grid_constant__ EdgeParams P) {
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS) validate_kernel(const __grid_constant__ EdgeParams P) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     __shared__ float4 det_tab[kNumDet];
@@ -469,7 +632,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
         }
         for (int d = lane; d < dof; d += 32) {
             const float df = d < 32 ? diff0 : diff1;
-            W.base[d] = P.q0[e * dof + d];
+            W.base[d] = qa[d];
             if (P.rule == kRulePlain) {
                 W.stepg[d] = __fdiv_rn(df, (float)g);
                 W.delta[d] = 0.0f;
@@ -492,13 +655,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
 #pragma unroll
             for (int s = 0; s < SPL; s++) {
                 const int k = lane + 1 + 32 * s;
-                envw[s] = selfw[s] = 0;
-                if (k <= g) broad_sample<A>(P, W, S, L, seg, k, envw[s], selfw[s]);
+                broad_sample<A>(P, W, S, L, seg, k <= g ? k : g, envw[s], selfw[s]);
+                if (k > g) envw[s] = selfw[s] = 0;
                 envc[s] = flag_count(envw[s]);
                 selfc[s] = flag_count(selfw[s]);
                 tot_env += envc[s];
                 tot_self += selfc[s];
             }
+            __syncwarp();
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 tot_env += __shfl_xor_sync(kFull, tot_env, o);
@@ -507,7 +671,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
             if (P.flops) tally += P.fbp * g;
             if (tot_env == 0 && tot_self == 0) {
                 if (P.rule == kRuleConnect) {
-                    __syncwarp();
                     for (int d = lane; d < dof; d += 32) W.base[d] = __fadd_rn(W.base[d], W.delta[d]);
                     __syncwarp();
                 }
@@ -581,13 +744,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
                     }
                 }
                 const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
-                if (narrow_sample<A>(P, W, S, L, det_tab, seg, bit + 1, ew, sw, dE, dS)) {
+                const bool h = narrow_sample<A>(P, W, S, L, det_tab, seg, bit + 1, ew, sw, dE, dS);
+                __syncwarp();
+                if (h) {
                     first = seg * g + bit + 1;
                     break;
                 }
             }
             if (P.rule == kRuleConnect) {
-                __syncwarp();
                 for (int d = lane; d < dof; d += 32) W.base[d] = __fadd_rn(W.base[d], W.delta[d]);
                 __syncwarp();
             }

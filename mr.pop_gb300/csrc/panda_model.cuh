@@ -105,6 +105,9 @@ __host__ __device__ __forceinline__ constexpr int det_joint(int i) {
     return i < 1 ? 0 : i < 5 ? 1 : i < 9 ? 2 : i < 13 ? 3 : i < 17 ? 4 : i < 29 ? 5 : i < 32 ? 6 : 7;
 }
 __host__ __device__ __forceinline__ constexpr int approx_joint(int i) { return i < 7 ? i : 7; }
+__host__ __device__ __forceinline__ constexpr int det_first(int j) {
+    return j == 0 ? 0 : j == 1 ? 1 : j == 2 ? 5 : j == 3 ? 9 : j == 4 ? 13 : j == 5 ? 17 : j == 6 ? 29 : j == 7 ? 32 : 59;
+}
 __host__ __device__ __forceinline__ constexpr int det_count(int j) {
     return j == 0 ? 1 : j < 5 ? 4 : j == 5 ? 12 : j == 6 ? 3 : 27;
 }

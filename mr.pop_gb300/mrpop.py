@@ -28,7 +28,7 @@ EXPORTED = [
     "mrpop_scene_create", "mrpop_scene_destroy", "mrpop_scene_status", "mrpop_robotset_create",
     "mrpop_robotset_destroy", "mrpop_validate_edges", "mrpop_validate_segments", "mrpop_workspace_create",
     "mrpop_workspace_destroy", "mrpop_validate_edges_host", "mrpop_fk_spheres", "mrpop_count_flops",
-    "mrpop_debug_trig", "mrpop_last_error", "mrpop_version",
+    "mrpop_debug_trig", "mrpop_fp32_peak_probe", "mrpop_last_error", "mrpop_version",
 ]
 
 
@@ -76,6 +76,7 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
         "mrpop_fk_spheres": [vp, i32, vp, i64, i32, vp, vp],
         "mrpop_count_flops": [vp, vp, vp, vp, i64, i32, i32, f32, u32, i32, vp, vp],
         "mrpop_debug_trig": [vp, i64, vp, vp, vp],
+        "mrpop_fp32_peak_probe": [i32, i32, vp, C.POINTER(C.c_double), vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -241,6 +242,14 @@ def debug_trig(x, lib: C.CDLL | None = None, stream=None):
     s = torch.empty_like(x)
     _check(lib, lib.mrpop_debug_trig(x.data_ptr(), x.numel(), c.data_ptr(), s.data_ptr(), _stream_ptr(stream)))
     return c, s
+
+
+def fp32_peak_probe(blocks: int, iters: int, scratch, stream=None, lib: C.CDLL | None = None) -> float:
+    """Launch the FMA loop; returns its flop count (time it with CUDA events)."""
+    lib = lib or library()
+    f = C.c_double()
+    _check(lib, lib.mrpop_fp32_peak_probe(blocks, iters, scratch.data_ptr(), C.byref(f), _stream_ptr(stream)))
+    return f.value
 
 
 class Workspace:
