@@ -51,6 +51,8 @@ const float kFiveBase[5][16] = {
     {1.00000000f, 0.00000000f, 0.f, -0.60000000f, 0.00000000f, 1.00000000f, 0.f, -0.20000000f, 0.f, 0.f, 1.f,
      0.10000000f, 0.f, 0.f, 0.f, 1.f}};
 
+unsigned long long *g_phase_counters = nullptr;  // development phase timers (see edge_kernel.cuh)
+
 size_t warp_scratch_bytes() { return sizeof(mrpop::WarpScratch) * mrpop::kWarpsPerBlock; }
 
 // Largest staged scene: the block's dynamic shared memory stays below this.
@@ -272,6 +274,7 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
     p.scene = scene->d_buf;
     p.sc = scene->counts;
     p.status = scene->d_status;
+    p.phase = g_phase_counters;
     p.env_test_flops = scene->env_test_flops;
     for (int j = 0; j < mrpop::kNumJoints; j++) {
         double r = 0.0;
@@ -280,6 +283,24 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
             r = std::fmax(r, std::sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z) + d.r);
         }
         p.group_r[j] = (float)(r * 1.001 + mrpop::kCullMargin);
+    }
+    static const int kGroupFirst[12] = {0, 1, 5, 9, 13, 17, 19, 21, 29, 32, 37, 59};
+    for (int g = 0; g < 11; g++) {
+        double lo[3] = {1e9, 1e9, 1e9}, hi[3] = {-1e9, -1e9, -1e9};
+        for (int i = kGroupFirst[g]; i < kGroupFirst[g + 1]; i++) {
+            const double v[3] = {mrpop::kDet[i].x, mrpop::kDet[i].y, mrpop::kDet[i].z};
+            for (int c = 0; c < 3; c++) {
+                lo[c] = std::fmin(lo[c], v[c]);
+                hi[c] = std::fmax(hi[c], v[c]);
+            }
+        }
+        const double cx = 0.5 * (lo[0] + hi[0]), cy = 0.5 * (lo[1] + hi[1]), cz = 0.5 * (lo[2] + hi[2]);
+        double r = 0.0;
+        for (int i = kGroupFirst[g]; i < kGroupFirst[g + 1]; i++) {
+            const mrpop::SphereDef &d = mrpop::kDet[i];
+            r = std::fmax(r, std::sqrt((d.x - cx) * (d.x - cx) + (d.y - cy) * (d.y - cy) + (d.z - cz) * (d.z - cz)) + d.r);
+        }
+        p.grp[g] = make_float4((float)cx, (float)cy, (float)cz, (float)(r * 1.001 + mrpop::kCullMargin));
     }
     const int A = arm >= 0 ? 1 : robots->n_arms;
     for (int a = 0; a < A; a++)
@@ -368,6 +389,10 @@ cudaError_t launch_validate(int arms, const EdgeParams &p, size_t smem_bytes, cu
 }  // namespace mrpop
 
 extern "C" {
+
+// Development hook: device array of >= 16 counters for builds with
+// MRPOP_PHASE_TIMERS (ignored otherwise).  Not part of the public header.
+void mrpop_dev_phase_counters(unsigned long long *dev_counters) { g_phase_counters = dev_counters; }
 
 mrpop_status mrpop_validate_edges(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
                                   const float *q1, int64_t n_edges, int granularity, uint32_t flags, int arm,

@@ -28,9 +28,32 @@ namespace mrpop {
 #ifndef MRPOP_MIN_BLOCKS
 #define MRPOP_MIN_BLOCKS 4
 #endif
+// Optional per-phase warp timers (development builds with
+// -DMRPOP_PHASE_TIMERS; compiled out otherwise): clock64() deltas of lane 0
+// accumulated into P.phase[i].
+#ifdef MRPOP_PHASE_TIMERS
+#define MRPOP_PHASE_START() long long _phase_t = clock64();
+#define MRPOP_PHASE(P, i)                                                                          \
+    do {                                                                                           \
+        const long long _n = clock64();                                                            \
+        if ((P).phase && (threadIdx.x & 31) == 0)                                                  \
+            atomicAdd((P).phase + (i), (unsigned long long)(_n - _phase_t));                       \
+        _phase_t = _n;                                                                             \
+    } while (0)
+#define MRPOP_COUNT(P, i, v)                                                                       \
+    do {                                                                                           \
+        if ((P).phase && (threadIdx.x & 31) == 0) atomicAdd((P).phase + (i), (unsigned long long)(v)); \
+    } while (0)
+#else
+#define MRPOP_PHASE_START()
+#define MRPOP_PHASE(P, i) do { } while (0)
+#define MRPOP_COUNT(P, i, v) do { } while (0)
+#endif
+
 constexpr int kWarpsPerBlock = 4;
 constexpr int kMaxArms = 5;
 constexpr int kMaxDof = 7 * kMaxArms;
+constexpr int kCrossStash = 16;        // per-lane arm-vs-arm candidate spheres
 constexpr float kCullMargin = 1e-3f;   // metres added to every bounding radius
 constexpr float kApproxMaxR = 0.176f;  // largest broad-phase sphere radius
 
@@ -81,7 +104,9 @@ struct EdgeParams {
     const float4 *scene;
     SceneCounts sc;
     unsigned int *status;
+    unsigned long long *phase;  // phase timers (MRPOP_PHASE_TIMERS builds only)
     float group_r[kNumJoints];  // bounding radius of each joint's detailed spheres (+margin)
+    float4 grp[11];             // detailed sub-group bounds in their joint frame (+margin)
     float base[kMaxArms][12];   // row-major 3x4 per arm of this check
 };
 
@@ -98,9 +123,16 @@ struct WarpScratch {
             float low[kNumApprox][3][32];   // per-lane approx spheres of a lower arm
         } broad;
         struct {
+            float4 dbound[kMaxArms][32];    // per-lane bound of each arm's detailed spheres
+            union {
+                float stash[kDetRows][3][32];        // first sphere of each detailed self row
+                float cstash[kCrossStash][4][32];    // arm-vs-arm candidates {x, y, z, r}
+            };
+        } lanes;
+        struct {
             float T[kMaxArms][kNumJoints][12];
             float4 P[kMaxArms][kNumDet];     // detailed sphere centres (w = radius)
-        } narrow;
+        } coop;
     };
 };
 
@@ -340,7 +372,9 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
     auto &low = W.broad.low;
 #pragma unroll 1
     for (int b = 0; b < A; b++) {
+        MRPOP_PHASE_START();
         const float4 cb = fk_approx_lane(P.base[b], W, P.rule, seg, P.single ? 0 : b, k, cur, lane);
+        MRPOP_PHASE(P, 0);
         if (do_env) {
             const uint32_t m = env_mask_approx(S, L, P.sc, cur, lane, cb);
             uint32_t jm = 0;
@@ -349,6 +383,7 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
                 if (m >> i & 1u) jm |= 1u << approx_joint(i);
             envw |= (uint64_t)jm << (8 * b);
         }
+        MRPOP_PHASE(P, 1);
         if (!do_self) continue;
         uint32_t jm = 0;
 #pragma unroll 1
@@ -359,6 +394,7 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
                 jm |= 1u << approx_joint(s1);
         }
         selfw |= (uint64_t)jm << (8 * b);
+        MRPOP_PHASE(P, 2);
         if (A == 1) continue;
         W.broad.armbs[b][lane] = cb;
         // arm-vs-arm against every lower arm a < b; flags go to arm a
@@ -394,6 +430,7 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
             }
             selfw |= (uint64_t)am << (8 * a);
         }
+        MRPOP_PHASE(P, 3);
     }
 }
 
@@ -438,7 +475,7 @@ __device__ __forceinline__ double narrow_flops(const EdgeParams &P, int A, uint6
 }
 
 // ---------------------------------------------------------------------------
-// narrow phase of one sample (whole warp)
+// narrow phase
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint64_t joint_sphere_mask(uint32_t jm) {
     uint64_t m = 0;
@@ -467,115 +504,395 @@ __device__ __forceinline__ uint32_t row_mask(uint32_t sm, bool quirk) {
     return m;
 }
 
-template <int A>
-__device__ __noinline__ bool narrow_sample(const EdgeParams &P, WarpScratch &W, const float4 *S, const SceneLayout &L,
-                                           const float4 *det_tab, int seg, int k, uint64_t envw, uint64_t selfw,
-                                           bool de, bool ds) {
-    const int lane = threadIdx.x & 31;
-    // joint frames of every arm
-    if (lane < A) {
-        float q[7];
-        sample_q(W, P.rule, seg, P.single ? 0 : lane, k, q);
-        Xf T;
-        load_base(T, P.base[lane]);
-#pragma unroll
-        for (int i = 0; i < 12; i++) W.narrow.T[lane][0][i] = T.m[i];
-#pragma unroll
-        for (int j = 1; j < kNumJoints; j++) {
-            joint_step_rt(T, q[j - 1], j);
-#pragma unroll
-            for (int i = 0; i < 12; i++) W.narrow.T[lane][j][i] = T.m[i];
-        }
+// Row bookkeeping of the detailed self check, per sphere index i:
+//   first[q][i]  rows whose first-read sphere is i (q = 1: the composite
+//                robots' reading, sphere r; q = 0: sphere first(r))
+//   cover[i]     rows whose target range lo..hi contains i
+// and the same ORed over the spheres of each joint.
+struct RowTab {
+    uint32_t first[2][kNumDet];
+    uint32_t cover[kNumDet];
+    uint32_t jfirst[2][kNumJoints];
+    uint32_t jcover[kNumJoints];
+};
+
+__host__ __device__ constexpr RowTab make_row_tab() {
+    RowTab t{};
+    for (int r = 0; r < kDetRows; r++) {
+        t.first[0][det_row_first(r)] |= 1u << r;
+        t.first[1][r] |= 1u << r;
+        for (int i = det_row_lo(r); i <= det_row_hi(r); i++) t.cover[i] |= 1u << r;
     }
-    __syncwarp();
-    for (int idx = lane; idx < A * kNumDet; idx += 32) {
-        const int a = idx / kNumDet, i = idx - a * kNumDet;
-        const float4 s = det_tab[i];
-        const float3 p = place_rt(W.narrow.T[a][det_joint(i)], s);
-        W.narrow.P[a][i] = make_float4(p.x, p.y, p.z, s.w);
+    for (int i = 0; i < kNumDet; i++) {
+        const int j = det_joint(i);
+        t.jfirst[0][j] |= t.first[0][i];
+        t.jfirst[1][j] |= t.first[1][i];
+        t.jcover[j] |= t.cover[i];
     }
-    __syncwarp();
-    bool hit = false;
-    if (de) {
-        // dense list of (arm, sphere) with the env flag on the sphere's joint
-        uint64_t m[A];
-        int total = 0;
-#pragma unroll
-        for (int a = 0; a < A; a++) {
-            m[a] = joint_sphere_mask((uint32_t)(envw >> (8 * a)) & 0xffu) & ~1ull; // sphere 0 is never env-tested
-            total += __popcll(m[a]);
-        }
-        for (int t = lane; t < total; t += 32) {
-            int a = 0, u = t;
-#pragma unroll
-            for (int aa = 0; aa < A - 1; aa++)
-                if (a == aa && u >= __popcll(m[aa])) {
-                    u -= __popcll(m[aa]);
-                    a = aa + 1;
-                }
-            const int i = nth_bit(m[a], u);
-            const float4 p = W.narrow.P[a][i];
-            hit |= env_hit_one(S, L, P.sc, p.x, p.y, p.z, p.w);
-        }
-        if (__any_sync(kFull, hit)) return true;
+    return t;
+}
+
+static __constant__ RowTab c_rows = make_row_tab();
+
+// Detailed sphere centre, transform in registers (the reference's full
+// expression, panda_four.cuh:363-366).
+__device__ __forceinline__ float3 place_reg(const Xf &T, float4 s) {
+    float3 p;
+    p.x = __fadd_rn(__fmaf_rn(T.m[2], s.z, pair_fma(T.m[0], s.x, T.m[1], s.y)), T.m[3]);
+    p.y = __fadd_rn(__fmaf_rn(T.m[6], s.z, pair_fma(T.m[4], s.x, T.m[5], s.y)), T.m[7]);
+    p.z = __fadd_rn(__fmaf_rn(T.m[10], s.z, pair_fma(T.m[8], s.x, T.m[9], s.y)), T.m[11]);
+    return p;
+}
+
+// Sub-groups of the detailed spheres (contiguous index ranges within one
+// joint): [0] [1-4] [5-8] [9-12] [13-16] [17-18] [19-20] [21-28] [29-31]
+// [32-36] [37-58].  EdgeParams::grp holds each group's bounding sphere in its
+// joint frame; a group's world bound is that centre through the joint frame.
+constexpr int kNumGroups = 11;
+__host__ __device__ __forceinline__ constexpr int grp_first(int g) {
+    return g == 0 ? 0 : g == 1 ? 1 : g == 2 ? 5 : g == 3 ? 9 : g == 4 ? 13 : g == 5 ? 17 : g == 6 ? 19 : g == 7 ? 21
+         : g == 8 ? 29 : g == 9 ? 32 : g == 10 ? 37 : 59;
+}
+// groups of joint j: [jgrp_first(j), jgrp_first(j + 1))
+__host__ __device__ __forceinline__ constexpr int jgrp_first(int j) {
+    return j < 5 ? j : j == 5 ? 5 : j == 6 ? 8 : j == 7 ? 9 : 11;
+}
+
+// Exact env test of one sphere against obstacle o (index over all classes in
+// the bound order cuboids, z-cuboids, capsules, z-capsules, spheres).
+__device__ __forceinline__ bool env_exact(const float4 *S, const SceneLayout &L, const SceneCounts &C, int o, float x,
+                                          float y, float z, float r) {
+    if (o < C.n_cub) {
+        const float4 *c = S + L.cub + 4 * o;
+        return hit_cuboid(c[0], c[1], c[2], c[3], x, y, z, __fmul_rn(r, r));
     }
-    if (ds) {
-        const bool quirk = !P.single && !(P.flags & kExactBit);
-        uint32_t rm[A];
-        uint64_t cm[A];
-        int n_rows = 0, n_cross = 0;
-#pragma unroll
-        for (int a = 0; a < A; a++) {
-            const uint32_t sm = (uint32_t)(selfw >> (8 * a)) & 0xffu;
-            rm[a] = row_mask(sm, quirk);
-            cm[a] = (a < A - 1) ? joint_sphere_mask(sm) : 0ull;
-            n_rows += __popc(rm[a]);
-            n_cross += __popcll(cm[a]) * (A - 1 - a);
-        }
-        const int total = n_rows + n_cross;
-        for (int t = lane; t < total; t += 32) {
-            if (t < n_rows) {
-                int a = 0, u = t;
-#pragma unroll
-                for (int aa = 0; aa < A - 1; aa++)
-                    if (a == aa && u >= __popc(rm[aa])) {
-                        u -= __popc(rm[aa]);
-                        a = aa + 1;
-                    }
-                const int r = (int)__fns(rm[a], 0, u + 1);
-                const int s1 = det_row_first(r);
-                const int pi = quirk ? r : s1; // composite robots read sphere r (panda_four.cuh:390-401)
-                const float4 p = W.narrow.P[a][pi];
-                const float r1 = W.narrow.P[a][s1].w;
-                for (int j = det_row_lo(r); j <= det_row_hi(r); j++) {
-                    const float4 o = W.narrow.P[a][j];
-                    hit |= hit_sphere_sphere(p.x, p.y, p.z, r1, o.x, o.y, o.z, o.w);
-                }
-            } else {
-                int u = t - n_rows, a = 0;
-#pragma unroll
-                for (int aa = 0; aa < A - 1; aa++)
-                    if (a == aa && u >= __popcll(cm[aa]) * (A - 1 - aa)) {
-                        u -= __popcll(cm[aa]) * (A - 1 - aa);
-                        a = aa + 1;
-                    }
-                const int others = A - 1 - a;
-                const int i = nth_bit(cm[a], u / others);
-                const int b = a + 1 + u % others;
-                const float4 p = W.narrow.P[a][i];
-                for (int j = 0; j < kNumJoints; j++) {
-                    const float *Tj = W.narrow.T[b][j];
-                    if (!near3(p.x, p.y, p.z, make_float4(Tj[3], Tj[7], Tj[11], P.group_r[j]), p.w)) continue;
-                    for (int s2 = det_first(j); s2 < det_first(j + 1); s2++) {
-                        const float4 o = W.narrow.P[b][s2];
-                        hit |= hit_sphere_sphere(p.x, p.y, p.z, p.w, o.x, o.y, o.z, o.w);
-                    }
-                }
+    o -= C.n_cub;
+    if (o < C.n_zcub) {
+        const float4 *c = S + L.zcub + 4 * o;
+        return hit_zcuboid(c[0], c[1], c[2], x, y, z, __fmul_rn(r, r));
+    }
+    o -= C.n_zcub;
+    if (o < C.n_cap) return hit_capsule(S[L.cap + 2 * o], S[L.cap + 2 * o + 1], x, y, z, r);
+    o -= C.n_cap;
+    if (o < C.n_zcap) return hit_zcapsule(S[L.zcap + 2 * o], S[L.zcap + 2 * o + 1], x, y, z, r);
+    o -= C.n_zcap;
+    const float4 c0 = S[L.sph + o];
+    return hit_sphere_sphere(c0.x, c0.y, c0.z, c0.w, x, y, z, r);
+}
+
+// Env test of the spheres of group g (sphere 0 is never env-tested): obstacles
+// are screened against the group bound in chunks of 64, then per sphere.
+static __device__ __noinline__ bool env_group(const float4 *S, const SceneLayout &L, const SceneCounts &C,
+                                              const Xf &T, int g, float4 gl) {
+    const float3 gc = place_reg(T, gl);
+    const int n_obst = C.n_cub + C.n_zcub + C.n_cap + C.n_zcap + C.n_sph;
+    const int i0 = grp_first(g) == 0 ? 1 : grp_first(g), i1 = grp_first(g + 1);
+    for (int base = 0; base < n_obst; base += 64) {
+        const int n = min(64, n_obst - base);
+        uint64_t m = 0;
+        for (int t = 0; t < n; t++)
+            if (near3(gc.x, gc.y, gc.z, S[L.b_cub + base + t], gl.w)) m |= 1ull << t;
+        if (!m) continue;
+        for (int i = i0; i < i1; i++) {
+            const float4 sd = c_det[i];
+            const float3 p = place_reg(T, sd);
+            uint64_t mm = m;
+            while (mm) {
+                const int t = __ffsll((long long)mm) - 1;
+                mm &= mm - 1;
+                if (near3(p.x, p.y, p.z, S[L.b_cub + base + t], sd.w) &&
+                    env_exact(S, L, C, base + t, p.x, p.y, p.z, sd.w))
+                    return true;
             }
         }
-        if (__any_sync(kFull, hit)) return true;
     }
     return false;
+}
+
+// Per-lane state of the lane-parallel detailed check of one arm.
+struct LaneCtx {
+    uint32_t em;  // env-flagged joints
+    uint32_t rm;  // flagged detailed self rows
+    int quirk;
+    bool hit;
+};
+
+// Joint J of one arm, frame T: env tests of an env-flagged joint, stash of the
+// first spheres of flagged rows, and the row tests whose targets are here
+// (screened by the target group's bound).
+template <int J>
+__device__ __forceinline__ void lane_joint(const EdgeParams &P, const Xf &T, LaneCtx &c, WarpScratch &W,
+                                           const float4 *S, const SceneLayout &L, const float4 *det_tab, int lane) {
+    if (c.hit) return;
+    if (c.em >> J & 1u) {
+#pragma unroll 1
+        for (int g = jgrp_first(J); g < jgrp_first(J + 1); g++)
+            if (env_group(S, L, P.sc, T, g, P.grp[g])) {
+                c.hit = true;
+                return;
+            }
+    }
+    if (!c.rm) return;
+    uint32_t m1 = c.rm & c_rows.jfirst[c.quirk][J];
+    while (m1) {
+        const int r = __ffs(m1) - 1;
+        m1 &= m1 - 1;
+        const float3 p = place_reg(T, c_det[c.quirk ? r : det_row_first(r)]);
+        W.lanes.stash[r][0][lane] = p.x;
+        W.lanes.stash[r][1][lane] = p.y;
+        W.lanes.stash[r][2][lane] = p.z;
+    }
+#pragma unroll 1
+    for (int g = jgrp_first(J); g < jgrp_first(J + 1); g++) {
+        uint32_t rows = c.rm & c_rows.cover[grp_first(g)];
+        if (!rows) continue;
+        const float4 gl = P.grp[g];
+        const float3 gc = place_reg(T, gl);
+        uint32_t nr = 0;
+        while (rows) {
+            const int r = __ffs(rows) - 1;
+            rows &= rows - 1;
+            if (near3(W.lanes.stash[r][0][lane], W.lanes.stash[r][1][lane], W.lanes.stash[r][2][lane],
+                      make_float4(gc.x, gc.y, gc.z, gl.w), det_tab[det_row_first(r)].w))
+                nr |= 1u << r;
+        }
+        if (!nr) continue;
+        bool h = false;
+        for (int i = grp_first(g); i < grp_first(g + 1); i++) {
+            const float4 sd = c_det[i];
+            const float3 p = place_reg(T, sd);
+            uint32_t m = nr;
+            while (m) {
+                const int r = __ffs(m) - 1;
+                m &= m - 1;
+                h |= hit_sphere_sphere(W.lanes.stash[r][0][lane], W.lanes.stash[r][1][lane],
+                                       W.lanes.stash[r][2][lane], det_tab[det_row_first(r)].w, p.x, p.y, p.z, sd.w);
+            }
+        }
+        if (h) {
+            c.hit = true;
+            return;
+        }
+    }
+}
+
+#define MRPOP_ORIGIN(J)                                                                                \
+    ox[J] = T.m[3];                                                                                    \
+    oy[J] = T.m[7];                                                                                    \
+    oz[J] = T.m[11];
+
+// Lane-parallel detailed check of this lane's sample: every arm's chain is
+// rebuilt in registers; env tests of env-flagged joints and the intra-arm rows
+// of self-flagged joints run as the frames stream by (the first sphere of
+// each row is stashed until its targets come).  Writes each arm's detailed
+// bound for the arm-vs-arm part.  Returns true if a test fired.
+template <int A>
+static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch &W, const float4 *S,
+                                                const SceneLayout &L, const float4 *det_tab, int seg, int k,
+                                                uint64_t envw, uint64_t selfw, bool de, bool ds, float max_group_r) {
+    const int lane = threadIdx.x & 31;
+    LaneCtx c;
+    c.quirk = (!P.single && !(P.flags & kExactBit)) ? 1 : 0;
+    c.hit = false;
+#pragma unroll 1
+    for (int a = 0; a < A && !c.hit; a++) {
+        c.em = de ? (uint32_t)(envw >> (8 * a)) & 0xffu : 0u;
+        const uint32_t sm = ds ? (uint32_t)(selfw >> (8 * a)) & 0xffu : 0u;
+        c.rm = sm ? row_mask(sm, c.quirk != 0) : 0u;
+        float q[7];
+        sample_q(W, P.rule, seg, P.single ? 0 : a, k, q);
+        Xf T;
+        load_base(T, P.base[a]);
+        float ox[kNumJoints], oy[kNumJoints], oz[kNumJoints];
+        MRPOP_ORIGIN(0)
+        lane_joint<0>(P, T, c, W, S, L, det_tab, lane);
+        joint_step<1>(T, q[0]);
+        MRPOP_ORIGIN(1)
+        lane_joint<1>(P, T, c, W, S, L, det_tab, lane);
+        joint_step<2>(T, q[1]);
+        MRPOP_ORIGIN(2)
+        lane_joint<2>(P, T, c, W, S, L, det_tab, lane);
+        joint_step<3>(T, q[2]);
+        MRPOP_ORIGIN(3)
+        lane_joint<3>(P, T, c, W, S, L, det_tab, lane);
+        joint_step<4>(T, q[3]);
+        MRPOP_ORIGIN(4)
+        lane_joint<4>(P, T, c, W, S, L, det_tab, lane);
+        joint_step<5>(T, q[4]);
+        MRPOP_ORIGIN(5)
+        lane_joint<5>(P, T, c, W, S, L, det_tab, lane);
+        joint_step<6>(T, q[5]);
+        MRPOP_ORIGIN(6)
+        lane_joint<6>(P, T, c, W, S, L, det_tab, lane);
+        joint_step<7>(T, q[6]);
+        MRPOP_ORIGIN(7)
+        lane_joint<7>(P, T, c, W, S, L, det_tab, lane);
+        float lx = ox[0], hx = ox[0], ly = oy[0], hy = oy[0], lz = oz[0], hz = oz[0];
+#pragma unroll
+        for (int j = 1; j < kNumJoints; j++) {
+            lx = fminf(lx, ox[j]);
+            hx = fmaxf(hx, ox[j]);
+            ly = fminf(ly, oy[j]);
+            hy = fmaxf(hy, oy[j]);
+            lz = fminf(lz, oz[j]);
+            hz = fmaxf(hz, oz[j]);
+        }
+        const float cx = 0.5f * (lx + hx), cy = 0.5f * (ly + hy), cz = 0.5f * (lz + hz);
+        float r2 = 0.f;
+#pragma unroll
+        for (int j = 0; j < kNumJoints; j++) {
+            const float dx = ox[j] - cx, dy = oy[j] - cy, dz = oz[j] - cz;
+            r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
+        }
+        W.lanes.dbound[a][lane] = make_float4(cx, cy, cz, sqrtf(r2) * 1.0001f + max_group_r);
+    }
+    return c.hit;
+}
+
+// Pairs (a, b), a < b, whose arm-vs-arm detailed test this lane's sample
+// needs: arm a has self flags and the two arms' detailed bounds meet.
+// Bit index of pair (a, b) is a * kMaxArms + b.
+template <int A>
+__device__ __forceinline__ uint32_t cross_pairs(const WarpScratch &W, uint64_t selfw, bool ds) {
+    const int lane = threadIdx.x & 31;
+    uint32_t pm = 0;
+    if (!ds) return 0;
+#pragma unroll
+    for (int a = 0; a < A - 1; a++) {
+        if (!((selfw >> (8 * a)) & 0xffull)) continue;
+        const float4 ba = W.lanes.dbound[a][lane];
+#pragma unroll
+        for (int b = a + 1; b < A; b++)
+            if (near3(ba.x, ba.y, ba.z, W.lanes.dbound[b][lane], ba.w)) pm |= 1u << (a * kMaxArms + b);
+    }
+    return pm;
+}
+
+// Arm a, joint J: stash the flagged spheres (index >= from) that can reach
+// bound bb, until the stash is full; `next` receives the first sphere left out.
+template <int J>
+__device__ __forceinline__ void stash_joint(const Xf &T, uint32_t sma, float4 bb, int from, int &n, int &next,
+                                            WarpScratch &W, int lane) {
+    if (next >= 0 || !(sma >> J & 1u) || det_first(J + 1) <= from) return;
+#pragma unroll 1
+    for (int i = max(det_first(J), from); i < det_first(J + 1); i++) {
+        const float4 sd = c_det[i];
+        const float3 p = place_reg(T, sd);
+        if (!near3(p.x, p.y, p.z, bb, sd.w)) continue;
+        if (n == kCrossStash) {
+            next = i;
+            return;
+        }
+        W.lanes.cstash[n][0][lane] = p.x;
+        W.lanes.cstash[n][1][lane] = p.y;
+        W.lanes.cstash[n][2][lane] = p.z;
+        W.lanes.cstash[n][3][lane] = sd.w;
+        n++;
+    }
+}
+
+// Arm b, joint J: its spheres against the stashed spheres, by sub-group.
+template <int J>
+__device__ __forceinline__ void probe_joint(const EdgeParams &P, const Xf &T, int n, bool &hit, WarpScratch &W,
+                                            int lane) {
+    if (hit) return;
+#pragma unroll 1
+    for (int g = jgrp_first(J); g < jgrp_first(J + 1); g++) {
+        const float4 gl = P.grp[g];
+        const float3 gc = place_reg(T, gl);
+        const float4 gb = make_float4(gc.x, gc.y, gc.z, gl.w);
+        uint32_t near = 0;
+        for (int e = 0; e < n; e++)
+            if (near3(W.lanes.cstash[e][0][lane], W.lanes.cstash[e][1][lane], W.lanes.cstash[e][2][lane], gb,
+                      W.lanes.cstash[e][3][lane]))
+                near |= 1u << e;
+        if (!near) continue;
+        bool h = false;
+        for (int i = grp_first(g); i < grp_first(g + 1); i++) {
+            const float4 sd = c_det[i];
+            const float3 p = place_reg(T, sd);
+            uint32_t m = near;
+            while (m) {
+                const int e = __ffs(m) - 1;
+                m &= m - 1;
+                // sphere_1 = the lower arm's sphere (panda_four.cuh:441-443)
+                h |= hit_sphere_sphere(W.lanes.cstash[e][0][lane], W.lanes.cstash[e][1][lane],
+                                       W.lanes.cstash[e][2][lane], W.lanes.cstash[e][3][lane], p.x, p.y, p.z, sd.w);
+            }
+        }
+        if (h) {
+            hit = true;
+            return;
+        }
+    }
+}
+
+// Lane-parallel arm-vs-arm detailed test of this lane's sample for the pairs
+// in pm (every lane of the warp calls it): arm a's flagged spheres that can
+// reach arm b's bound are stashed (in chunks of kCrossStash) and arm b's
+// spheres are streamed against them.  Returns true if a test fired.
+template <int A>
+static __device__ __noinline__ bool cross_lane(const EdgeParams &P, WarpScratch &W, int seg, int k, uint64_t selfw,
+                                               uint32_t pm) {
+    const int lane = threadIdx.x & 31;
+    bool hit = false;
+#pragma unroll 1
+    for (int a = 0; a < A - 1; a++) {
+        const uint32_t sma = (uint32_t)(selfw >> (8 * a)) & 0xffu;
+#pragma unroll 1
+        for (int b = a + 1; b < A; b++) {
+            const bool need = (pm >> (a * kMaxArms + b) & 1u) && !hit;
+            if (!__any_sync(kFull, need)) continue;
+            if (!need) continue;
+            const float4 bb = W.lanes.dbound[b][lane];
+            int from = 0;
+            while (from >= 0 && !hit) {
+                float q[7];
+                int n = 0, next = -1;
+                {
+                    sample_q(W, P.rule, seg, a, k, q);
+                    Xf T;
+                    load_base(T, P.base[a]);
+                    stash_joint<0>(T, sma, bb, from, n, next, W, lane);
+                    joint_step<1>(T, q[0]);
+                    stash_joint<1>(T, sma, bb, from, n, next, W, lane);
+                    joint_step<2>(T, q[1]);
+                    stash_joint<2>(T, sma, bb, from, n, next, W, lane);
+                    joint_step<3>(T, q[2]);
+                    stash_joint<3>(T, sma, bb, from, n, next, W, lane);
+                    joint_step<4>(T, q[3]);
+                    stash_joint<4>(T, sma, bb, from, n, next, W, lane);
+                    joint_step<5>(T, q[4]);
+                    stash_joint<5>(T, sma, bb, from, n, next, W, lane);
+                    joint_step<6>(T, q[5]);
+                    stash_joint<6>(T, sma, bb, from, n, next, W, lane);
+                    joint_step<7>(T, q[6]);
+                    stash_joint<7>(T, sma, bb, from, n, next, W, lane);
+                }
+                from = next;
+                if (n == 0) break;
+                sample_q(W, P.rule, seg, b, k, q);
+                Xf T;
+                load_base(T, P.base[b]);
+                probe_joint<0>(P, T, n, hit, W, lane);
+                joint_step<1>(T, q[0]);
+                probe_joint<1>(P, T, n, hit, W, lane);
+                joint_step<2>(T, q[1]);
+                probe_joint<2>(P, T, n, hit, W, lane);
+                joint_step<3>(T, q[2]);
+                probe_joint<3>(P, T, n, hit, W, lane);
+                joint_step<4>(T, q[3]);
+                probe_joint<4>(P, T, n, hit, W, lane);
+                joint_step<5>(T, q[4]);
+                probe_joint<5>(P, T, n, hit, W, lane);
+                joint_step<6>(T, q[5]);
+                probe_joint<6>(P, T, n, hit, W, lane);
+                joint_step<7>(T, q[6]);
+                probe_joint<7>(P, T, n, hit, W, lane);
+            }
+        }
+    }
+    return hit;
 }
 
 // ---------------------------------------------------------------------------
@@ -598,6 +915,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS) validat
 
     const int g = P.g;
     const int dof = 7 * (P.single ? 1 : A);
+    float max_group_r = 0.f;
+#pragma unroll
+    for (int j = 0; j < kNumJoints; j++) max_group_r = fmaxf(max_group_r, P.group_r[j]);
     const long long nwarps = (long long)gridDim.x * kWarpsPerBlock;
 
     for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps) {
@@ -648,6 +968,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS) validat
         double tally = 0.0;
         const int nseg_run = too_many ? 0 : nseg;
         for (int seg = 0; seg < nseg_run && first == 0; seg++) {
+            MRPOP_PHASE_START();
             // ---- broad phase: this lane's samples
             uint64_t envw[SPL], selfw[SPL];
             int envc[SPL], selfc[SPL];
@@ -676,6 +997,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS) validat
                 }
                 continue;
             }
+            MRPOP_PHASE(P, 7);
             // ---- decision: which samples get the detailed check
             uint64_t cand_env = 0, cand_self = 0;
             const bool exact = P.flags & kExactBit;
@@ -727,30 +1049,27 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS) validat
                 for (int o = 16; o > 0; o >>= 1) f += __shfl_xor_sync(kFull, f, o);
                 tally += f;
             }
-            // ---- narrow phase, samples in increasing order
-            uint64_t cand = cand_env | cand_self;
-            while (cand) {
-                const int bit = __ffsll((long long)cand) - 1;
-                cand &= cand - 1;
-                const int src = bit & 31, slot = bit >> 5;
-                uint64_t ew = 0, sw = 0;
+            // ---- narrow phase: every candidate sample in parallel, one lane
+            // each; the first colliding sample is the lowest set bit
+            uint64_t hits = 0;
 #pragma unroll
-                for (int s = 0; s < SPL; s++) {
-                    const uint64_t e2 = __shfl_sync(kFull, envw[s], src);
-                    const uint64_t s2 = __shfl_sync(kFull, selfw[s], src);
-                    if (s == slot) {
-                        ew = e2;
-                        sw = s2;
-                    }
-                }
+            for (int s = 0; s < SPL; s++) {
+                const int bit = lane + 32 * s;
                 const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
-                const bool h = narrow_sample<A>(P, W, S, L, det_tab, seg, bit + 1, ew, sw, dE, dS);
-                __syncwarp();
-                if (h) {
-                    first = seg * g + bit + 1;
-                    break;
+                bool h = false;
+                uint32_t pm = 0;
+                if (dE || dS) {
+                    h = narrow_lane<A>(P, W, S, L, det_tab, seg, bit + 1, envw[s], selfw[s], dE, dS, max_group_r);
+                    if (!h && A > 1) pm = cross_pairs<A>(W, selfw[s], dS);
                 }
+                MRPOP_PHASE(P, 5);
+                if (A > 1 && __any_sync(kFull, pm != 0u)) h |= cross_lane<A>(P, W, seg, bit + 1, selfw[s], pm);
+                MRPOP_PHASE(P, 6);
+                hits |= (uint64_t)__ballot_sync(kFull, h) << (32 * s);
+                if (hits) break; // later slots hold only later samples
             }
+            const int first_bit = hits ? __ffsll((long long)hits) - 1 : 64;
+            if (first_bit < 64) first = seg * g + first_bit + 1;
             if (P.rule == kRuleConnect) {
                 for (int d = lane; d < dof; d += 32) W.base[d] = __fadd_rn(W.base[d], W.delta[d]);
                 __syncwarp();
