@@ -239,6 +239,14 @@ __device__ __forceinline__ void sample_q(const WarpScratch &W, int rule, int seg
     }
 }
 
+// One joint value (dof index i) of sample k of segment `seg`.
+__device__ __forceinline__ float sample_q1(const WarpScratch &W, int rule, int seg, int i, int k) {
+    float v = __fmaf_rn((float)k, W.stepg[i], W.base[i]);
+    if (rule == kRuleBspline || rule == kRuleShortcut)
+        for (int s = 0; s < seg; s++) v = __fadd_rn(v, W.delta[i]);
+    return v;
+}
+
 // FK of arm `qarm`'s joint values (base12) for this lane's sample; writes the
 // 11 centres into the lane's column of dst and returns a conservative bounding
 // sphere of the arm's approx spheres (w = radius).
@@ -451,7 +459,7 @@ __device__ __forceinline__ int ref_share(int cnt, int total, int g) {
 }
 
 // dense narrow-phase tally for one sample (per the flop convention)
-__device__ __forceinline__ double narrow_flops(const EdgeParams &P, int A, uint64_t envw, uint64_t selfw, bool de,
+static __device__ __noinline__ double narrow_flops(const EdgeParams &P, int A, uint64_t envw, uint64_t selfw, bool de,
                                                bool ds) {
     double f = 0.0;
     const bool quirk = !P.single && !(P.flags & kExactBit);
@@ -617,23 +625,22 @@ struct LaneCtx {
     bool hit;
 };
 
-// Joint J of one arm, frame T: env tests of an env-flagged joint, stash of the
+// Joint j of one arm, frame T: env tests of an env-flagged joint, stash of the
 // first spheres of flagged rows, and the row tests whose targets are here
 // (screened by the target group's bound).
-template <int J>
-__device__ __forceinline__ void lane_joint(const EdgeParams &P, const Xf &T, LaneCtx &c, WarpScratch &W,
+__device__ __forceinline__ void lane_joint(int j, const EdgeParams &P, const Xf &T, LaneCtx &c, WarpScratch &W,
                                            const float4 *S, const SceneLayout &L, const float4 *det_tab, int lane) {
     if (c.hit) return;
-    if (c.em >> J & 1u) {
+    if (c.em >> j & 1u) {
 #pragma unroll 1
-        for (int g = jgrp_first(J); g < jgrp_first(J + 1); g++)
+        for (int g = jgrp_first(j); g < jgrp_first(j + 1); g++)
             if (env_group(S, L, P.sc, T, g, P.grp[g])) {
                 c.hit = true;
                 return;
             }
     }
     if (!c.rm) return;
-    uint32_t m1 = c.rm & c_rows.jfirst[c.quirk][J];
+    uint32_t m1 = c.rm & c_rows.jfirst[c.quirk][j];
     while (m1) {
         const int r = __ffs(m1) - 1;
         m1 &= m1 - 1;
@@ -643,7 +650,7 @@ __device__ __forceinline__ void lane_joint(const EdgeParams &P, const Xf &T, Lan
         W.lanes.stash[r][2][lane] = p.z;
     }
 #pragma unroll 1
-    for (int g = jgrp_first(J); g < jgrp_first(J + 1); g++) {
+    for (int g = jgrp_first(j); g < jgrp_first(j + 1); g++) {
         uint32_t rows = c.rm & c_rows.cover[grp_first(g)];
         if (!rows) continue;
         const float4 gl = P.grp[g];
@@ -676,11 +683,6 @@ __device__ __forceinline__ void lane_joint(const EdgeParams &P, const Xf &T, Lan
     }
 }
 
-#define MRPOP_ORIGIN(J)                                                                                \
-    ox[J] = T.m[3];                                                                                    \
-    oy[J] = T.m[7];                                                                                    \
-    oz[J] = T.m[11];
-
 // Lane-parallel detailed check of this lane's sample: every arm's chain is
 // rebuilt in registers; env tests of env-flagged joints and the intra-arm rows
 // of self-flagged joints run as the frames stream by (the first sphere of
@@ -699,51 +701,26 @@ static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch
         c.em = de ? (uint32_t)(envw >> (8 * a)) & 0xffu : 0u;
         const uint32_t sm = ds ? (uint32_t)(selfw >> (8 * a)) & 0xffu : 0u;
         c.rm = sm ? row_mask(sm, c.quirk != 0) : 0u;
-        float q[7];
-        sample_q(W, P.rule, seg, P.single ? 0 : a, k, q);
+        const int qa = 7 * (P.single ? 0 : a);
         Xf T;
         load_base(T, P.base[a]);
-        float ox[kNumJoints], oy[kNumJoints], oz[kNumJoints];
-        MRPOP_ORIGIN(0)
-        lane_joint<0>(P, T, c, W, S, L, det_tab, lane);
-        joint_step<1>(T, q[0]);
-        MRPOP_ORIGIN(1)
-        lane_joint<1>(P, T, c, W, S, L, det_tab, lane);
-        joint_step<2>(T, q[1]);
-        MRPOP_ORIGIN(2)
-        lane_joint<2>(P, T, c, W, S, L, det_tab, lane);
-        joint_step<3>(T, q[2]);
-        MRPOP_ORIGIN(3)
-        lane_joint<3>(P, T, c, W, S, L, det_tab, lane);
-        joint_step<4>(T, q[3]);
-        MRPOP_ORIGIN(4)
-        lane_joint<4>(P, T, c, W, S, L, det_tab, lane);
-        joint_step<5>(T, q[4]);
-        MRPOP_ORIGIN(5)
-        lane_joint<5>(P, T, c, W, S, L, det_tab, lane);
-        joint_step<6>(T, q[5]);
-        MRPOP_ORIGIN(6)
-        lane_joint<6>(P, T, c, W, S, L, det_tab, lane);
-        joint_step<7>(T, q[6]);
-        MRPOP_ORIGIN(7)
-        lane_joint<7>(P, T, c, W, S, L, det_tab, lane);
-        float lx = ox[0], hx = ox[0], ly = oy[0], hy = oy[0], lz = oz[0], hz = oz[0];
-#pragma unroll
-        for (int j = 1; j < kNumJoints; j++) {
-            lx = fminf(lx, ox[j]);
-            hx = fmaxf(hx, ox[j]);
-            ly = fminf(ly, oy[j]);
-            hy = fmaxf(hy, oy[j]);
-            lz = fminf(lz, oz[j]);
-            hz = fmaxf(hz, oz[j]);
-        }
-        const float cx = 0.5f * (lx + hx), cy = 0.5f * (ly + hy), cz = 0.5f * (lz + hz);
-        float r2 = 0.f;
-#pragma unroll
+        float lx = T.m[3], hx = T.m[3], ly = T.m[7], hy = T.m[7], lz = T.m[11], hz = T.m[11];
+#pragma unroll 1
         for (int j = 0; j < kNumJoints; j++) {
-            const float dx = ox[j] - cx, dy = oy[j] - cy, dz = oz[j] - cz;
-            r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
+            if (j > 0) joint_step_rt(T, sample_q1(W, P.rule, seg, qa + j - 1, k), j);
+            lx = fminf(lx, T.m[3]);
+            hx = fmaxf(hx, T.m[3]);
+            ly = fminf(ly, T.m[7]);
+            hy = fmaxf(hy, T.m[7]);
+            lz = fminf(lz, T.m[11]);
+            hz = fmaxf(hz, T.m[11]);
+            lane_joint(j, P, T, c, W, S, L, det_tab, lane);
         }
+        // bound of every joint origin (half-diagonal of their box) plus the
+        // largest sub-group radius about a joint origin
+        const float cx = 0.5f * (lx + hx), cy = 0.5f * (ly + hy), cz = 0.5f * (lz + hz);
+        const float dx = hx - lx, dy = hy - ly, dz = hz - lz;
+        const float r2 = 0.25f * (dx * dx + dy * dy + dz * dz);
         W.lanes.dbound[a][lane] = make_float4(cx, cy, cz, sqrtf(r2) * 1.0001f + max_group_r);
     }
     return c.hit;
@@ -768,14 +745,13 @@ __device__ __forceinline__ uint32_t cross_pairs(const WarpScratch &W, uint64_t s
     return pm;
 }
 
-// Arm a, joint J: stash the flagged spheres (index >= from) that can reach
+// Arm a, joint j: stash the flagged spheres (index >= from) that can reach
 // bound bb, until the stash is full; `next` receives the first sphere left out.
-template <int J>
-__device__ __forceinline__ void stash_joint(const Xf &T, uint32_t sma, float4 bb, int from, int &n, int &next,
+__device__ __forceinline__ void stash_joint(int j, const Xf &T, uint32_t sma, float4 bb, int from, int &n, int &next,
                                             WarpScratch &W, int lane) {
-    if (next >= 0 || !(sma >> J & 1u) || det_first(J + 1) <= from) return;
+    if (next >= 0 || !(sma >> j & 1u) || det_first(j + 1) <= from) return;
 #pragma unroll 1
-    for (int i = max(det_first(J), from); i < det_first(J + 1); i++) {
+    for (int i = max(det_first(j), from); i < det_first(j + 1); i++) {
         const float4 sd = c_det[i];
         const float3 p = place_reg(T, sd);
         if (!near3(p.x, p.y, p.z, bb, sd.w)) continue;
@@ -791,13 +767,12 @@ __device__ __forceinline__ void stash_joint(const Xf &T, uint32_t sma, float4 bb
     }
 }
 
-// Arm b, joint J: its spheres against the stashed spheres, by sub-group.
-template <int J>
-__device__ __forceinline__ void probe_joint(const EdgeParams &P, const Xf &T, int n, bool &hit, WarpScratch &W,
-                                            int lane) {
+// Arm b, joint j: its spheres against the stashed spheres, by sub-group.
+__device__ __forceinline__ void probe_joint(int j, const EdgeParams &P, const Xf &T, int n, bool &hit,
+                                            WarpScratch &W, int lane) {
     if (hit) return;
 #pragma unroll 1
-    for (int g = jgrp_first(J); g < jgrp_first(J + 1); g++) {
+    for (int g = jgrp_first(j); g < jgrp_first(j + 1); g++) {
         const float4 gl = P.grp[g];
         const float3 gc = place_reg(T, gl);
         const float4 gb = make_float4(gc.x, gc.y, gc.z, gl.w);
@@ -847,48 +822,25 @@ static __device__ __noinline__ bool cross_lane(const EdgeParams &P, WarpScratch 
             const float4 bb = W.lanes.dbound[b][lane];
             int from = 0;
             while (from >= 0 && !hit) {
-                float q[7];
                 int n = 0, next = -1;
                 {
-                    sample_q(W, P.rule, seg, a, k, q);
                     Xf T;
                     load_base(T, P.base[a]);
-                    stash_joint<0>(T, sma, bb, from, n, next, W, lane);
-                    joint_step<1>(T, q[0]);
-                    stash_joint<1>(T, sma, bb, from, n, next, W, lane);
-                    joint_step<2>(T, q[1]);
-                    stash_joint<2>(T, sma, bb, from, n, next, W, lane);
-                    joint_step<3>(T, q[2]);
-                    stash_joint<3>(T, sma, bb, from, n, next, W, lane);
-                    joint_step<4>(T, q[3]);
-                    stash_joint<4>(T, sma, bb, from, n, next, W, lane);
-                    joint_step<5>(T, q[4]);
-                    stash_joint<5>(T, sma, bb, from, n, next, W, lane);
-                    joint_step<6>(T, q[5]);
-                    stash_joint<6>(T, sma, bb, from, n, next, W, lane);
-                    joint_step<7>(T, q[6]);
-                    stash_joint<7>(T, sma, bb, from, n, next, W, lane);
+#pragma unroll 1
+                    for (int j = 0; j < kNumJoints; j++) {
+                        if (j > 0) joint_step_rt(T, sample_q1(W, P.rule, seg, 7 * a + j - 1, k), j);
+                        stash_joint(j, T, sma, bb, from, n, next, W, lane);
+                    }
                 }
                 from = next;
                 if (n == 0) break;
-                sample_q(W, P.rule, seg, b, k, q);
                 Xf T;
                 load_base(T, P.base[b]);
-                probe_joint<0>(P, T, n, hit, W, lane);
-                joint_step<1>(T, q[0]);
-                probe_joint<1>(P, T, n, hit, W, lane);
-                joint_step<2>(T, q[1]);
-                probe_joint<2>(P, T, n, hit, W, lane);
-                joint_step<3>(T, q[2]);
-                probe_joint<3>(P, T, n, hit, W, lane);
-                joint_step<4>(T, q[3]);
-                probe_joint<4>(P, T, n, hit, W, lane);
-                joint_step<5>(T, q[4]);
-                probe_joint<5>(P, T, n, hit, W, lane);
-                joint_step<6>(T, q[5]);
-                probe_joint<6>(P, T, n, hit, W, lane);
-                joint_step<7>(T, q[6]);
-                probe_joint<7>(P, T, n, hit, W, lane);
+#pragma unroll 1
+                for (int j = 0; j < kNumJoints; j++) {
+                    if (j > 0) joint_step_rt(T, sample_q1(W, P.rule, seg, 7 * b + j - 1, k), j);
+                    probe_joint(j, P, T, n, hit, W, lane);
+                }
             }
         }
     }

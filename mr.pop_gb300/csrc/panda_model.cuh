@@ -186,15 +186,30 @@ __device__ __forceinline__ void joint_step(Xf &T, float q) {
     }
 }
 
+// Joints 2..7 share one form: rows of F_J are e0, A*e2, -A*e1 (A = +-1) with
+// translation (tx, ty, 0).  The reference's chains then reduce to
+//   n0 = fma(t2, A*s, t0*c), n1 = fma(t2, A*c, t0*(-s)), n2 = -A*t1,
+//   n3 = t3 + (t0*tx + t1*ty)
+// where a zero translation term contributes an exact signed zero, exactly as
+// the reference's zero products do.  {A, tx, ty} per joint 2..7:
+static __constant__ float c_joint_k[6][3] = {{-1.f, 0.f, 0.f},      {1.f, 0.f, -0.316f}, {1.f, 0.0825f, 0.f},
+                                             {-1.f, -0.0825f, 0.384f}, {1.f, 0.f, 0.f},     {1.f, 0.088f, 0.f}};
+
 __device__ __forceinline__ void joint_step_rt(Xf &T, float q, int j) {
-    switch (j) {
-    case 1: joint_step<1>(T, q); break;
-    case 2: joint_step<2>(T, q); break;
-    case 3: joint_step<3>(T, q); break;
-    case 4: joint_step<4>(T, q); break;
-    case 5: joint_step<5>(T, q); break;
-    case 6: joint_step<6>(T, q); break;
-    default: joint_step<7>(T, q); break;
+    if (j == 1) {
+        joint_step<1>(T, q);
+        return;
+    }
+    const float A = c_joint_k[j - 2][0], tx = c_joint_k[j - 2][1], ty = c_joint_k[j - 2][2];
+    const float c = __cosf(q);
+    const float s = __sinf(q);
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        const float t0 = T.m[r * 4 + 0], t1 = T.m[r * 4 + 1], t2 = T.m[r * 4 + 2], t3 = T.m[r * 4 + 3];
+        T.m[r * 4 + 0] = __fmaf_rn(t2, A * s, __fmul_rn(t0, c));
+        T.m[r * 4 + 1] = __fmaf_rn(t2, A * c, __fmul_rn(t0, -s));
+        T.m[r * 4 + 2] = -A * t1;
+        T.m[r * 4 + 3] = __fadd_rn(t3, pair_fma(t0, tx, t1, ty));
     }
 }
 
