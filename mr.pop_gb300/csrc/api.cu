@@ -53,6 +53,34 @@ const float kFiveBase[5][16] = {
 
 unsigned long long *g_phase_counters = nullptr;  // development phase timers (see edge_kernel.cuh)
 
+// Per-device pool for the split pipeline's stream-ordered scratch; keeps
+// freed memory cached (release threshold = max) so steady-state calls do not
+// map new memory.  Created on first use, never destroyed.
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[64] = {};
+
+cudaError_t scratch_pool(cudaMemPool_t *out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool;
+        e = cudaMemPoolCreate(&pool, &props);
+        if (e != cudaSuccess) return e;
+        uint64_t threshold = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+        g_pools[dev] = pool;
+    }
+    *out = g_pools[dev];
+    return cudaSuccess;
+}
+
 size_t warp_scratch_bytes() { return sizeof(mrpop::WarpScratch) * mrpop::kWarpsPerBlock; }
 
 // Largest staged scene: the block's dynamic shared memory stays below this.
@@ -320,7 +348,26 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
         p.first_hit = tmp_first;
     }
     const size_t smem = (size_t)scene->total_f4 * sizeof(float4) + warp_scratch_bytes();
-    cudaError_t err = mrpop::launch_validate(A, p, smem, stream);
+    cudaError_t err;
+    if (rule == MRPOP_RULE_PLAIN) {
+        // split pipeline: flags of every sample and candidate masks in stream-ordered scratch
+        const int spl = g > 32 ? 2 : 1;
+        const size_t flag_bytes = (size_t)n_edges * 32 * spl * 2 * sizeof(uint64_t);
+        const size_t mask_bytes = (size_t)n_edges * 2 * sizeof(uint64_t);
+        void *scratch = nullptr;
+        cudaMemPool_t pool;
+        err = scratch_pool(&pool);
+        if (err == cudaSuccess) err = cudaMallocFromPoolAsync(&scratch, flag_bytes + mask_bytes, pool, stream);
+        if (err == cudaSuccess) {
+            p.sflags = (uint64_t *)scratch;
+            p.smasks = (uint64_t *)((char *)scratch + flag_bytes);
+            err = mrpop::launch_validate(A, mrpop::kBroad, p, smem, stream);
+            if (err == cudaSuccess) err = mrpop::launch_validate(A, mrpop::kNarrow, p, smem, stream);
+            cudaFreeAsync(scratch, stream);
+        }
+    } else {
+        err = mrpop::launch_validate(A, mrpop::kFused, p, smem, stream);
+    }
     if (tmp_valid) cudaFreeAsync(tmp_valid, stream);
     if (tmp_first) cudaFreeAsync(tmp_first, stream);
     if (err != cudaSuccess) return cuda_fail(err, "validate: launch");
@@ -376,13 +423,13 @@ __global__ void trig_kernel(const float *x, long long n, float *c, float *s) {
 }  // namespace
 
 namespace mrpop {
-cudaError_t launch_validate(int arms, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream) {
+cudaError_t launch_validate(int arms, KernelKind kind, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream) {
     switch (arms) {
-    case 1: return launch_validate_arms<1>(p, smem_bytes, stream);
-    case 2: return launch_validate_arms<2>(p, smem_bytes, stream);
-    case 3: return launch_validate_arms<3>(p, smem_bytes, stream);
-    case 4: return launch_validate_arms<4>(p, smem_bytes, stream);
-    case 5: return launch_validate_arms<5>(p, smem_bytes, stream);
+    case 1: return launch_validate_arms<1>(kind, p, smem_bytes, stream);
+    case 2: return launch_validate_arms<2>(kind, p, smem_bytes, stream);
+    case 3: return launch_validate_arms<3>(kind, p, smem_bytes, stream);
+    case 4: return launch_validate_arms<4>(kind, p, smem_bytes, stream);
+    case 5: return launch_validate_arms<5>(kind, p, smem_bytes, stream);
     default: return cudaErrorInvalidValue;
     }
 }

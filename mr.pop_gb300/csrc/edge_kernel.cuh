@@ -105,6 +105,8 @@ struct EdgeParams {
     SceneCounts sc;
     unsigned int *status;
     unsigned long long *phase;  // phase timers (MRPOP_PHASE_TIMERS builds only)
+    uint64_t *sflags;           // split pipeline: per-sample {env, self} flag words
+    uint64_t *smasks;           // split pipeline: per-edge {env, self} candidate masks
     float group_r[kNumJoints];  // bounding radius of each joint's detailed spheres (+margin)
     float4 grp[11];             // detailed sub-group bounds in their joint frame (+margin)
     float base[kMaxArms][12];   // row-major 3x4 per arm of this check
@@ -848,30 +850,188 @@ static __device__ __noinline__ bool cross_lane(const EdgeParams &P, WarpScratch 
 }
 
 // ---------------------------------------------------------------------------
-// the kernel
+// per-edge building blocks shared by the kernels
+// ---------------------------------------------------------------------------
+// Edge set-up: segment start and per-sample / per-segment steps of every dof
+// into warp scratch (call-site formulas, see the rule constants).  Returns
+// the segment count; too_many marks counts beyond kMaxSegments.
+__device__ __forceinline__ int edge_setup(const EdgeParams &P, WarpScratch &W, long long e, int dof, int g, int lane,
+                                          bool &too_many) {
+    const float *qa = P.q0 + e * dof, *qb = P.q1 + e * dof;
+    float diff0 = 0.f, diff1 = 0.f;
+    if (lane < dof) diff0 = __fsub_rn(qb[lane], qa[lane]);
+    if (lane + 32 < dof) diff1 = __fsub_rn(qb[lane + 32], qa[lane + 32]);
+    int nseg = 1;
+    too_many = false;
+    if (P.rule != kRulePlain) {
+        // |q1 - q0| with the reference's sequential FMA chain (utils.cuh:123-133)
+        float acc = 0.0f;
+        for (int d = 0; d < dof; d++) {
+            const float v = __shfl_sync(kFull, d < 32 ? diff0 : diff1, d & 31);
+            acc = __fmaf_rn(v, v, acc);
+        }
+        const float dist = __fsqrt_rn(acc);
+        float n;
+        if (P.rule == kRuleConnect) n = truncf(__fdiv_rn(dist, P.range)) + 1.0f;
+        else if (P.rule == kRuleBspline) n = ceilf(__fdiv_rn(dist, P.range));
+        else n = ceilf(__fdiv_rn(__fsub_rn(dist, 0.001f), P.range));
+        if (n > (float)kMaxSegments) too_many = true;
+        else nseg = (int)n; // may be <= 0: no segment is checked (the reference's loop runs 0 times)
+    }
+    for (int d = lane; d < dof; d += 32) {
+        const float df = d < 32 ? diff0 : diff1;
+        W.base[d] = qa[d];
+        if (P.rule == kRulePlain) {
+            W.stepg[d] = __fdiv_rn(df, (float)g);
+            W.delta[d] = 0.0f;
+        } else {
+            const float step = __fdiv_rn(df, (float)nseg);
+            W.delta[d] = step;
+            W.stepg[d] = __fdiv_rn(step, (float)g);
+        }
+    }
+    __syncwarp();
+    return nseg;
+}
+
+// Broad phase of one segment for this lane's samples plus the decision: which
+// samples get the detailed check (the reference's thread split, or every
+// flagged sample in EXACT mode).  Returns false when no sample is flagged.
+template <int A, int SPL>
+__device__ __forceinline__ bool broad_decide(const EdgeParams &P, WarpScratch &W, const float4 *S,
+                                             const SceneLayout &L, int seg, int g, int lane, uint64_t (&envw)[SPL],
+                                             uint64_t (&selfw)[SPL], uint64_t &cand_env, uint64_t &cand_self,
+                                             double &tally) {
+    MRPOP_PHASE_START();
+    int envc[SPL], selfc[SPL];
+    int tot_env = 0, tot_self = 0;
+#pragma unroll
+    for (int s = 0; s < SPL; s++) {
+        const int k = lane + 1 + 32 * s;
+        broad_sample<A>(P, W, S, L, seg, k <= g ? k : g, envw[s], selfw[s]);
+        if (k > g) envw[s] = selfw[s] = 0;
+        envc[s] = flag_count(envw[s]);
+        selfc[s] = flag_count(selfw[s]);
+        tot_env += envc[s];
+        tot_self += selfc[s];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        tot_env += __shfl_xor_sync(kFull, tot_env, o);
+        tot_self += __shfl_xor_sync(kFull, tot_self, o);
+    }
+    if (P.flops) tally += P.fbp * g;
+    cand_env = cand_self = 0;
+    if (tot_env == 0 && tot_self == 0) return false;
+    MRPOP_PHASE(P, 7);
+    if (P.flags & kExactBit) {
+#pragma unroll
+        for (int s = 0; s < SPL; s++) {
+            const uint64_t be = __ballot_sync(kFull, envc[s] > 0);
+            const uint64_t bs = __ballot_sync(kFull, selfc[s] > 0);
+            cand_env |= be << (32 * s);
+            cand_self |= bs << (32 * s);
+        }
+    } else {
+        int de[SPL], ds[SPL], sum_e = 0, sum_s = 0;
+#pragma unroll
+        for (int s = 0; s < SPL; s++) {
+            const int k = lane + 1 + 32 * s;
+            de[s] = k <= g ? ref_share(envc[s], tot_env, g) : 0;
+            ds[s] = k <= g ? ref_share(selfc[s], tot_self, g) : 0;
+            sum_e += de[s];
+            sum_s += ds[s];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sum_e += __shfl_xor_sync(kFull, sum_e, o);
+            sum_s += __shfl_xor_sync(kFull, sum_s, o);
+        }
+#pragma unroll
+        for (int s = 0; s < SPL; s++) {
+            const int k = lane + 1 + 32 * s;
+            if (k == g) { // the remainder goes to the last sample
+                de[s] += 4 * g - sum_e;
+                ds[s] += 4 * g - sum_s;
+            }
+            const uint64_t be = __ballot_sync(kFull, tot_env > 0 && de[s] > 0);
+            const uint64_t bs = __ballot_sync(kFull, tot_self > 0 && ds[s] > 0);
+            cand_env |= be << (32 * s);
+            cand_self |= bs << (32 * s);
+        }
+    }
+    if (P.flops) {
+        double f = 0.0;
+#pragma unroll
+        for (int s = 0; s < SPL; s++) {
+            const int bit = lane + 32 * s;
+            const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
+            if (dE || dS) f += narrow_flops(P, P.single ? 1 : A, envw[s], selfw[s], dE, dS);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) f += __shfl_xor_sync(kFull, f, o);
+        tally += f;
+    }
+    MRPOP_PHASE(P, 4);
+    return true;
+}
+
+// Detailed phase of one segment: every candidate sample in parallel, one lane
+// each.  Returns the 0-based index of the first colliding sample, or 64.
+template <int A, int SPL>
+__device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &W, const float4 *S,
+                                              const SceneLayout &L, const float4 *det_tab, int seg, int lane,
+                                              const uint64_t (&envw)[SPL], const uint64_t (&selfw)[SPL],
+                                              uint64_t cand_env, uint64_t cand_self, float max_group_r) {
+    MRPOP_PHASE_START();
+    uint64_t hits = 0;
+#pragma unroll
+    for (int s = 0; s < SPL; s++) {
+        const int bit = lane + 32 * s;
+        const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
+        bool h = false;
+        uint32_t pm = 0;
+        if (dE || dS) {
+            h = narrow_lane<A>(P, W, S, L, det_tab, seg, bit + 1, envw[s], selfw[s], dE, dS, max_group_r);
+            if (!h && A > 1) pm = cross_pairs<A>(W, selfw[s], dS);
+        }
+        MRPOP_PHASE(P, 5);
+        if (A > 1 && __any_sync(kFull, pm != 0u)) h |= cross_lane<A>(P, W, seg, bit + 1, selfw[s], pm);
+        MRPOP_PHASE(P, 6);
+        hits |= (uint64_t)__ballot_sync(kFull, h) << (32 * s);
+        if (hits) break; // later slots hold only later samples
+    }
+    return hits ? __ffsll((long long)hits) - 1 : 64;
+}
+
+// Common kernel prologue: scene staged in shared memory, warp scratch.
+#define MRPOP_KERNEL_PROLOGUE()                                                                        \
+    extern __shared__ __align__(128) unsigned char smem_raw[];                                         \
+    __shared__ __align__(8) uint64_t bar;                                                              \
+    __shared__ float4 det_tab[kNumDet];                                                                \
+    const SceneLayout L = scene_layout(P.sc);                                                          \
+    float4 *S = reinterpret_cast<float4 *>(smem_raw);                                                  \
+    WarpScratch *Wall = reinterpret_cast<WarpScratch *>(smem_raw + (size_t)L.total * sizeof(float4));  \
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;                                        \
+    WarpScratch &W = Wall[warp];                                                                       \
+    for (int i = threadIdx.x; i < kNumDet; i += blockDim.x) det_tab[i] = c_det[i];                     \
+    const bool staged = stage_scene(S, P.scene, (uint32_t)(L.total * sizeof(float4)), &bar, P.status); \
+    const int g = P.g;                                                                                 \
+    const int dof = 7 * (P.single ? 1 : A);                                                            \
+    float max_group_r = 0.f;                                                                           \
+    for (int j = 0; j < kNumJoints; j++) max_group_r = fmaxf(max_group_r, P.group_r[j]);               \
+    const long long nwarps = (long long)gridDim.x * kWarpsPerBlock;                                    \
+    (void)max_group_r;                                                                                 \
+    (void)det_tab;
+
+// ---------------------------------------------------------------------------
+// fused kernel: every rule, segments in order with early exit
 // ---------------------------------------------------------------------------
 template <int A, int SPL>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS) validate_kernel(const __grid_constant__ EdgeParams P) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bar;
-    __shared__ float4 det_tab[kNumDet];
-
-    const SceneLayout L = scene_layout(P.sc);
-    float4 *S = reinterpret_cast<float4 *>(smem_raw);
-    WarpScratch *Wall = reinterpret_cast<WarpScratch *>(smem_raw + (size_t)L.total * sizeof(float4));
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    WarpScratch &W = Wall[warp];
-
-    for (int i = threadIdx.x; i < kNumDet; i += blockDim.x) det_tab[i] = c_det[i];
-    const bool staged = stage_scene(S, P.scene, (uint32_t)(L.total * sizeof(float4)), &bar, P.status);
-
-    const int g = P.g;
-    const int dof = 7 * (P.single ? 1 : A);
-    float max_group_r = 0.f;
-#pragma unroll
-    for (int j = 0; j < kNumJoints; j++) max_group_r = fmaxf(max_group_r, P.group_r[j]);
-    const long long nwarps = (long long)gridDim.x * kWarpsPerBlock;
-
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
+    validate_kernel(const __grid_constant__ EdgeParams P) {
+    MRPOP_KERNEL_PROLOGUE()
     for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps) {
         if (!staged) {
             if (lane == 0) {
@@ -880,149 +1040,20 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS) validat
             }
             continue;
         }
-        // edge set-up: per-dof segment start and steps in warp scratch
-        const float *qa = P.q0 + e * dof, *qb = P.q1 + e * dof;
-        float diff0 = 0.f, diff1 = 0.f;
-        if (lane < dof) diff0 = __fsub_rn(qb[lane], qa[lane]);
-        if (lane + 32 < dof) diff1 = __fsub_rn(qb[lane + 32], qa[lane + 32]);
-        int nseg = 1;
-        bool too_many = false;
-        if (P.rule != kRulePlain) {
-            // |q1 - q0| with the reference's sequential FMA chain (utils.cuh:123-133)
-            float acc = 0.0f;
-            for (int d = 0; d < dof; d++) {
-                const float v = __shfl_sync(kFull, d < 32 ? diff0 : diff1, d & 31);
-                acc = __fmaf_rn(v, v, acc);
-            }
-            const float dist = __fsqrt_rn(acc);
-            float n;
-            if (P.rule == kRuleConnect) n = truncf(__fdiv_rn(dist, P.range)) + 1.0f;
-            else if (P.rule == kRuleBspline) n = ceilf(__fdiv_rn(dist, P.range));
-            else n = ceilf(__fdiv_rn(__fsub_rn(dist, 0.001f), P.range));
-            if (n > (float)kMaxSegments) too_many = true;
-            else nseg = (int)n; // may be <= 0: no segment is checked (the reference's loop runs 0 times)
-        }
-        for (int d = lane; d < dof; d += 32) {
-            const float df = d < 32 ? diff0 : diff1;
-            W.base[d] = qa[d];
-            if (P.rule == kRulePlain) {
-                W.stepg[d] = __fdiv_rn(df, (float)g);
-                W.delta[d] = 0.0f;
-            } else {
-                const float step = __fdiv_rn(df, (float)nseg);
-                W.delta[d] = step;
-                W.stepg[d] = __fdiv_rn(step, (float)g);
-            }
-        }
-        __syncwarp();
-
+        bool too_many;
+        const int nseg = edge_setup(P, W, e, dof, g, lane, too_many);
         int first = 0;
         double tally = 0.0;
         const int nseg_run = too_many ? 0 : nseg;
         for (int seg = 0; seg < nseg_run && first == 0; seg++) {
-            MRPOP_PHASE_START();
-            // ---- broad phase: this lane's samples
-            uint64_t envw[SPL], selfw[SPL];
-            int envc[SPL], selfc[SPL];
-            int tot_env = 0, tot_self = 0;
-#pragma unroll
-            for (int s = 0; s < SPL; s++) {
-                const int k = lane + 1 + 32 * s;
-                broad_sample<A>(P, W, S, L, seg, k <= g ? k : g, envw[s], selfw[s]);
-                if (k > g) envw[s] = selfw[s] = 0;
-                envc[s] = flag_count(envw[s]);
-                selfc[s] = flag_count(selfw[s]);
-                tot_env += envc[s];
-                tot_self += selfc[s];
+            uint64_t envw[SPL], selfw[SPL], cand_env, cand_self;
+            if (broad_decide<A, SPL>(P, W, S, L, seg, g, lane, envw, selfw, cand_env, cand_self, tally)) {
+                const int fb = narrow_segment<A, SPL>(P, W, S, L, det_tab, seg, lane, envw, selfw, cand_env,
+                                                      cand_self, max_group_r);
+                if (fb < 64) first = seg * g + fb + 1;
             }
-            __syncwarp();
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                tot_env += __shfl_xor_sync(kFull, tot_env, o);
-                tot_self += __shfl_xor_sync(kFull, tot_self, o);
-            }
-            if (P.flops) tally += P.fbp * g;
-            if (tot_env == 0 && tot_self == 0) {
-                if (P.rule == kRuleConnect) {
-                    for (int d = lane; d < dof; d += 32) W.base[d] = __fadd_rn(W.base[d], W.delta[d]);
-                    __syncwarp();
-                }
-                continue;
-            }
-            MRPOP_PHASE(P, 7);
-            // ---- decision: which samples get the detailed check
-            uint64_t cand_env = 0, cand_self = 0;
-            const bool exact = P.flags & kExactBit;
-            if (exact) {
-#pragma unroll
-                for (int s = 0; s < SPL; s++) {
-                    const uint64_t be = __ballot_sync(kFull, envc[s] > 0);
-                    const uint64_t bs = __ballot_sync(kFull, selfc[s] > 0);
-                    cand_env |= be << (32 * s);
-                    cand_self |= bs << (32 * s);
-                }
-            } else {
-                int de[SPL], ds[SPL], sum_e = 0, sum_s = 0;
-#pragma unroll
-                for (int s = 0; s < SPL; s++) {
-                    const int k = lane + 1 + 32 * s;
-                    de[s] = k <= g ? ref_share(envc[s], tot_env, g) : 0;
-                    ds[s] = k <= g ? ref_share(selfc[s], tot_self, g) : 0;
-                    sum_e += de[s];
-                    sum_s += ds[s];
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    sum_e += __shfl_xor_sync(kFull, sum_e, o);
-                    sum_s += __shfl_xor_sync(kFull, sum_s, o);
-                }
-#pragma unroll
-                for (int s = 0; s < SPL; s++) {
-                    const int k = lane + 1 + 32 * s;
-                    if (k == g) { // the remainder goes to the last sample
-                        de[s] += 4 * g - sum_e;
-                        ds[s] += 4 * g - sum_s;
-                    }
-                    const uint64_t be = __ballot_sync(kFull, tot_env > 0 && de[s] > 0);
-                    const uint64_t bs = __ballot_sync(kFull, tot_self > 0 && ds[s] > 0);
-                    cand_env |= be << (32 * s);
-                    cand_self |= bs << (32 * s);
-                }
-            }
-            if (P.flops) {
-                double f = 0.0;
-#pragma unroll
-                for (int s = 0; s < SPL; s++) {
-                    const int bit = lane + 32 * s;
-                    const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
-                    if (dE || dS) f += narrow_flops(P, P.single ? 1 : A, envw[s], selfw[s], dE, dS);
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) f += __shfl_xor_sync(kFull, f, o);
-                tally += f;
-            }
-            // ---- narrow phase: every candidate sample in parallel, one lane
-            // each; the first colliding sample is the lowest set bit
-            uint64_t hits = 0;
-#pragma unroll
-            for (int s = 0; s < SPL; s++) {
-                const int bit = lane + 32 * s;
-                const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
-                bool h = false;
-                uint32_t pm = 0;
-                if (dE || dS) {
-                    h = narrow_lane<A>(P, W, S, L, det_tab, seg, bit + 1, envw[s], selfw[s], dE, dS, max_group_r);
-                    if (!h && A > 1) pm = cross_pairs<A>(W, selfw[s], dS);
-                }
-                MRPOP_PHASE(P, 5);
-                if (A > 1 && __any_sync(kFull, pm != 0u)) h |= cross_lane<A>(P, W, seg, bit + 1, selfw[s], pm);
-                MRPOP_PHASE(P, 6);
-                hits |= (uint64_t)__ballot_sync(kFull, h) << (32 * s);
-                if (hits) break; // later slots hold only later samples
-            }
-            const int first_bit = hits ? __ffsll((long long)hits) - 1 : 64;
-            if (first_bit < 64) first = seg * g + first_bit + 1;
             if (P.rule == kRuleConnect) {
+                __syncwarp();
                 for (int d = lane; d < dof; d += 32) W.base[d] = __fadd_rn(W.base[d], W.delta[d]);
                 __syncwarp();
             }
@@ -1032,6 +1063,85 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS) validat
             P.first_hit[e] = too_many ? -2 : (first ? first : -1);
             if (P.n_seg_out) P.n_seg_out[e] = nseg;
             if (P.flops) P.flops[e] = tally;
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// split pipeline for single-segment edges: the broad kernel writes every
+// sample's flag words and each edge's candidate masks to HBM (P.sflags,
+// P.smasks); the narrow kernel runs the detailed phase of edges with
+// candidates.  Each kernel's code fits the instruction cache on its own.
+// ---------------------------------------------------------------------------
+template <int A, int SPL>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
+    broad_kernel(const __grid_constant__ EdgeParams P) {
+    MRPOP_KERNEL_PROLOGUE()
+    for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps) {
+        if (!staged) {
+            if (lane == 0) {
+                P.valid[e] = 0;
+                P.first_hit[e] = -2;
+                P.smasks[2 * e] = P.smasks[2 * e + 1] = 0;
+            }
+            continue;
+        }
+        bool too_many;
+        edge_setup(P, W, e, dof, g, lane, too_many);
+        uint64_t envw[SPL], selfw[SPL], cand_env, cand_self;
+        double tally = 0.0;
+        const bool any = broad_decide<A, SPL>(P, W, S, L, 0, g, lane, envw, selfw, cand_env, cand_self, tally);
+        if (any) {
+#pragma unroll
+            for (int s = 0; s < SPL; s++) {
+                const long long o = (e * (32 * SPL) + lane + 32 * s) * 2;
+                P.sflags[o] = envw[s];
+                P.sflags[o + 1] = selfw[s];
+            }
+        }
+        if (lane == 0) {
+            P.smasks[2 * e] = cand_env;
+            P.smasks[2 * e + 1] = cand_self;
+            if (!any) {
+                P.valid[e] = 1;
+                P.first_hit[e] = -1;
+            }
+            if (P.n_seg_out) P.n_seg_out[e] = 1;
+            if (P.flops) P.flops[e] = tally;
+        }
+        __syncwarp();
+    }
+}
+
+template <int A, int SPL>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
+    narrow_kernel(const __grid_constant__ EdgeParams P) {
+    MRPOP_KERNEL_PROLOGUE()
+    for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps) {
+        const uint64_t cand_env = P.smasks[2 * e], cand_self = P.smasks[2 * e + 1];
+        if (!(cand_env | cand_self)) continue; // verdict written by the broad kernel
+        if (!staged) {
+            if (lane == 0) {
+                P.valid[e] = 0;
+                P.first_hit[e] = -2;
+            }
+            continue;
+        }
+        bool too_many;
+        edge_setup(P, W, e, dof, g, lane, too_many);
+        uint64_t envw[SPL], selfw[SPL];
+#pragma unroll
+        for (int s = 0; s < SPL; s++) {
+            const long long o = (e * (32 * SPL) + lane + 32 * s) * 2;
+            envw[s] = P.sflags[o];
+            selfw[s] = P.sflags[o + 1];
+        }
+        const int fb =
+            narrow_segment<A, SPL>(P, W, S, L, det_tab, 0, lane, envw, selfw, cand_env, cand_self, max_group_r);
+        if (lane == 0) {
+            P.valid[e] = fb < 64 ? 0 : 1;
+            P.first_hit[e] = fb < 64 ? fb + 1 : -1;
         }
         __syncwarp();
     }

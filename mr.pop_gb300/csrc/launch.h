@@ -7,14 +7,14 @@
 
 namespace mrpop {
 
-// Launch the validator for `arms` arms (1..5).  smem_bytes: dynamic shared
-// memory (staged scene + per-warp scratch).  Returns the launch error.
-cudaError_t launch_validate(int arms, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream);
+// Which kernel to launch.
+enum KernelKind { kFused = 0, kBroad = 1, kNarrow = 2 };
+
+// Launch a validator kernel for `arms` arms (1..5).  smem_bytes: dynamic
+// shared memory (staged scene + per-warp scratch).  Returns the launch error.
+cudaError_t launch_validate(int arms, KernelKind kind, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream);
 
 template <int A>
-cudaError_t launch_validate_arms(const EdgeParams &p, size_t smem_bytes, cudaStream_t stream);
-
-// Blocks of `validate_kernel<A, SPL>` that fit on one SM with smem_bytes.
-int validate_occupancy(int arms, int spl, size_t smem_bytes);
+cudaError_t launch_validate_arms(KernelKind kind, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream);
 
 }  // namespace mrpop
