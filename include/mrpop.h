@@ -143,6 +143,30 @@ mrpop_status mrpop_validate_segments(const mrpop_scene *scene, const mrpop_robot
                                      int32_t *n_seg_out, void *stream);
 
 /*
+ * Same verdicts as mrpop_validate_edges (single-segment edges), for callers that
+ * must not allocate device memory while they run -- e.g. a serving process that
+ * reserves its whole device-memory budget at start-up and admits work against
+ * it, or a planner loop that may not enter the allocator.  No counterpart in the
+ * reference (its planner keeps all scratch in fixed __device__ arrays).
+ *   - Calls no allocation routine.  Its scratch is one fixed array in the
+ *     library's device memory, about 16.3 MiB per device
+ *     (MRPOP_NOALLOC_MAX_EDGES edges at granularity 64), held by every GPU that
+ *     loads the library until the process exits.
+ *   - n_edges above MRPOP_NOALLOC_MAX_EDGES is rejected (MRPOP_ERR_INVALID_ARGUMENT).
+ *   - The first call on a device looks up the array's device address (a one-time
+ *     set-up per device, done with that device current); make that first call
+ *     before any stream capture.
+ *   - Every call shares the array: calls that overlap on the GPU (different
+ *     streams, other host threads) race on it and must be ordered by the caller.
+ *     The array keeps the last call's contents; no call depends on them.
+ */
+#define MRPOP_NOALLOC_MAX_EDGES 16384
+mrpop_status mrpop_validate_edges_noalloc(const mrpop_scene *scene, const mrpop_robotset *robots,
+                                          const float *q0, const float *q1, int64_t n_edges,
+                                          int granularity, uint32_t flags, int arm, uint8_t *valid,
+                                          int32_t *first_hit, void *stream);
+
+/*
  * Host-buffer form for callers without device memory (the reference's host
  * API, dRRT::solve in Planners.hh:57-64, hands host arrays across): copies
  * q0/q1 from host memory, validates, copies valid/first_hit back and waits.

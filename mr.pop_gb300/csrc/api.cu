@@ -264,10 +264,17 @@ mrpop_status mrpop_robotset_destroy(mrpop_robotset *robots) {
 
 namespace {
 
+}  // namespace
+
+namespace mrpop {
+
+// ext_scratch: caller-provided device scratch for the single-segment pipeline
+// (at least n_edges * (32 * samples-per-lane + 1) * 16 bytes); nullptr = the
+// library's stream-ordered pool.
 mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
                            const float *q1, int64_t n_edges, int g, int rule, float range, uint32_t flags,
                            int arm, uint8_t *valid, int32_t *first_hit, int32_t *n_seg_out, double *flops,
-                           cudaStream_t stream) {
+                           cudaStream_t stream, void *ext_scratch) {
     if (!scene || !robots) return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: null scene or robots");
     if (n_edges < 0) return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: n_edges < 0");
     if (n_edges == 0) return MRPOP_OK;
@@ -354,16 +361,20 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
         const int spl = g > 32 ? 2 : 1;
         const size_t flag_bytes = (size_t)n_edges * 32 * spl * 2 * sizeof(uint64_t);
         const size_t mask_bytes = (size_t)n_edges * 2 * sizeof(uint64_t);
-        void *scratch = nullptr;
-        cudaMemPool_t pool;
-        err = scratch_pool(&pool);
-        if (err == cudaSuccess) err = cudaMallocFromPoolAsync(&scratch, flag_bytes + mask_bytes, pool, stream);
+        void *scratch = ext_scratch;
+        if (!scratch) {
+            cudaMemPool_t pool;
+            err = scratch_pool(&pool);
+            if (err == cudaSuccess) err = cudaMallocFromPoolAsync(&scratch, flag_bytes + mask_bytes, pool, stream);
+        } else {
+            err = cudaSuccess;
+        }
         if (err == cudaSuccess) {
             p.sflags = (uint64_t *)scratch;
             p.smasks = (uint64_t *)((char *)scratch + flag_bytes);
             err = mrpop::launch_validate(A, mrpop::kBroad, p, smem, stream);
             if (err == cudaSuccess) err = mrpop::launch_validate(A, mrpop::kNarrow, p, smem, stream);
-            cudaFreeAsync(scratch, stream);
+            if (!ext_scratch) cudaFreeAsync(scratch, stream);
         }
     } else {
         err = mrpop::launch_validate(A, mrpop::kFused, p, smem, stream);
@@ -373,6 +384,12 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
     if (err != cudaSuccess) return cuda_fail(err, "validate: launch");
     return MRPOP_OK;
 }
+
+mrpop_status fail_status(mrpop_status st, const char *msg) { return fail(st, msg); }
+
+}  // namespace mrpop
+
+namespace {
 
 struct Base12 {
     float m[12];
@@ -444,24 +461,24 @@ void mrpop_dev_phase_counters(unsigned long long *dev_counters) { g_phase_counte
 mrpop_status mrpop_validate_edges(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
                                   const float *q1, int64_t n_edges, int granularity, uint32_t flags, int arm,
                                   uint8_t *valid, int32_t *first_hit, void *stream) {
-    return run_validator(scene, robots, q0, q1, n_edges, granularity, MRPOP_RULE_PLAIN, 0.0f, flags, arm, valid,
-                         first_hit, nullptr, nullptr, (cudaStream_t)stream);
+    return mrpop::run_validator(scene, robots, q0, q1, n_edges, granularity, MRPOP_RULE_PLAIN, 0.0f, flags, arm,
+                                valid, first_hit, nullptr, nullptr, (cudaStream_t)stream, nullptr);
 }
 
 mrpop_status mrpop_validate_segments(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
                                      const float *q1, int64_t n_edges, int granularity, int rule, float range,
                                      uint32_t flags, int arm, uint8_t *valid, int32_t *first_hit,
                                      int32_t *n_seg_out, void *stream) {
-    return run_validator(scene, robots, q0, q1, n_edges, granularity, rule, range, flags, arm, valid, first_hit,
-                         n_seg_out, nullptr, (cudaStream_t)stream);
+    return mrpop::run_validator(scene, robots, q0, q1, n_edges, granularity, rule, range, flags, arm, valid,
+                                first_hit, n_seg_out, nullptr, (cudaStream_t)stream, nullptr);
 }
 
 mrpop_status mrpop_count_flops(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
                                const float *q1, int64_t n_edges, int granularity, int rule, float range,
                                uint32_t flags, int arm, double *flops, void *stream) {
     if (!flops) return fail(MRPOP_ERR_INVALID_ARGUMENT, "count_flops: null output");
-    return run_validator(scene, robots, q0, q1, n_edges, granularity, rule, range, flags, arm, nullptr, nullptr,
-                         nullptr, flops, (cudaStream_t)stream);
+    return mrpop::run_validator(scene, robots, q0, q1, n_edges, granularity, rule, range, flags, arm, nullptr,
+                                nullptr, nullptr, flops, (cudaStream_t)stream, nullptr);
 }
 
 mrpop_status mrpop_fk_spheres(const mrpop_robotset *robots, int arm, const float *q, int64_t n, int detailed,
@@ -545,8 +562,8 @@ mrpop_status mrpop_validate_edges_host(mrpop_workspace *ws, const mrpop_scene *s
     cudaStream_t st = ws->stream;
     MRPOP_CUDA(cudaMemcpyAsync(ws->d_q0, q0, ncfg * sizeof(float), cudaMemcpyHostToDevice, st), "H2D q0");
     MRPOP_CUDA(cudaMemcpyAsync(ws->d_q1, q1, ncfg * sizeof(float), cudaMemcpyHostToDevice, st), "H2D q1");
-    mrpop_status s = run_validator(scene, robots, ws->d_q0, ws->d_q1, n_edges, granularity, rule, range, flags, arm,
-                                   ws->d_valid, ws->d_first, nullptr, nullptr, st);
+    mrpop_status s = mrpop::run_validator(scene, robots, ws->d_q0, ws->d_q1, n_edges, granularity, rule, range,
+                                          flags, arm, ws->d_valid, ws->d_first, nullptr, nullptr, st, nullptr);
     if (s != MRPOP_OK) return s;
     MRPOP_CUDA(cudaMemcpyAsync(valid, ws->d_valid, (size_t)n_edges, cudaMemcpyDeviceToHost, st), "D2H valid");
     MRPOP_CUDA(cudaMemcpyAsync(first_hit, ws->d_first, (size_t)n_edges * 4, cudaMemcpyDeviceToHost, st),

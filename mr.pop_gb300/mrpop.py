@@ -29,7 +29,9 @@ EXPORTED = [
     "mrpop_robotset_destroy", "mrpop_validate_edges", "mrpop_validate_segments", "mrpop_workspace_create",
     "mrpop_workspace_destroy", "mrpop_validate_edges_host", "mrpop_fk_spheres", "mrpop_count_flops",
     "mrpop_debug_trig", "mrpop_fp32_peak_probe", "mrpop_last_error", "mrpop_version",
+    "mrpop_validate_edges_noalloc",
 ]
+NOALLOC_MAX_EDGES = 16384
 
 
 class MrpopError(RuntimeError):
@@ -77,6 +79,7 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
         "mrpop_count_flops": [vp, vp, vp, vp, i64, i32, i32, f32, u32, i32, vp, vp],
         "mrpop_debug_trig": [vp, i64, vp, vp, vp],
         "mrpop_fp32_peak_probe": [i32, i32, vp, C.POINTER(C.c_double), vp],
+        "mrpop_validate_edges_noalloc": [vp, vp, vp, vp, i64, i32, u32, i32, vp, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
