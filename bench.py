@@ -147,16 +147,24 @@ def workload_config(wl, extra):
 
 
 def cpu_baseline(orc, wl, n_edges: int):
-    """The CPU restatement on all host threads over the first n_edges edges."""
+    """The CPU restatement on all host threads over the first n_edges edges,
+    plus a one-thread figure over an eighth of them (about 15-40 s of CPU
+    work in all on the workloads here)."""
     threads = orc.max_threads()
     sub0, sub1 = wl.q0[:n_edges], wl.q1[:n_edges]
     orc.validate(wl.scene, wl.bases, sub0[:64], sub1[:64], wl.granularity, wl.flags, wl.arm, threads=threads)
     t = time.perf_counter()
     orc.validate(wl.scene, wl.bases, sub0, sub1, wl.granularity, wl.flags, wl.arm, threads=threads)
     dt = time.perf_counter() - t
+    n1 = max(1, n_edges // 8)
+    t = time.perf_counter()
+    orc.validate(wl.scene, wl.bases, sub0[:n1], sub1[:n1], wl.granularity, wl.flags, wl.arm, threads=1)
+    dt1 = time.perf_counter() - t
     return {"value": n_edges * wl.granularity / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "value_1core": n1 * wl.granularity / dt1,
             "sample": f"first {n_edges} of the {len(wl.q0)} edges, oracle/edge_oracle.c (FP32 restatement of the "
-                      f"reference check), OpenMP over edges, {dt:.2f} s wall"}
+                      f"reference check), OpenMP over edges, {dt:.2f} s wall; value_1core: first {n1} edges on "
+                      f"one thread, {dt1:.2f} s"}
 
 
 def fp32_peak(pkg, torch) -> float:
@@ -176,16 +184,48 @@ def fp32_peak(pkg, torch) -> float:
     return best
 
 
-def committed_traffic(workload: str):
-    """DRAM bytes per launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / f"validate_{workload}.json"
+KERNEL_NAMES = {"fused": "validate_kernel", "broad": "broad_kernel", "narrow": "narrow_kernel"}
+
+
+def committed_profile(kernel: str, workload: str) -> dict:
+    """Per-launch figures of one kernel from the committed ncu summary
+    (profiles/<kernel>_<workload>.json): DRAM bytes and executed FP32 flops."""
+    p = ROOT / "profiles" / f"{kernel}_{workload}.json"
     if p.exists():
         try:
-            d = json.loads(p.read_text())
-            return d.get("dram_bytes_per_launch")
-        except Exception:
-            return None
-    return None
+            return json.loads(p.read_text())
+        except ValueError:
+            return {}
+    return {}
+
+
+def roofline(kt: dict, flops: dict, peak: float, workload: str, arms: int, spl: int) -> dict:
+    """Roofline of the kernel with the largest share of device time.
+    kt: {kind: (launches, total ms)} from the library's event timing;
+    flops: algorithmic flops per launch of each kind."""
+    ran = {k: v for k, v in kt.items() if v[0] > 0}
+    total_ms = sum(v[1] for v in ran.values())
+    dom = max(ran, key=lambda k: ran[k][1])
+    launches, ms = ran[dom]
+    launch_s = ms / launches / 1e3
+    achieved = flops[dom] / launch_s / 1e12
+    prof = committed_profile(KERNEL_NAMES[dom], workload)
+    out = {"bound": "fp32", "kernel": f"{KERNEL_NAMES[dom]}<{arms},{spl}>", "achieved": achieved, "peak": peak,
+           "unit": "TFLOP/s", "frac": achieved / peak, "traffic": prof.get("dram_bytes_per_launch"),
+           "launch_ms": launch_s * 1e3, "share": ms / total_ms,
+           "peak_source": "measured: FP32 FMA loop (mrpop_fp32_peak_probe) timed in this run; "
+                          "MEASURED_PEAKS.json has no FP32 figure",
+           "achieved_basis": f"{flops[dom]:.4g} algorithmic flops per launch (FMA=2, unculled per-test costs) / "
+                             f"CUDA-event launch time on the launching stream"}
+    if prof.get("executed_fp32_flops_per_launch"):
+        ex = prof["executed_fp32_flops_per_launch"] / launch_s / 1e12
+        out["executed"] = {"achieved": ex, "frac": ex / peak,
+                           "basis": "FP32 flops the kernel executed (ncu: 2*ffma + fadd + fmul thread "
+                                    "instructions) / live launch time; culling skips algorithmic work"}
+    out["kernels"] = {KERNEL_NAMES[k]: {"launches": v[0], "avg_ms": v[1] / v[0], "share": v[1] / total_ms,
+                                        "algorithmic_tflops": flops[k] / (v[1] / v[0] / 1e3) / 1e12}
+                      for k, v in ran.items()}
+    return out
 
 
 def run_mine(args, world, rank, local):
@@ -212,6 +252,8 @@ def run_mine(args, world, rank, local):
         pkg.validate(scene, robots, q0, q1, wl.granularity, wl.flags, wl.arm, valid=valid, first_hit=first)
 
     flops_launch = float(pkg.count_flops(scene, robots, q0, q1, wl.granularity, wl.flags, wl.arm).sum().item())
+    broad_launch = pkg.broad_flops_per_sample(scene, robots, wl.flags, wl.arm) * samples
+    flops = {"fused": flops_launch, "broad": broad_launch, "narrow": flops_launch - broad_launch}
     for _ in range(args.warmup):
         flush.zero_()
         step()
@@ -219,6 +261,8 @@ def run_mine(args, world, rank, local):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     clocks = ClockSampler(local)
     clocks.start()
+    pkg.kernel_times()
+    pkg.kernel_timing(True)
     barrier(world)
     torch.cuda.synchronize()
     for s, e in ev:
@@ -228,27 +272,24 @@ def run_mine(args, world, rank, local):
         e.record(stream)
     torch.cuda.synchronize()
     barrier(world)
+    pkg.kernel_timing(False)
     clk = clocks.stop()
+    kt = pkg.kernel_times()
     step_ms = [s.elapsed_time(e) for s, e in ev]
     t_total = max_over_ranks(sum(step_ms) / 1e3, world)
     value = world * samples * args.steps / t_total
-    launch_s = sum(step_ms) / len(step_ms) / 1e3
     assert scene.status() == 0, "device status word set during the bench"
 
     peak = fp32_peak(pkg, torch)
-    achieved = flops_launch / launch_s / 1e12
-    traffic = committed_traffic(args.workload)
+    arms = int(len(wl.bases)) if wl.arm < 0 else 1
+    spl = 2 if wl.granularity > 32 else 1
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
         "config": workload_config(wl, {"parallelism": f"replica x{world}, independent edge batches"}),
-        "gpu_launches": args.steps,
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "peak_source": "measured: FP32 FMA loop (mrpop_fp32_peak_probe) timed in this run",
-                     "achieved_basis": f"{flops_launch:.4g} algorithmic flops per launch (FMA=2, per-test costs "
-                                       f"of the flop convention, dense narrow tally) / CUDA-event launch time"},
+        "gpu_launches": sum(v[0] for v in kt.values()),
+        "roofline": roofline(kt, flops, peak, args.workload, arms, spl),
         "clocks": clk,
     }
     if not args.no_e2e:
@@ -271,7 +312,7 @@ def run_mine(args, world, rank, local):
         assert np.array_equal(av, valid.cpu().numpy())
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as orc
-        out["cpu_baseline"] = cpu_baseline(orc, wl, min(n, 4096))
+        out["cpu_baseline"] = cpu_baseline(orc, wl, min(n, 65536))
     if rank == 0:
         print(json.dumps(out), flush=True)
 

@@ -197,6 +197,28 @@ mrpop_status mrpop_count_flops(const mrpop_scene *scene, const mrpop_robotset *r
                                int granularity, int rule, float range, uint32_t flags, int arm,
                                double *flops, void *stream);
 
+/* Algorithmic flops of the broad phase per sample (FMA = 2) for a scene,
+ * robot set, check flags and arm selection: FK of every arm, every env-tested
+ * broad sphere against every obstacle, every intra-arm and arm-vs-arm broad
+ * pair, with no culling.  Measurement utility, no counterpart in the
+ * reference (the broad phase is utils.cuh:461-475 there). */
+mrpop_status mrpop_broad_flops_per_sample(const mrpop_scene *scene, const mrpop_robotset *robots,
+                                          uint32_t flags, int arm, double *out);
+
+/* Per-kernel timing, a measurement utility with no counterpart in the
+ * reference.  While enabled, every validate call records a pair of CUDA
+ * events on its stream around each kernel it launches.  mrpop_kernel_times
+ * waits for the recorded launches, writes per kernel kind (index
+ * MRPOP_KERNEL_FUSED / _BROAD / _NARROW) the number of launches and their
+ * summed device time in ms since the previous read, and releases the events.
+ * Read on the device the launches ran on. */
+#define MRPOP_KERNEL_KINDS 3
+#define MRPOP_KERNEL_FUSED 0  /* segmented rules: broad and narrow phase in one kernel */
+#define MRPOP_KERNEL_BROAD 1  /* single-segment edges: broad phase */
+#define MRPOP_KERNEL_NARROW 2 /* single-segment edges: narrow phase */
+mrpop_status mrpop_kernel_timing(int enable);
+mrpop_status mrpop_kernel_times(int64_t *launches, double *ms);
+
 /* The __cosf/__sinf values the validator uses for inputs x (device arrays). */
 mrpop_status mrpop_debug_trig(const float *x, int64_t n, float *cos_out, float *sin_out,
                               void *stream);

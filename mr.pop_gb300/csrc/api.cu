@@ -83,6 +83,55 @@ cudaError_t scratch_pool(cudaMemPool_t *out) {
 
 size_t warp_scratch_bytes() { return sizeof(mrpop::WarpScratch) * mrpop::kWarpsPerBlock; }
 
+// Optional per-kernel timing (mrpop_kernel_timing): a pair of CUDA events is
+// recorded on the caller's stream around every validator launch while it is
+// on; mrpop_kernel_times sums and releases them.
+static_assert(mrpop::kFused == MRPOP_KERNEL_FUSED && mrpop::kBroad == MRPOP_KERNEL_BROAD &&
+                  mrpop::kNarrow == MRPOP_KERNEL_NARROW,
+              "kernel kinds of launch.h and mrpop.h differ");
+struct TimedLaunch {
+    cudaEvent_t start, stop;
+    int kind;
+};
+std::mutex g_timing_mu;
+bool g_timing_on = false;
+std::vector<TimedLaunch> g_timed;
+
+cudaError_t timed_launch(int arms, mrpop::KernelKind kind, const mrpop::EdgeParams &p, size_t smem,
+                         cudaStream_t stream) {
+    bool on;
+    {
+        std::lock_guard<std::mutex> lk(g_timing_mu);
+        on = g_timing_on;
+    }
+    if (!on) return mrpop::launch_validate(arms, kind, p, smem, stream);
+    TimedLaunch t{nullptr, nullptr, (int)kind};
+    cudaError_t e = cudaEventCreate(&t.start);
+    if (e == cudaSuccess) e = cudaEventCreate(&t.stop);
+    if (e == cudaSuccess) e = cudaEventRecord(t.start, stream);
+    if (e == cudaSuccess) e = mrpop::launch_validate(arms, kind, p, smem, stream);
+    if (e == cudaSuccess) e = cudaEventRecord(t.stop, stream);
+    if (e != cudaSuccess) {
+        if (t.start) cudaEventDestroy(t.start);
+        if (t.stop) cudaEventDestroy(t.stop);
+        return e;
+    }
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    g_timed.push_back(t);
+    return cudaSuccess;
+}
+
+// Algorithmic flops of the broad phase for one sample (FMA = 2): FK of every
+// arm (7 joint composes of 81 and 11 sphere placements of 18), the 10
+// env-tested spheres of every arm against every obstacle, the 21 intra-arm
+// pairs and the 121 pairs of every arm pair, each test at 11 flops.
+double broad_flops_per_sample(int A, double env_test_flops, uint32_t flags) {
+    double f = A * (7.0 * 81.0 + 11.0 * 18.0);
+    if (flags & MRPOP_CHECK_ENV) f += A * 10.0 * env_test_flops;
+    if (flags & MRPOP_CHECK_SELF) f += A * 21.0 * 11.0 + (A * (A - 1) / 2) * 121.0 * 11.0;
+    return f;
+}
+
 // Largest staged scene: the block's dynamic shared memory stays below this.
 constexpr size_t kMaxDynSmem = 200 * 1024;
 
@@ -340,10 +389,7 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
     const int A = arm >= 0 ? 1 : robots->n_arms;
     for (int a = 0; a < A; a++)
         for (int i = 0; i < 12; i++) p.base[a][i] = robots->base[arm >= 0 ? arm : a][i];
-    double fbp = A * (7.0 * 81.0 + 11.0 * 18.0);
-    if (flags & MRPOP_CHECK_ENV) fbp += A * 10.0 * scene->env_test_flops;
-    if (flags & MRPOP_CHECK_SELF) fbp += A * 21.0 * 11.0 + (A * (A - 1) / 2) * 121.0 * 11.0;
-    p.fbp = fbp;
+    p.fbp = broad_flops_per_sample(A, scene->env_test_flops, flags);
 
     // scratch outputs when only the tally is wanted
     uint8_t *tmp_valid = nullptr;
@@ -372,12 +418,12 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
         if (err == cudaSuccess) {
             p.sflags = (uint64_t *)scratch;
             p.smasks = (uint64_t *)((char *)scratch + flag_bytes);
-            err = mrpop::launch_validate(A, mrpop::kBroad, p, smem, stream);
-            if (err == cudaSuccess) err = mrpop::launch_validate(A, mrpop::kNarrow, p, smem, stream);
+            err = timed_launch(A, mrpop::kBroad, p, smem, stream);
+            if (err == cudaSuccess) err = timed_launch(A, mrpop::kNarrow, p, smem, stream);
             if (!ext_scratch) cudaFreeAsync(scratch, stream);
         }
     } else {
-        err = mrpop::launch_validate(A, mrpop::kFused, p, smem, stream);
+        err = timed_launch(A, mrpop::kFused, p, smem, stream);
     }
     if (tmp_valid) cudaFreeAsync(tmp_valid, stream);
     if (tmp_first) cudaFreeAsync(tmp_first, stream);
@@ -479,6 +525,49 @@ mrpop_status mrpop_count_flops(const mrpop_scene *scene, const mrpop_robotset *r
     if (!flops) return fail(MRPOP_ERR_INVALID_ARGUMENT, "count_flops: null output");
     return mrpop::run_validator(scene, robots, q0, q1, n_edges, granularity, rule, range, flags, arm, nullptr,
                                 nullptr, nullptr, flops, (cudaStream_t)stream, nullptr);
+}
+
+mrpop_status mrpop_broad_flops_per_sample(const mrpop_scene *scene, const mrpop_robotset *robots, uint32_t flags,
+                                          int arm, double *out) {
+    if (!scene || !robots || !out) return fail(MRPOP_ERR_INVALID_ARGUMENT, "broad_flops_per_sample: null argument");
+    if (arm >= robots->n_arms) return fail(MRPOP_ERR_INVALID_ARGUMENT, "broad_flops_per_sample: arm out of range");
+    *out = broad_flops_per_sample(arm >= 0 ? 1 : robots->n_arms, scene->env_test_flops, flags);
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_kernel_timing(int enable) {
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    g_timing_on = enable != 0;
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_kernel_times(int64_t *launches, double *ms) {
+    if (!launches || !ms) return fail(MRPOP_ERR_INVALID_ARGUMENT, "kernel_times: null argument");
+    std::vector<TimedLaunch> taken;
+    {
+        std::lock_guard<std::mutex> lk(g_timing_mu);
+        taken.swap(g_timed);
+    }
+    for (int k = 0; k < MRPOP_KERNEL_KINDS; k++) {
+        launches[k] = 0;
+        ms[k] = 0.0;
+    }
+    cudaError_t first_err = cudaSuccess;
+    for (const TimedLaunch &t : taken) {
+        float dt = 0.0f;
+        cudaError_t e = cudaEventSynchronize(t.stop);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&dt, t.start, t.stop);
+        if (e == cudaSuccess) {
+            launches[t.kind] += 1;
+            ms[t.kind] += dt;
+        } else if (first_err == cudaSuccess) {
+            first_err = e;
+        }
+        cudaEventDestroy(t.start);
+        cudaEventDestroy(t.stop);
+    }
+    if (first_err != cudaSuccess) return cuda_fail(first_err, "kernel_times");
+    return MRPOP_OK;
 }
 
 mrpop_status mrpop_fk_spheres(const mrpop_robotset *robots, int arm, const float *q, int64_t n, int detailed,

@@ -120,7 +120,7 @@ struct WarpScratch {
     float delta[kMaxDof];  // per-segment step (B-spline / shortcut accumulation)
     union {
         struct {
-            float4 armbs[kMaxArms][32];     // per-lane arm bounding sphere
+            float4 swept[kMaxArms][kNumApprox]; // per-arm swept bound of each approx sphere
             float cur[kNumApprox][3][32];   // per-lane approx spheres of the current arm
             float low[kNumApprox][3][32];   // per-lane approx spheres of a lower arm
         } broad;
@@ -249,92 +249,123 @@ __device__ __forceinline__ float sample_q1(const WarpScratch &W, int rule, int s
     return v;
 }
 
-// FK of arm `qarm`'s joint values (base12) for this lane's sample; writes the
-// 11 centres into the lane's column of dst and returns a conservative bounding
-// sphere of the arm's approx spheres (w = radius).
-static __device__ __noinline__ float4 fk_approx_lane(const float *base12, const WarpScratch &W, int rule, int seg,
-                                                     int qarm, int k, float (*dst)[3][32], int lane) {
+// Order-preserving map of a float onto an unsigned key, so that warp-wide
+// min/max of floats can use redux.sync on integers; key_float inverts it.
+__device__ __forceinline__ uint32_t order_key(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+__device__ __forceinline__ float warp_min(float v) { return key_float(__reduce_min_sync(kFull, order_key(v))); }
+__device__ __forceinline__ float warp_max(float v) { return key_float(__reduce_max_sync(kFull, order_key(v))); }
+
+// FK of one arm for this lane's sample; the 11 approx centres go to column
+// `lane` of dst.  With swept != nullptr it also writes, for every approx
+// sphere, a bound of that sphere over the warp's 32 samples: the centre of
+// the box around its 32 centres, radius = half the box diagonal (+0.4 %) +
+// sphere radius + cull margin.  If the sphere touches something at any of the
+// samples, its swept bound touches it too (the margin covers FP rounding).
+static __device__ __noinline__ void fk_approx_lane(const float *base12, const WarpScratch &W, int rule, int seg,
+                                                   int qarm, int k, float (*dst)[3][32], int lane, float4 *swept) {
     float q[7];
     sample_q(W, rule, seg, qarm, k, q);
     ArmSpheres s;
     fk_approx_arm(base12, q, s);
-    float lx = s.x[0], hx = s.x[0], ly = s.y[0], hy = s.y[0], lz = s.z[0], hz = s.z[0];
 #pragma unroll
     for (int i = 0; i < kNumApprox; i++) {
         dst[i][0][lane] = s.x[i];
         dst[i][1][lane] = s.y[i];
         dst[i][2][lane] = s.z[i];
-        lx = fminf(lx, s.x[i]);
-        hx = fmaxf(hx, s.x[i]);
-        ly = fminf(ly, s.y[i]);
-        hy = fmaxf(hy, s.y[i]);
-        lz = fminf(lz, s.z[i]);
-        hz = fmaxf(hz, s.z[i]);
     }
-    const float cx = 0.5f * (lx + hx), cy = 0.5f * (ly + hy), cz = 0.5f * (lz + hz);
-    float r2 = 0.f;
+    if (!swept) return;
 #pragma unroll
     for (int i = 0; i < kNumApprox; i++) {
-        const float dx = s.x[i] - cx, dy = s.y[i] - cy, dz = s.z[i] - cz;
-        r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
+        const float lx = warp_min(s.x[i]), hx = warp_max(s.x[i]);
+        const float ly = warp_min(s.y[i]), hy = warp_max(s.y[i]);
+        const float lz = warp_min(s.z[i]), hz = warp_max(s.z[i]);
+        if (lane == 0) {
+            const float dx = hx - lx, dy = hy - ly, dz = hz - lz;
+            swept[i] = make_float4(0.5f * (lx + hx), 0.5f * (ly + hy), 0.5f * (lz + hz),
+                                   0.5f * sqrtf(dx * dx + dy * dy + dz * dz) * 1.004f + c_approx[i].w + kCullMargin);
+        }
     }
-    return make_float4(cx, cy, cz, sqrtf(r2) * 1.0001f + kApproxMaxR + 1e-4f);
+    __syncwarp();
 }
 
 // ---------------------------------------------------------------------------
 // broad phase: approx spheres 1..10 of one arm (lane column `lane` of sp)
 // against the scene.  Returns a bitmask over sphere index (bit i = sphere i
-// touches some obstacle).  Each obstacle is first tested against every lane's
-// arm bound (warp vote), then against each sphere's bound (warp OR); exact
-// tests run, for the whole warp, only for spheres some lane cannot rule out.
+// of this lane's sample touches some obstacle).  The (sphere, obstacle) pairs
+// of each obstacle class are screened lane-parallel, one pair per lane, with
+// the sphere's swept bound (sw) against the obstacle: the exact test of the
+// class for cuboids with orthonormal axes, the obstacle's bounding sphere for
+// the other classes (both conservative).  Exact per-sample tests then run,
+// for the whole warp, only for the pairs that survive.
 // ---------------------------------------------------------------------------
-template <typename ExactFn>
-__device__ __forceinline__ void env_obstacle(const float (*sp)[3][32], int lane, float4 cb, float4 ob, uint32_t &m,
-                                             ExactFn exact) {
-    if (!__any_sync(kFull, near3(cb.x, cb.y, cb.z, ob, cb.w))) return;
-    uint32_t q = 0;
-#pragma unroll
-    for (int i = 1; i < kNumApprox; i++)
-        if (near3(sp[i][0][lane], sp[i][1][lane], sp[i][2][lane], ob, c_approx[i].w)) q |= 1u << i;
-    q = __reduce_or_sync(kFull, q);
-    while (q) {
-        const int i = __ffs(q) - 1;
-        q &= q - 1;
-        if (exact(sp[i][0][lane], sp[i][1][lane], sp[i][2][lane], c_approx[i].w)) m |= 1u << i;
+template <typename PreFn, typename ExactFn>
+__device__ __forceinline__ void env_pairs(int n, int lane, const float4 *sw, const float (*sp)[3][32], uint32_t &m,
+                                          PreFn pre, ExactFn exact) {
+    const int pairs = n * (kNumApprox - 1);
+#pragma unroll 1
+    for (int t0 = 0; t0 < pairs; t0 += 32) {
+        const int t = t0 + lane;
+        bool c = false;
+        if (t < pairs) {
+            const int o = t / (kNumApprox - 1);
+            c = pre(o, sw[t - (kNumApprox - 1) * o + 1]);
+        }
+        uint32_t bal = __ballot_sync(kFull, c);
+        while (bal) {
+            const int tt = t0 + __ffs(bal) - 1;
+            bal &= bal - 1;
+            const int o = tt / (kNumApprox - 1), i = tt - (kNumApprox - 1) * o + 1;
+            if (exact(o, sp[i][0][lane], sp[i][1][lane], sp[i][2][lane], c_approx[i].w)) m |= 1u << i;
+        }
     }
 }
 
 static __device__ __noinline__ uint32_t env_mask_approx(const float4 *S, const SceneLayout &L, const SceneCounts &C,
-                                                        const float (*sp)[3][32], int lane, float4 cb) {
+                                                        const float (*sp)[3][32], int lane, const float4 *sw) {
     uint32_t m = 0;
-    for (int o = 0; o < C.n_cub; o++) {
-        const float4 *r = S + L.cub + 4 * o;
-        env_obstacle(sp, lane, cb, S[L.b_cub + o], m, [&](float x, float y, float z, float rad) {
+    env_pairs(
+        C.n_cub, lane, sw, sp, m,
+        [&](int o, float4 u) {
+            const float4 *r = S + L.cub + 4 * o;
+            return S[L.b_cub + o].w > 1e17f || hit_cuboid(r[0], r[1], r[2], r[3], u.x, u.y, u.z, u.w * u.w);
+        },
+        [&](int o, float x, float y, float z, float rad) {
+            const float4 *r = S + L.cub + 4 * o;
             return hit_cuboid(r[0], r[1], r[2], r[3], x, y, z, __fmul_rn(rad, rad));
         });
-    }
-    for (int o = 0; o < C.n_zcub; o++) {
-        const float4 *r = S + L.zcub + 4 * o;
-        env_obstacle(sp, lane, cb, S[L.b_zcub + o], m, [&](float x, float y, float z, float rad) {
+    env_pairs(
+        C.n_zcub, lane, sw, sp, m,
+        [&](int o, float4 u) {
+            const float4 *r = S + L.zcub + 4 * o;
+            return S[L.b_zcub + o].w > 1e17f || hit_zcuboid(r[0], r[1], r[2], u.x, u.y, u.z, u.w * u.w);
+        },
+        [&](int o, float x, float y, float z, float rad) {
+            const float4 *r = S + L.zcub + 4 * o;
             return hit_zcuboid(r[0], r[1], r[2], x, y, z, __fmul_rn(rad, rad));
         });
-    }
-    for (int o = 0; o < C.n_cap; o++) {
-        const float4 *r = S + L.cap + 2 * o;
-        env_obstacle(sp, lane, cb, S[L.b_cap + o], m,
-                     [&](float x, float y, float z, float rad) { return hit_capsule(r[0], r[1], x, y, z, rad); });
-    }
-    for (int o = 0; o < C.n_zcap; o++) {
-        const float4 *r = S + L.zcap + 2 * o;
-        env_obstacle(sp, lane, cb, S[L.b_zcap + o], m,
-                     [&](float x, float y, float z, float rad) { return hit_zcapsule(r[0], r[1], x, y, z, rad); });
-    }
-    for (int o = 0; o < C.n_sph; o++) {
-        const float4 c0 = S[L.sph + o];
-        env_obstacle(sp, lane, cb, S[L.b_sph + o], m, [&](float x, float y, float z, float rad) {
+    env_pairs(
+        C.n_cap, lane, sw, sp, m, [&](int o, float4 u) { return near3(u.x, u.y, u.z, S[L.b_cap + o], u.w); },
+        [&](int o, float x, float y, float z, float rad) {
+            return hit_capsule(S[L.cap + 2 * o], S[L.cap + 2 * o + 1], x, y, z, rad);
+        });
+    env_pairs(
+        C.n_zcap, lane, sw, sp, m, [&](int o, float4 u) { return near3(u.x, u.y, u.z, S[L.b_zcap + o], u.w); },
+        [&](int o, float x, float y, float z, float rad) {
+            return hit_zcapsule(S[L.zcap + 2 * o], S[L.zcap + 2 * o + 1], x, y, z, rad);
+        });
+    env_pairs(
+        C.n_sph, lane, sw, sp, m, [&](int o, float4 u) { return near3(u.x, u.y, u.z, S[L.sph + o], u.w); },
+        [&](int o, float x, float y, float z, float rad) {
+            const float4 c0 = S[L.sph + o];
             return hit_sphere_sphere(c0.x, c0.y, c0.z, c0.w, x, y, z, rad);
         });
-    }
     return m;
 }
 
@@ -383,10 +414,11 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
 #pragma unroll 1
     for (int b = 0; b < A; b++) {
         MRPOP_PHASE_START();
-        const float4 cb = fk_approx_lane(P.base[b], W, P.rule, seg, P.single ? 0 : b, k, cur, lane);
+        float4 *sw = W.broad.swept[b];
+        fk_approx_lane(P.base[b], W, P.rule, seg, P.single ? 0 : b, k, cur, lane, sw);
         MRPOP_PHASE(P, 0);
         if (do_env) {
-            const uint32_t m = env_mask_approx(S, L, P.sc, cur, lane, cb);
+            const uint32_t m = env_mask_approx(S, L, P.sc, cur, lane, sw);
             uint32_t jm = 0;
 #pragma unroll
             for (int i = 1; i < kNumApprox; i++)
@@ -395,48 +427,57 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
         }
         MRPOP_PHASE(P, 1);
         if (!do_self) continue;
+        // intra-arm pairs: one pair per lane screened by swept bounds, exact
+        // per-sample tests for the survivors
         uint32_t jm = 0;
-#pragma unroll 1
-        for (int t = 0; t < 21; t++) {
-            const int s1 = c_intra_pairs[t][0], s2 = c_intra_pairs[t][1];
-            if (hit_sphere_sphere(cur[s1][0][lane], cur[s1][1][lane], cur[s1][2][lane], c_approx[s1].w,
-                                  cur[s2][0][lane], cur[s2][1][lane], cur[s2][2][lane], c_approx[s2].w))
-                jm |= 1u << approx_joint(s1);
+        {
+            // pair `lane` of c_intra_pairs, computed rather than read per lane
+            const int p1 = lane < 6 ? 0 : lane < 12 ? 1 : lane < 17 ? 2 : 5;
+            const int p2 = lane < 12 ? 5 + lane % 6 : lane == 12 ? 5 : lane < 17 ? lane - 6 : lane - 10;
+            const float4 u1 = sw[p1];
+            const bool c = lane < 21 && near3(u1.x, u1.y, u1.z, sw[p2], u1.w);
+            uint32_t bal = __ballot_sync(kFull, c);
+            while (bal) {
+                const int t = __ffs(bal) - 1;
+                bal &= bal - 1;
+                const int s1 = c_intra_pairs[t][0], s2 = c_intra_pairs[t][1];
+                if (hit_sphere_sphere(cur[s1][0][lane], cur[s1][1][lane], cur[s1][2][lane], c_approx[s1].w,
+                                      cur[s2][0][lane], cur[s2][1][lane], cur[s2][2][lane], c_approx[s2].w))
+                    jm |= 1u << approx_joint(s1);
+            }
         }
         selfw |= (uint64_t)jm << (8 * b);
         MRPOP_PHASE(P, 2);
         if (A == 1) continue;
-        W.broad.armbs[b][lane] = cb;
         // arm-vs-arm against every lower arm a < b; flags go to arm a
-        // (panda_four.cuh:178-214).  Pairs whose bounds are apart in every
-        // lane are skipped; otherwise arm a's spheres are rebuilt.
+        // (panda_four.cuh:178-214).  The 121 sphere pairs are screened by
+        // swept bounds, four rounds of one pair per lane; arm a's spheres are
+        // rebuilt only when some pair survives.
 #pragma unroll 1
         for (int a = 0; a < b; a++) {
-            const float4 ca = W.broad.armbs[a][lane];
-            if (!__any_sync(kFull, near3(cb.x, cb.y, cb.z, ca, cb.w))) continue;
-            fk_approx_lane(P.base[a], W, P.rule, seg, a, k, low, lane);
-            uint32_t qa = 0, qb = 0;
+            const float4 *swa = W.broad.swept[a];
+            uint32_t bal[4];
 #pragma unroll
-            for (int i = 0; i < kNumApprox; i++) {
-                if (near3(low[i][0][lane], low[i][1][lane], low[i][2][lane], cb, c_approx[i].w)) qa |= 1u << i;
-                if (near3(cur[i][0][lane], cur[i][1][lane], cur[i][2][lane], ca, c_approx[i].w)) qb |= 1u << i;
+            for (int r = 0; r < 4; r++) {
+                const int t = 32 * r + lane;
+                const int i = t / kNumApprox, j = t - kNumApprox * i;
+                bal[r] = __ballot_sync(kFull, t < kNumApprox * kNumApprox &&
+                                                  near3(swa[i].x, swa[i].y, swa[i].z, sw[j], swa[i].w));
             }
-            qa = __reduce_or_sync(kFull, qa);
-            qb = __reduce_or_sync(kFull, qb);
+            if (!(bal[0] | bal[1] | bal[2] | bal[3])) continue;
+            fk_approx_lane(P.base[a], W, P.rule, seg, a, k, low, lane, nullptr);
             uint32_t am = 0;
-            while (qa) {
-                const int i = __ffs(qa) - 1;
-                qa &= qa - 1;
-                const float ax = low[i][0][lane], ay = low[i][1][lane], az = low[i][2][lane], ar = c_approx[i].w;
-                bool h = false;
-                uint32_t qj = qb;
-                while (qj) {
-                    const int j = __ffs(qj) - 1;
-                    qj &= qj - 1;
-                    h |= hit_sphere_sphere(ax, ay, az, ar, cur[j][0][lane], cur[j][1][lane], cur[j][2][lane],
-                                           c_approx[j].w);
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                uint32_t q = bal[r];
+                while (q) {
+                    const int t = 32 * r + __ffs(q) - 1;
+                    q &= q - 1;
+                    const int i = t / kNumApprox, j = t - kNumApprox * i;
+                    if (hit_sphere_sphere(low[i][0][lane], low[i][1][lane], low[i][2][lane], c_approx[i].w,
+                                          cur[j][0][lane], cur[j][1][lane], cur[j][2][lane], c_approx[j].w))
+                        am |= 1u << approx_joint(i);
                 }
-                if (h) am |= 1u << approx_joint(i);
             }
             selfw |= (uint64_t)am << (8 * a);
         }
@@ -590,33 +631,67 @@ __device__ __forceinline__ bool env_exact(const float4 *S, const SceneLayout &L,
     return hit_sphere_sphere(c0.x, c0.y, c0.z, c0.w, x, y, z, r);
 }
 
-// Env test of the spheres of group g (sphere 0 is never env-tested): obstacles
-// are screened against the group bound in chunks of 64, then per sphere.
-static __device__ __noinline__ bool env_group(const float4 *S, const SceneLayout &L, const SceneCounts &C,
-                                              const Xf &T, int g, float4 gl) {
+// Conservative screen of obstacle o (index over all classes, in the order of
+// env_exact) against ball U: the obstacle's bounding sphere, then for cuboids
+// with orthonormal axes the exact sphere-cuboid test with U's radius.
+__device__ __forceinline__ bool screen_obstacle(const float4 *S, const SceneLayout &L, const SceneCounts &C, int o,
+                                                float4 U) {
+    const float4 bs = S[L.b_cub + o];
+    if (!near3(U.x, U.y, U.z, bs, U.w)) return false;
+    if (bs.w > 1e17f) return true;
+    if (o < C.n_cub) {
+        const float4 *c = S + L.cub + 4 * o;
+        return hit_cuboid(c[0], c[1], c[2], c[3], U.x, U.y, U.z, U.w * U.w);
+    }
+    o -= C.n_cub;
+    if (o < C.n_zcub) {
+        const float4 *c = S + L.zcub + 4 * o;
+        return hit_zcuboid(c[0], c[1], c[2], U.x, U.y, U.z, U.w * U.w);
+    }
+    return true;
+}
+
+// Env test of the spheres of sub-group g (sphere 0 is never env-tested) for
+// the lanes with act set; every lane of the warp calls it.  The active lanes'
+// group bounds are merged into one ball U (box of their centres, half
+// diagonal + group radius); obstacles are screened against U one per lane, 32
+// at a time, and each active lane tests its spheres against the survivors.
+static __device__ __noinline__ bool env_group_warp(const float4 *S, const SceneLayout &L, const SceneCounts &C,
+                                                   const Xf &T, int g, float4 gl, bool act) {
+    const int lane = threadIdx.x & 31;
     const float3 gc = place_reg(T, gl);
+    constexpr float kBig = 3.0e38f;
+    const float lx = warp_min(act ? gc.x : kBig), hx = warp_max(act ? gc.x : -kBig);
+    const float ly = warp_min(act ? gc.y : kBig), hy = warp_max(act ? gc.y : -kBig);
+    const float lz = warp_min(act ? gc.z : kBig), hz = warp_max(act ? gc.z : -kBig);
+    const float dx = hx - lx, dy = hy - ly, dz = hz - lz;
+    const float4 U = make_float4(0.5f * (lx + hx), 0.5f * (ly + hy), 0.5f * (lz + hz),
+                                 0.5f * sqrtf(dx * dx + dy * dy + dz * dz) * 1.004f + gl.w);
     const int n_obst = C.n_cub + C.n_zcub + C.n_cap + C.n_zcap + C.n_sph;
     const int i0 = grp_first(g) == 0 ? 1 : grp_first(g), i1 = grp_first(g + 1);
-    for (int base = 0; base < n_obst; base += 64) {
-        const int n = min(64, n_obst - base);
-        uint64_t m = 0;
-        for (int t = 0; t < n; t++)
-            if (near3(gc.x, gc.y, gc.z, S[L.b_cub + base + t], gl.w)) m |= 1ull << t;
-        if (!m) continue;
-        for (int i = i0; i < i1; i++) {
+    bool hit = false;
+#pragma unroll 1
+    for (int base = 0; base < n_obst; base += 32) {
+        if (__all_sync(kFull, !act || hit)) break;
+        const int o = base + lane;
+        const uint32_t m = __ballot_sync(kFull, o < n_obst && screen_obstacle(S, L, C, o, U));
+        if (!m || !act || hit) continue;
+        for (int i = i0; i < i1 && !hit; i++) {
             const float4 sd = c_det[i];
             const float3 p = place_reg(T, sd);
-            uint64_t mm = m;
+            uint32_t mm = m;
             while (mm) {
-                const int t = __ffsll((long long)mm) - 1;
+                const int t = __ffs(mm) - 1;
                 mm &= mm - 1;
                 if (near3(p.x, p.y, p.z, S[L.b_cub + base + t], sd.w) &&
-                    env_exact(S, L, C, base + t, p.x, p.y, p.z, sd.w))
-                    return true;
+                    env_exact(S, L, C, base + t, p.x, p.y, p.z, sd.w)) {
+                    hit = true;
+                    break;
+                }
             }
         }
     }
-    return false;
+    return hit;
 }
 
 // Per-lane state of the lane-parallel detailed check of one arm.
@@ -632,16 +707,13 @@ struct LaneCtx {
 // (screened by the target group's bound).
 __device__ __forceinline__ void lane_joint(int j, const EdgeParams &P, const Xf &T, LaneCtx &c, WarpScratch &W,
                                            const float4 *S, const SceneLayout &L, const float4 *det_tab, int lane) {
-    if (c.hit) return;
-    if (c.em >> j & 1u) {
+    // every lane takes part in the env screening (warp-wide votes inside)
+    if (__any_sync(kFull, !c.hit && (c.em >> j & 1u))) {
 #pragma unroll 1
         for (int g = jgrp_first(j); g < jgrp_first(j + 1); g++)
-            if (env_group(S, L, P.sc, T, g, P.grp[g])) {
-                c.hit = true;
-                return;
-            }
+            if (env_group_warp(S, L, P.sc, T, g, P.grp[g], !c.hit && (c.em >> j & 1u))) c.hit = true;
     }
-    if (!c.rm) return;
+    if (c.hit || !c.rm) return;
     uint32_t m1 = c.rm & c_rows.jfirst[c.quirk][j];
     while (m1) {
         const int r = __ffs(m1) - 1;
@@ -685,11 +757,13 @@ __device__ __forceinline__ void lane_joint(int j, const EdgeParams &P, const Xf 
     }
 }
 
-// Lane-parallel detailed check of this lane's sample: every arm's chain is
-// rebuilt in registers; env tests of env-flagged joints and the intra-arm rows
-// of self-flagged joints run as the frames stream by (the first sphere of
-// each row is stashed until its targets come).  Writes each arm's detailed
-// bound for the arm-vs-arm part.  Returns true if a test fired.
+// Lane-parallel detailed check of this lane's sample, called by every lane of
+// the warp (de = ds = false for a lane without a candidate sample): every
+// arm's chain is rebuilt in registers; env tests of env-flagged joints
+// (screened warp-wide per sub-group) and the intra-arm rows of self-flagged
+// joints run as the frames stream by (the first sphere of each row is stashed
+// until its targets come).  Writes each arm's detailed bound for the
+// arm-vs-arm part.  Returns true if a test fired.
 template <int A>
 static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch &W, const float4 *S,
                                                 const SceneLayout &L, const float4 *det_tab, int seg, int k,
@@ -699,7 +773,8 @@ static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch
     c.quirk = (!P.single && !(P.flags & kExactBit)) ? 1 : 0;
     c.hit = false;
 #pragma unroll 1
-    for (int a = 0; a < A && !c.hit; a++) {
+    for (int a = 0; a < A; a++) {
+        if (__all_sync(kFull, c.hit || !(de || ds))) break;
         c.em = de ? (uint32_t)(envw >> (8 * a)) & 0xffu : 0u;
         const uint32_t sm = ds ? (uint32_t)(selfw >> (8 * a)) & 0xffu : 0u;
         c.rm = sm ? row_mask(sm, c.quirk != 0) : 0u;
@@ -990,12 +1065,11 @@ __device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &
     for (int s = 0; s < SPL; s++) {
         const int bit = lane + 32 * s;
         const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
-        bool h = false;
         uint32_t pm = 0;
-        if (dE || dS) {
-            h = narrow_lane<A>(P, W, S, L, det_tab, seg, bit + 1, envw[s], selfw[s], dE, dS, max_group_r);
-            if (!h && A > 1) pm = cross_pairs<A>(W, selfw[s], dS);
-        }
+        // every lane walks the arms (warp-wide screening inside); lanes
+        // without a candidate sample only keep the others company
+        bool h = narrow_lane<A>(P, W, S, L, det_tab, seg, bit + 1, envw[s], selfw[s], dE, dS, max_group_r);
+        if ((dE || dS) && !h && A > 1) pm = cross_pairs<A>(W, selfw[s], dS);
         MRPOP_PHASE(P, 5);
         if (A > 1 && __any_sync(kFull, pm != 0u)) h |= cross_lane<A>(P, W, seg, bit + 1, selfw[s], pm);
         MRPOP_PHASE(P, 6);

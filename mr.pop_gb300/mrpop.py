@@ -29,8 +29,9 @@ EXPORTED = [
     "mrpop_robotset_destroy", "mrpop_validate_edges", "mrpop_validate_segments", "mrpop_workspace_create",
     "mrpop_workspace_destroy", "mrpop_validate_edges_host", "mrpop_fk_spheres", "mrpop_count_flops",
     "mrpop_debug_trig", "mrpop_fp32_peak_probe", "mrpop_last_error", "mrpop_version",
-    "mrpop_validate_edges_noalloc",
+    "mrpop_validate_edges_noalloc", "mrpop_broad_flops_per_sample", "mrpop_kernel_timing", "mrpop_kernel_times",
 ]
+KERNEL_KINDS = ("fused", "broad", "narrow")
 NOALLOC_MAX_EDGES = 16384
 
 
@@ -80,6 +81,9 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
         "mrpop_debug_trig": [vp, i64, vp, vp, vp],
         "mrpop_fp32_peak_probe": [i32, i32, vp, C.POINTER(C.c_double), vp],
         "mrpop_validate_edges_noalloc": [vp, vp, vp, vp, i64, i32, u32, i32, vp, vp, vp],
+        "mrpop_broad_flops_per_sample": [vp, vp, u32, i32, C.POINTER(C.c_double)],
+        "mrpop_kernel_timing": [i32],
+        "mrpop_kernel_times": [C.POINTER(C.c_int64), C.POINTER(C.c_double)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -253,6 +257,29 @@ def fp32_peak_probe(blocks: int, iters: int, scratch, stream=None, lib: C.CDLL |
     f = C.c_double()
     _check(lib, lib.mrpop_fp32_peak_probe(blocks, iters, scratch.data_ptr(), C.byref(f), _stream_ptr(stream)))
     return f.value
+
+
+def broad_flops_per_sample(scene: Scene, robots: RobotSet, flags: int = CHECK_ENV | CHECK_SELF,
+                           arm: int = -1) -> float:
+    """Algorithmic (unculled) broad-phase flops of one sample, FMA = 2."""
+    f = C.c_double()
+    _check(scene.lib, scene.lib.mrpop_broad_flops_per_sample(scene.handle, robots.handle, flags, arm, C.byref(f)))
+    return f.value
+
+
+def kernel_timing(enable: bool, lib: C.CDLL | None = None) -> None:
+    """Turn the library's per-kernel CUDA-event timing on or off."""
+    lib = lib or library()
+    _check(lib, lib.mrpop_kernel_timing(1 if enable else 0))
+
+
+def kernel_times(lib: C.CDLL | None = None) -> dict:
+    """{kind: (launches, total ms)} recorded since the previous read."""
+    lib = lib or library()
+    n = (C.c_int64 * 3)()
+    ms = (C.c_double * 3)()
+    _check(lib, lib.mrpop_kernel_times(n, ms))
+    return {k: (int(n[i]), float(ms[i])) for i, k in enumerate(KERNEL_KINDS)}
 
 
 class Workspace:
