@@ -219,6 +219,13 @@ mrpop_status mrpop_broad_flops_per_sample(const mrpop_scene *scene, const mrpop_
 mrpop_status mrpop_kernel_timing(int enable);
 mrpop_status mrpop_kernel_times(int64_t *launches, double *ms);
 
+/* Test utility, no counterpart in the reference: the host copy of the
+ * forearm-hand rows table (bit i6 * n7 + i7 set when the detailed self rows
+ * between the joint-5 spheres and the hand cannot fire for any (q6, q7) in
+ * cell (i6, i7) of the joint-6 x joint-7 limit box, cells of equal size).
+ * out needs n6 * n7 / 32 words; 3072 today. */
+mrpop_status mrpop_debug_row5_table(uint32_t *out, int64_t words, int *n6, int *n7);
+
 /* The __cosf/__sinf values the validator uses for inputs x (device arrays). */
 mrpop_status mrpop_debug_trig(const float *x, int64_t n, float *cos_out, float *sin_out,
                               void *stream);

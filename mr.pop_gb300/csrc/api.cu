@@ -132,6 +132,78 @@ double broad_flops_per_sample(int A, double env_test_flops, uint32_t flags) {
     return f;
 }
 
+// Forearm-hand rows table (panda_model.cuh): built once per process on the
+// host, copied once per device into g_row5 when the device's first scene is
+// created.
+__device__ uint32_t g_row5[mrpop::kRow5Words];
+
+const std::vector<uint32_t> &row5_host_table() {
+    static std::vector<uint32_t> tab;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        using namespace mrpop;
+        tab.assign(kRow5Words, 0u);
+        const double h6 = ((double)kRow5Hi6 - kRow5Lo6) / kRow5N6, h7 = ((double)kRow5Hi7 - kRow5Lo7) / kRow5N7;
+        constexpr int s0 = 17, s1 = 28, t0 = 32, t1 = 58;
+        double R[s1 - s0 + 1], slack[t1 - t0 + 1];
+        for (int s = s0; s <= s1; s++)
+            R[s - s0] = s + 4 <= s1 ? std::fmax(kDet[s].r, kDet[s + 4].r) : (double)kDet[s].r;
+        for (int t = t0; t <= t1; t++) {
+            const SphereDef &x = kDet[t];
+            const double n = std::sqrt((double)x.x * x.x + (double)x.y * x.y + (double)x.z * x.z);
+            const double rxy = std::sqrt((double)x.x * x.x + (double)x.y * x.y);
+            // a hand sphere moves at most (distance from the joint axis) x (angle) per joint:
+            // <= |F7 translation| + |x| from axis 6, exactly |x_xy| from axis 7
+            slack[t - t0] = (0.088 + n) * (0.5 * h6 + 1e-4) + rxy * (0.5 * h7 + 1e-4);
+        }
+        for (int i6 = 0; i6 < kRow5N6; i6++) {
+            const double q6 = kRow5Lo6 + (i6 + 0.5) * h6, c6 = std::cos(q6), sn6 = std::sin(q6);
+            for (int i7 = 0; i7 < kRow5N7; i7++) {
+                const double q7 = kRow5Lo7 + (i7 + 0.5) * h7, c7 = std::cos(q7), sn7 = std::sin(q7);
+                double gap = 1e30;
+                for (int t = t0; t <= t1 && gap > kRow5Margin; t++) {
+                    // hand sphere in the joint-5 frame: F6 Rz(q6) F7 Rz(q7) x
+                    const SphereDef &x = kDet[t];
+                    const double y0 = c7 * x.x - sn7 * x.y + 0.088, y1 = -(double)x.z, y2 = sn7 * x.x + c7 * x.y;
+                    const double p0 = c6 * y0 - sn6 * y1, p1 = -y2, p2 = sn6 * y0 + c6 * y1;
+                    for (int s = s0; s <= s1; s++) {
+                        const double d0 = kDet[s].x - p0, d1 = kDet[s].y - p1, d2 = kDet[s].z - p2;
+                        gap = std::fmin(gap, std::sqrt(d0 * d0 + d1 * d1 + d2 * d2) - R[s - s0] - x.r -
+                                                 slack[t - t0]);
+                    }
+                }
+                if (gap > kRow5Margin) {
+                    const int cell = i6 * kRow5N7 + i7;
+                    tab[cell >> 5] |= 1u << (cell & 31);
+                }
+            }
+        }
+    });
+    return tab;
+}
+
+std::mutex g_row5_mu;
+const uint32_t *g_row5_dev[64] = {};
+
+// Device copy of the table on the current device (uploaded on first use).
+cudaError_t row5_device_table(const uint32_t **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    const std::vector<uint32_t> &tab = row5_host_table();
+    std::lock_guard<std::mutex> lk(g_row5_mu);
+    if (!g_row5_dev[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_row5);
+        if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_row5, tab.data(), tab.size() * sizeof(uint32_t));
+        if (e != cudaSuccess) return e;
+        g_row5_dev[dev] = (const uint32_t *)p;
+    }
+    *out = g_row5_dev[dev];
+    return cudaSuccess;
+}
+
 // Largest staged scene: the block's dynamic shared memory stays below this.
 constexpr size_t kMaxDynSmem = 200 * 1024;
 
@@ -139,6 +211,7 @@ constexpr size_t kMaxDynSmem = 200 * 1024;
 
 struct mrpop_scene {
     float4 *d_buf = nullptr;          // packed obstacles (float4 units)
+    const uint32_t *row5 = nullptr;   // forearm-hand rows table on the scene's device
     unsigned int *d_status = nullptr; // bounded-wait error word
     mrpop::SceneCounts counts{};
     int total_f4 = 0;
@@ -249,7 +322,8 @@ mrpop_status mrpop_scene_create(const mrpop_scene_desc *desc, mrpop_scene **out)
     sc->total_f4 = L.total;
     sc->env_test_flops = 27.0 * (c.n_cub + c.n_zcub) + 26.0 * (c.n_cap + c.n_zcap) + 11.0 * c.n_sph;
     cudaGetDevice(&sc->device);
-    cudaError_t e = cudaMalloc(&sc->d_status, sizeof(unsigned int));
+    cudaError_t e = row5_device_table(&sc->row5);
+    if (e == cudaSuccess) e = cudaMalloc(&sc->d_status, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMemset(sc->d_status, 0, sizeof(unsigned int));
     if (e == cudaSuccess && L.total > 0) e = cudaMalloc(&sc->d_buf, (size_t)L.total * sizeof(float4));
     if (e == cudaSuccess && L.total > 0)
@@ -360,6 +434,7 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
     p.status = scene->d_status;
     p.phase = g_phase_counters;
     p.env_test_flops = scene->env_test_flops;
+    p.row5 = scene->row5;
     for (int j = 0; j < mrpop::kNumJoints; j++) {
         double r = 0.0;
         for (int i = mrpop::kDetFirst[j]; i < mrpop::kDetFirst[j + 1]; i++) {
@@ -532,6 +607,16 @@ mrpop_status mrpop_broad_flops_per_sample(const mrpop_scene *scene, const mrpop_
     if (!scene || !robots || !out) return fail(MRPOP_ERR_INVALID_ARGUMENT, "broad_flops_per_sample: null argument");
     if (arm >= robots->n_arms) return fail(MRPOP_ERR_INVALID_ARGUMENT, "broad_flops_per_sample: arm out of range");
     *out = broad_flops_per_sample(arm >= 0 ? 1 : robots->n_arms, scene->env_test_flops, flags);
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_debug_row5_table(uint32_t *out, int64_t words, int *n6, int *n7) {
+    if (!out || !n6 || !n7) return fail(MRPOP_ERR_INVALID_ARGUMENT, "debug_row5_table: null argument");
+    if (words < mrpop::kRow5Words) return fail(MRPOP_ERR_INVALID_ARGUMENT, "debug_row5_table: buffer too small");
+    const std::vector<uint32_t> &tab = row5_host_table();
+    std::memcpy(out, tab.data(), tab.size() * sizeof(uint32_t));
+    *n6 = mrpop::kRow5N6;
+    *n7 = mrpop::kRow5N7;
     return MRPOP_OK;
 }
 

@@ -35,6 +35,7 @@ namespace mrpop {
 #define MRPOP_PHASE_START() long long _phase_t = clock64();
 #define MRPOP_PHASE(P, i)                                                                          \
     do {                                                                                           \
+        __syncwarp();                                                                              \
         const long long _n = clock64();                                                            \
         if ((P).phase && (threadIdx.x & 31) == 0)                                                  \
             atomicAdd((P).phase + (i), (unsigned long long)(_n - _phase_t));                       \
@@ -44,7 +45,25 @@ namespace mrpop {
     do {                                                                                           \
         if ((P).phase && (threadIdx.x & 31) == 0) atomicAdd((P).phase + (i), (unsigned long long)(v)); \
     } while (0)
+// counter update from code without the parameter block (warp-uniform v)
+// (per translation unit; set from the parameter block by the kernel prologue)
+static __device__ unsigned long long *g_dev_phase;
+#define MRPOP_PHASE_BIND(P) do { if (threadIdx.x == 0) g_dev_phase = (P).phase; __syncthreads(); } while (0)
+// count of lanes with pred set; the vote runs on every lane of the warp,
+// only the add is lane 0's
+#define MRPOP_COUNT_LANES(i, pred)                                                                 \
+    do {                                                                                           \
+        const uint32_t _votes = __ballot_sync(kFull, (pred));                                      \
+        MRPOP_COUNT_W(i, __popc(_votes));                                                          \
+    } while (0)
+#define MRPOP_COUNT_W(i, v)                                                                        \
+    do {                                                                                           \
+        if (g_dev_phase && (threadIdx.x & 31) == 0) atomicAdd(g_dev_phase + (i), (unsigned long long)(v)); \
+    } while (0)
 #else
+#define MRPOP_COUNT_W(i, v) do { } while (0)
+#define MRPOP_PHASE_BIND(P) do { } while (0)
+#define MRPOP_COUNT_LANES(i, pred) do { } while (0)
 #define MRPOP_PHASE_START()
 #define MRPOP_PHASE(P, i) do { } while (0)
 #define MRPOP_COUNT(P, i, v) do { } while (0)
@@ -109,6 +128,7 @@ struct EdgeParams {
     uint64_t *smasks;           // split pipeline: per-edge {env, self} candidate masks
     float group_r[kNumJoints];  // bounding radius of each joint's detailed spheres (+margin)
     float4 grp[11];             // detailed sub-group bounds in their joint frame (+margin)
+    const uint32_t *row5;       // forearm-hand rows table (kRow5N6 x kRow5N7 bits), or nullptr
     float base[kMaxArms][12];   // row-major 3x4 per arm of this check
 };
 
@@ -675,6 +695,9 @@ static __device__ __noinline__ bool env_group_warp(const float4 *S, const SceneL
         if (__all_sync(kFull, !act || hit)) break;
         const int o = base + lane;
         const uint32_t m = __ballot_sync(kFull, o < n_obst && screen_obstacle(S, L, C, o, U));
+        MRPOP_COUNT_W(11, 1);
+        MRPOP_COUNT_W(12, __popc(m));
+        MRPOP_COUNT_LANES(13, act && !hit);
         if (!m || !act || hit) continue;
         for (int i = i0; i < i1 && !hit; i++) {
             const float4 sd = c_det[i];
@@ -694,6 +717,16 @@ static __device__ __noinline__ bool env_group_warp(const float4 *S, const SceneL
     return hit;
 }
 
+// True when the forearm-hand rows cannot fire at joint values (q6, q7): the
+// cell's bit of the table is set.  NaN or out-of-range values give false.
+__device__ __forceinline__ bool row5_apart(const uint32_t *tab, float q6, float q7) {
+    const float f6 = (q6 - kRow5Lo6) * ((float)kRow5N6 / (kRow5Hi6 - kRow5Lo6));
+    const float f7 = (q7 - kRow5Lo7) * ((float)kRow5N7 / (kRow5Hi7 - kRow5Lo7));
+    if (!(f6 >= 0.0f && f6 < (float)kRow5N6 && f7 >= 0.0f && f7 < (float)kRow5N7)) return false;
+    const int cell = (int)f6 * kRow5N7 + (int)f7;
+    return (__ldg(tab + (cell >> 5)) >> (cell & 31)) & 1u;
+}
+
 // Per-lane state of the lane-parallel detailed check of one arm.
 struct LaneCtx {
     uint32_t em;  // env-flagged joints
@@ -705,14 +738,18 @@ struct LaneCtx {
 // Joint j of one arm, frame T: env tests of an env-flagged joint, stash of the
 // first spheres of flagged rows, and the row tests whose targets are here
 // (screened by the target group's bound).
-__device__ __forceinline__ void lane_joint(int j, const EdgeParams &P, const Xf &T, LaneCtx &c, WarpScratch &W,
-                                           const float4 *S, const SceneLayout &L, const float4 *det_tab, int lane) {
+__device__ __forceinline__ void lane_env(int j, const EdgeParams &P, const Xf &T, LaneCtx &c, const float4 *S,
+                                         const SceneLayout &L) {
     // every lane takes part in the env screening (warp-wide votes inside)
     if (__any_sync(kFull, !c.hit && (c.em >> j & 1u))) {
 #pragma unroll 1
         for (int g = jgrp_first(j); g < jgrp_first(j + 1); g++)
             if (env_group_warp(S, L, P.sc, T, g, P.grp[g], !c.hit && (c.em >> j & 1u))) c.hit = true;
     }
+}
+
+__device__ __forceinline__ void lane_rows(int j, const EdgeParams &P, const Xf &T, LaneCtx &c, WarpScratch &W,
+                                          const float4 *det_tab, int lane) {
     if (c.hit || !c.rm) return;
     uint32_t m1 = c.rm & c_rows.jfirst[c.quirk][j];
     while (m1) {
@@ -772,6 +809,7 @@ static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch
     LaneCtx c;
     c.quirk = (!P.single && !(P.flags & kExactBit)) ? 1 : 0;
     c.hit = false;
+    MRPOP_PHASE_START();
 #pragma unroll 1
     for (int a = 0; a < A; a++) {
         if (__all_sync(kFull, c.hit || !(de || ds))) break;
@@ -779,6 +817,9 @@ static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch
         const uint32_t sm = ds ? (uint32_t)(selfw >> (8 * a)) & 0xffu : 0u;
         c.rm = sm ? row_mask(sm, c.quirk != 0) : 0u;
         const int qa = 7 * (P.single ? 0 : a);
+        if (P.row5 && (c.rm & row5_rows(c.quirk)) &&
+            row5_apart(P.row5, sample_q1(W, P.rule, seg, qa + 5, k), sample_q1(W, P.rule, seg, qa + 6, k)))
+            c.rm &= ~row5_rows(c.quirk);
         Xf T;
         load_base(T, P.base[a]);
         float lx = T.m[3], hx = T.m[3], ly = T.m[7], hy = T.m[7], lz = T.m[11], hz = T.m[11];
@@ -791,7 +832,11 @@ static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch
             hy = fmaxf(hy, T.m[7]);
             lz = fminf(lz, T.m[11]);
             hz = fmaxf(hz, T.m[11]);
-            lane_joint(j, P, T, c, W, S, L, det_tab, lane);
+            MRPOP_PHASE(P, 8);
+            lane_env(j, P, T, c, S, L);
+            MRPOP_PHASE(P, 9);
+            lane_rows(j, P, T, c, W, det_tab, lane);
+            MRPOP_PHASE(P, 10);
         }
         // bound of every joint origin (half-diagonal of their box) plus the
         // largest sub-group radius about a joint origin
@@ -1071,7 +1116,11 @@ __device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &
         bool h = narrow_lane<A>(P, W, S, L, det_tab, seg, bit + 1, envw[s], selfw[s], dE, dS, max_group_r);
         if ((dE || dS) && !h && A > 1) pm = cross_pairs<A>(W, selfw[s], dS);
         MRPOP_PHASE(P, 5);
-        if (A > 1 && __any_sync(kFull, pm != 0u)) h |= cross_lane<A>(P, W, seg, bit + 1, selfw[s], pm);
+        MRPOP_COUNT_LANES(14, dE || dS);
+        if (A > 1 && __any_sync(kFull, pm != 0u)) {
+            MRPOP_COUNT_W(15, 1);
+            h |= cross_lane<A>(P, W, seg, bit + 1, selfw[s], pm);
+        }
         MRPOP_PHASE(P, 6);
         hits |= (uint64_t)__ballot_sync(kFull, h) << (32 * s);
         if (hits) break; // later slots hold only later samples
@@ -1091,6 +1140,7 @@ __device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &
     WarpScratch &W = Wall[warp];                                                                       \
     for (int i = threadIdx.x; i < kNumDet; i += blockDim.x) det_tab[i] = c_det[i];                     \
     const bool staged = stage_scene(S, P.scene, (uint32_t)(L.total * sizeof(float4)), &bar, P.status); \
+    MRPOP_PHASE_BIND(P);                                                                               \
     const int g = P.g;                                                                                 \
     const int dof = 7 * (P.single ? 1 : A);                                                            \
     float max_group_r = 0.f;                                                                           \

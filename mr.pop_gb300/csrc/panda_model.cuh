@@ -125,6 +125,29 @@ __host__ __device__ __forceinline__ constexpr int det_row_hi(int r) {
 }
 constexpr int kDetRows = 25;
 
+// Forearm-hand rows.  The rows whose first-read sphere sits on joint 5
+// (positions 17..28: rows 13..24 by sphere index, rows 17..24 in the
+// composite robots' reading) test it against the hand spheres 32..58 of
+// joint 7.  Their distances depend only on q6 and q7 (the frames between are
+// F6 Rz(q6) F7 Rz(q7)), and the Panda's approx spheres 5 and 7/8 overlap in
+// every configuration, so these rows are flagged in every sample.  A table
+// over (q6, q7) cells, built on the host in double precision, marks the cells
+// where every such pair is apart by more than kRow5Margin for every
+// configuration in the cell (distance at the cell centre minus the largest
+// displacement a hand sphere can make inside the cell, with the larger of the
+// two radii a row can read).  For a sample in a marked cell those rows cannot
+// fire (the FP32 evaluation errs by ~1e-5 m at most), so they are skipped;
+// samples outside the table's range are tested as usual.
+constexpr int kRow5N6 = 256, kRow5N7 = 384;
+constexpr int kRow5Words = kRow5N6 * kRow5N7 / 32;
+constexpr float kRow5Lo6 = -0.0873f, kRow5Hi6 = 3.8223f;  // joint 6 limits (Robots.hh:13-23)
+constexpr float kRow5Lo7 = -2.9671f, kRow5Hi7 = 2.9671f;  // joint 7 limits
+constexpr double kRow5Margin = 2e-4;
+// rows covered, by reading: [0] sphere index (single arm, EXACT), [1] composite
+__host__ __device__ __forceinline__ constexpr uint32_t row5_rows(int quirk) {
+    return quirk ? 0x01FE0000u /* rows 17..24 */ : 0x01FFE000u /* rows 13..24 */;
+}
+
 // ---------------------------------------------------------------------------
 // exact-order arithmetic helpers
 // ---------------------------------------------------------------------------

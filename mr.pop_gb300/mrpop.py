@@ -30,6 +30,7 @@ EXPORTED = [
     "mrpop_workspace_destroy", "mrpop_validate_edges_host", "mrpop_fk_spheres", "mrpop_count_flops",
     "mrpop_debug_trig", "mrpop_fp32_peak_probe", "mrpop_last_error", "mrpop_version",
     "mrpop_validate_edges_noalloc", "mrpop_broad_flops_per_sample", "mrpop_kernel_timing", "mrpop_kernel_times",
+    "mrpop_debug_row5_table",
 ]
 KERNEL_KINDS = ("fused", "broad", "narrow")
 NOALLOC_MAX_EDGES = 16384
@@ -84,6 +85,7 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
         "mrpop_broad_flops_per_sample": [vp, vp, u32, i32, C.POINTER(C.c_double)],
         "mrpop_kernel_timing": [i32],
         "mrpop_kernel_times": [C.POINTER(C.c_int64), C.POINTER(C.c_double)],
+        "mrpop_debug_row5_table": [vp, i64, C.POINTER(C.c_int), C.POINTER(C.c_int)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -265,6 +267,16 @@ def broad_flops_per_sample(scene: Scene, robots: RobotSet, flags: int = CHECK_EN
     f = C.c_double()
     _check(scene.lib, scene.lib.mrpop_broad_flops_per_sample(scene.handle, robots.handle, flags, arm, C.byref(f)))
     return f.value
+
+
+def row5_table(lib: C.CDLL | None = None) -> np.ndarray:
+    """The forearm-hand rows table as a bool array [n6, n7] (True: rows apart)."""
+    lib = lib or library()
+    words = np.zeros(1 << 14, np.uint32)
+    n6, n7 = C.c_int(), C.c_int()
+    _check(lib, lib.mrpop_debug_row5_table(words.ctypes.data, len(words), C.byref(n6), C.byref(n7)))
+    bits = np.unpackbits(words.view(np.uint8), bitorder="little")[: n6.value * n7.value]
+    return bits.reshape(n6.value, n7.value).astype(bool)
 
 
 def kernel_timing(enable: bool, lib: C.CDLL | None = None) -> None:

@@ -804,6 +804,13 @@ int64_t oracle_edge_samples(const float *q0, const float *q1, int dim, int g, in
     return w;
 }
 
+/* The detailed sphere table {x, y, z, r} x 59 (local frames), for tests. */
+int oracle_det_spheres(float *out) {
+    for (int i = 0; i < OR_ND; i++)
+        for (int c = 0; c < 4; c++) out[4 * i + c] = OR_DET_SPH[i][c];
+    return 0;
+}
+
 int oracle_max_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

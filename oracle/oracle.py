@@ -50,6 +50,8 @@ def lib() -> C.CDLL:
         L.oracle_segment_count.argtypes = [vp, vp, C.c_int, C.c_int, C.c_float]
         L.oracle_segment_count.restype = C.c_int
         L.oracle_max_threads.restype = C.c_int
+        L.oracle_det_spheres.argtypes = [vp]
+        L.oracle_det_spheres.restype = C.c_int
         L.oracle_env_hit.argtypes = [C.POINTER(_Scene), C.c_float, C.c_float, C.c_float, C.c_float, C.c_int]
         L.oracle_env_hit.restype = C.c_int
         L.oracle_env_sd.argtypes = [C.POINTER(_Scene), C.c_double, C.c_double, C.c_double, C.c_double]
@@ -160,6 +162,13 @@ def env_sd(scene, x, y, z, r) -> float:
     """FP64 signed distance of one sphere to the closest obstacle."""
     sc, keep = _scene_struct(scene)
     return float(lib().oracle_env_sd(C.byref(sc), float(x), float(y), float(z), float(r)))
+
+
+def det_spheres() -> np.ndarray:
+    """The detailed sphere table (59, 4): local centre and radius."""
+    out = np.zeros((59, 4), np.float32)
+    lib().oracle_det_spheres(out.ctypes.data)
+    return out
 
 
 def max_threads() -> int:

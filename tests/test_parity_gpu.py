@@ -248,3 +248,42 @@ def test_full_size_properties(cuda, pkg, orc):
     ref = orc.validate(wl.scene, wl.bases, wl.q0[sub], wl.q1[sub], 32, wl.flags, trig=trig)
     assert np.array_equal(a[0][sub], ref["valid"]) and np.array_equal(a[1][sub], ref["first_hit"])
     assert scene.status() == 0
+
+
+def test_forearm_hand_rows_near_contact(cuda, pkg, orc):
+    """Edges whose joint-6/7 values cross the cells where the forearm-hand rows
+    can fire (the table leaves those cells unmarked): verdicts still match the
+    oracle, composite and single-arm readings, REF and EXACT modes."""
+    W = pkg.workloads
+    T = pkg.mrpop.row5_table()
+    rng = np.random.default_rng(77)
+    bad = np.argwhere(~T)
+    n = 256
+    bases = W.bases_config2()
+    q0, q1 = W.random_edges(rng, n, 4, 0.6)
+    for a in range(4):
+        pick = bad[rng.integers(0, len(bad), n)]
+        q6 = -0.0873 + (pick[:, 0] + rng.uniform(0, 1, n)) * (3.8223 + 0.0873) / 256
+        q7 = -2.9671 + (pick[:, 1] + rng.uniform(0, 1, n)) * (2 * 2.9671) / 384
+        q0[:, 7 * a + 5], q0[:, 7 * a + 6] = q6, q7
+        q1[:, 7 * a + 5] = np.clip(q6 + rng.uniform(-0.1, 0.1, n), -0.0873, 3.8223)
+        q1[:, 7 * a + 6] = np.clip(q7 + rng.uniform(-0.1, 0.1, n), -2.9671, 2.9671)
+    q0, q1 = q0.astype(np.float32), q1.astype(np.float32)
+    sc = W.scene_config2(4)
+    scene = pkg.Scene(sc)
+    rb = pkg.RobotSet(4, bases)
+    trig = _edge_trig(cuda, pkg, orc, q0, q1, 32)
+    fired = 0
+    for flags in (pkg.CHECK_SELF, pkg.CHECK_SELF | pkg.MODE_EXACT, pkg.CHECK_ENV | pkg.CHECK_SELF):
+        wl = W.Workload("t", sc, bases, q0, q1, 32, flags)
+        got = _run(cuda, pkg, scene, rb, wl)
+        ref = orc.validate(sc, bases, q0, q1, 32, flags, trig=trig)
+        assert np.array_equal(got[0], ref["valid"]) and np.array_equal(got[1], ref["first_hit"])
+        fired += int((ref["valid"] == 0).sum())
+        for a in range(4):
+            qa0, qa1 = np.ascontiguousarray(q0[:, 7 * a:7 * a + 7]), np.ascontiguousarray(q1[:, 7 * a:7 * a + 7])
+            wl = W.Workload("t", sc, bases, qa0, qa1, 32, flags, arm=a)
+            got = _run(cuda, pkg, scene, rb, wl)
+            ref = orc.validate(sc, bases, qa0, qa1, 32, flags, arm=a, trig=trig)
+            assert np.array_equal(got[0], ref["valid"]) and np.array_equal(got[1], ref["first_hit"])
+    assert fired > 0
