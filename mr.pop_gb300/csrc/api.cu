@@ -435,14 +435,6 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
     p.phase = g_phase_counters;
     p.env_test_flops = scene->env_test_flops;
     p.row5 = scene->row5;
-    for (int j = 0; j < mrpop::kNumJoints; j++) {
-        double r = 0.0;
-        for (int i = mrpop::kDetFirst[j]; i < mrpop::kDetFirst[j + 1]; i++) {
-            const mrpop::SphereDef &d = mrpop::kDet[i];
-            r = std::fmax(r, std::sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z) + d.r);
-        }
-        p.group_r[j] = (float)(r * 1.001 + mrpop::kCullMargin);
-    }
     static const int kGroupFirst[12] = {0, 1, 5, 9, 13, 17, 19, 21, 29, 32, 37, 59};
     for (int g = 0; g < 11; g++) {
         double lo[3] = {1e9, 1e9, 1e9}, hi[3] = {-1e9, -1e9, -1e9};

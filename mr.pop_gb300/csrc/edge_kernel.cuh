@@ -126,7 +126,6 @@ struct EdgeParams {
     unsigned long long *phase;  // phase timers (MRPOP_PHASE_TIMERS builds only)
     uint64_t *sflags;           // split pipeline: per-sample {env, self} flag words
     uint64_t *smasks;           // split pipeline: per-edge {env, self} candidate masks
-    float group_r[kNumJoints];  // bounding radius of each joint's detailed spheres (+margin)
     float4 grp[11];             // detailed sub-group bounds in their joint frame (+margin)
     const uint32_t *row5;       // forearm-hand rows table (kRow5N6 x kRow5N7 bits), or nullptr
     float base[kMaxArms][12];   // row-major 3x4 per arm of this check
@@ -145,7 +144,7 @@ struct WarpScratch {
             float low[kNumApprox][3][32];   // per-lane approx spheres of a lower arm
         } broad;
         struct {
-            float4 dbound[kMaxArms][32];    // per-lane bound of each arm's detailed spheres
+            float4 gsw[kMaxArms][11];       // swept bound of each detailed sub-group over the warp's samples
             union {
                 float stash[kDetRows][3][32];        // first sphere of each detailed self row
                 float cstash[kCrossStash][4][32];    // arm-vs-arm candidates {x, y, z, r}
@@ -269,18 +268,19 @@ __device__ __forceinline__ float sample_q1(const WarpScratch &W, int rule, int s
     return v;
 }
 
-// Order-preserving map of a float onto an unsigned key, so that warp-wide
-// min/max of floats can use redux.sync on integers; key_float inverts it.
-__device__ __forceinline__ uint32_t order_key(float f) {
-    const uint32_t u = __float_as_uint(f);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+// Warp-wide float min / max (redux.sync on f32, sm_100a family).  NaN inputs
+// are ignored; a lane with a NaN position can never pass an exact test, so the
+// bounds built from these stay conservative.
+__device__ __forceinline__ float warp_min(float v) {
+    float r;
+    asm volatile("redux.sync.min.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(v));
+    return r;
 }
-__device__ __forceinline__ float key_float(uint32_t k) {
-    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+__device__ __forceinline__ float warp_max(float v) {
+    float r;
+    asm volatile("redux.sync.max.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(v));
+    return r;
 }
-
-__device__ __forceinline__ float warp_min(float v) { return key_float(__reduce_min_sync(kFull, order_key(v))); }
-__device__ __forceinline__ float warp_max(float v) { return key_float(__reduce_max_sync(kFull, order_key(v))); }
 
 // FK of one arm for this lane's sample; the 11 approx centres go to column
 // `lane` of dst.  With swept != nullptr it also writes, for every approx
@@ -799,12 +799,13 @@ __device__ __forceinline__ void lane_rows(int j, const EdgeParams &P, const Xf &
 // arm's chain is rebuilt in registers; env tests of env-flagged joints
 // (screened warp-wide per sub-group) and the intra-arm rows of self-flagged
 // joints run as the frames stream by (the first sphere of each row is stashed
-// until its targets come).  Writes each arm's detailed bound for the
-// arm-vs-arm part.  Returns true if a test fired.
+// until its targets come).  With track set it also writes the swept bound of
+// every sub-group over the warp's samples (W.lanes.gsw) for the arm-vs-arm
+// part.  Returns true if a test fired.
 template <int A>
 static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch &W, const float4 *S,
                                                 const SceneLayout &L, const float4 *det_tab, int seg, int k,
-                                                uint64_t envw, uint64_t selfw, bool de, bool ds, float max_group_r) {
+                                                uint64_t envw, uint64_t selfw, bool de, bool ds, bool track) {
     const int lane = threadIdx.x & 31;
     LaneCtx c;
     c.quirk = (!P.single && !(P.flags & kExactBit)) ? 1 : 0;
@@ -822,79 +823,67 @@ static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch
             c.rm &= ~row5_rows(c.quirk);
         Xf T;
         load_base(T, P.base[a]);
-        float lx = T.m[3], hx = T.m[3], ly = T.m[7], hy = T.m[7], lz = T.m[11], hz = T.m[11];
 #pragma unroll 1
         for (int j = 0; j < kNumJoints; j++) {
             if (j > 0) joint_step_rt(T, sample_q1(W, P.rule, seg, qa + j - 1, k), j);
-            lx = fminf(lx, T.m[3]);
-            hx = fmaxf(hx, T.m[3]);
-            ly = fminf(ly, T.m[7]);
-            hy = fmaxf(hy, T.m[7]);
-            lz = fminf(lz, T.m[11]);
-            hz = fmaxf(hz, T.m[11]);
+            if (track) {
+                // swept bound of each sub-group of this joint over the warp's samples
+#pragma unroll 1
+                for (int g = jgrp_first(j); g < jgrp_first(j + 1); g++) {
+                    const float4 gl = P.grp[g];
+                    const float3 gc = place_reg(T, gl);
+                    const float gx = warp_min(gc.x), hx2 = warp_max(gc.x);
+                    const float gy = warp_min(gc.y), hy2 = warp_max(gc.y);
+                    const float gz = warp_min(gc.z), hz2 = warp_max(gc.z);
+                    if (lane == 0) {
+                        const float dx = hx2 - gx, dy = hy2 - gy, dz = hz2 - gz;
+                        W.lanes.gsw[a][g] = make_float4(0.5f * (gx + hx2), 0.5f * (gy + hy2), 0.5f * (gz + hz2),
+                                                        0.5f * sqrtf(dx * dx + dy * dy + dz * dz) * 1.004f + gl.w);
+                    }
+                }
+            }
             MRPOP_PHASE(P, 8);
             lane_env(j, P, T, c, S, L);
             MRPOP_PHASE(P, 9);
             lane_rows(j, P, T, c, W, det_tab, lane);
             MRPOP_PHASE(P, 10);
         }
-        // bound of every joint origin (half-diagonal of their box) plus the
-        // largest sub-group radius about a joint origin
-        const float cx = 0.5f * (lx + hx), cy = 0.5f * (ly + hy), cz = 0.5f * (lz + hz);
-        const float dx = hx - lx, dy = hy - ly, dz = hz - lz;
-        const float r2 = 0.25f * (dx * dx + dy * dy + dz * dz);
-        W.lanes.dbound[a][lane] = make_float4(cx, cy, cz, sqrtf(r2) * 1.0001f + max_group_r);
     }
     return c.hit;
 }
 
-// Pairs (a, b), a < b, whose arm-vs-arm detailed test this lane's sample
-// needs: arm a has self flags and the two arms' detailed bounds meet.
-// Bit index of pair (a, b) is a * kMaxArms + b.
-template <int A>
-__device__ __forceinline__ uint32_t cross_pairs(const WarpScratch &W, uint64_t selfw, bool ds) {
-    const int lane = threadIdx.x & 31;
-    uint32_t pm = 0;
-    if (!ds) return 0;
-#pragma unroll
-    for (int a = 0; a < A - 1; a++) {
-        if (!((selfw >> (8 * a)) & 0xffull)) continue;
-        const float4 ba = W.lanes.dbound[a][lane];
-#pragma unroll
-        for (int b = a + 1; b < A; b++)
-            if (near3(ba.x, ba.y, ba.z, W.lanes.dbound[b][lane], ba.w)) pm |= 1u << (a * kMaxArms + b);
-    }
-    return pm;
-}
-
 // Arm a, joint j: stash the flagged spheres (index >= from) that can reach
 // bound bb, until the stash is full; `next` receives the first sphere left out.
-__device__ __forceinline__ void stash_joint(int j, const Xf &T, uint32_t sma, float4 bb, int from, int &n, int &next,
-                                            WarpScratch &W, int lane) {
+__device__ __forceinline__ void stash_joint(int j, const Xf &T, uint32_t sma, uint32_t qa, int from, int &n,
+                                            int &next, WarpScratch &W, int lane) {
     if (next >= 0 || !(sma >> j & 1u) || det_first(j + 1) <= from) return;
 #pragma unroll 1
-    for (int i = max(det_first(j), from); i < det_first(j + 1); i++) {
-        const float4 sd = c_det[i];
-        const float3 p = place_reg(T, sd);
-        if (!near3(p.x, p.y, p.z, bb, sd.w)) continue;
-        if (n == kCrossStash) {
-            next = i;
-            return;
+    for (int g = jgrp_first(j); g < jgrp_first(j + 1); g++) {
+        if (!(qa >> g & 1u) || grp_first(g + 1) <= from) continue;
+#pragma unroll 1
+        for (int i = max(grp_first(g), from); i < grp_first(g + 1); i++) {
+            const float4 sd = c_det[i];
+            const float3 p = place_reg(T, sd);
+            if (n == kCrossStash) {
+                next = i;
+                return;
+            }
+            W.lanes.cstash[n][0][lane] = p.x;
+            W.lanes.cstash[n][1][lane] = p.y;
+            W.lanes.cstash[n][2][lane] = p.z;
+            W.lanes.cstash[n][3][lane] = sd.w;
+            n++;
         }
-        W.lanes.cstash[n][0][lane] = p.x;
-        W.lanes.cstash[n][1][lane] = p.y;
-        W.lanes.cstash[n][2][lane] = p.z;
-        W.lanes.cstash[n][3][lane] = sd.w;
-        n++;
     }
 }
 
 // Arm b, joint j: its spheres against the stashed spheres, by sub-group.
-__device__ __forceinline__ void probe_joint(int j, const EdgeParams &P, const Xf &T, int n, bool &hit,
+__device__ __forceinline__ void probe_joint(int j, const EdgeParams &P, const Xf &T, uint32_t qb, int n, bool &hit,
                                             WarpScratch &W, int lane) {
     if (hit) return;
 #pragma unroll 1
     for (int g = jgrp_first(j); g < jgrp_first(j + 1); g++) {
+        if (!(qb >> g & 1u)) continue;
         const float4 gl = P.grp[g];
         const float3 gc = place_reg(T, gl);
         const float4 gb = make_float4(gc.x, gc.y, gc.z, gl.w);
@@ -924,24 +913,49 @@ __device__ __forceinline__ void probe_joint(int j, const EdgeParams &P, const Xf
     }
 }
 
-// Lane-parallel arm-vs-arm detailed test of this lane's sample for the pairs
-// in pm (every lane of the warp calls it): arm a's flagged spheres that can
-// reach arm b's bound are stashed (in chunks of kCrossStash) and arm b's
-// spheres are streamed against them.  Returns true if a test fired.
+// Joint of detailed sub-group g.
+__device__ __forceinline__ constexpr int grp_joint(int g) { return g < 5 ? g : g < 8 ? 5 : g < 9 ? 6 : 7; }
+
+// Arm-vs-arm detailed test (panda_four.cuh:415-453) of this lane's sample;
+// every lane of the warp calls it, lanes with act set take part.  For each arm
+// pair (a, b) the 121 sub-group pairs are screened warp-wide, one per lane,
+// with the swept sub-group bounds of the warp's samples (W.lanes.gsw; groups
+// of a restricted to joints some active lane has self-flagged).  Pairs with no
+// surviving group pair are skipped by the whole warp.  Otherwise each active
+// lane stashes arm a's flagged spheres of the surviving groups that can reach
+// arm b's bound (chunks of kCrossStash) and streams arm b's surviving groups
+// against them.  Returns true if a test fired.
 template <int A>
-static __device__ __noinline__ bool cross_lane(const EdgeParams &P, WarpScratch &W, int seg, int k, uint64_t selfw,
-                                               uint32_t pm) {
+static __device__ __noinline__ bool cross_swept(const EdgeParams &P, WarpScratch &W, int seg, int k, uint64_t selfw,
+                                                bool act) {
     const int lane = threadIdx.x & 31;
     bool hit = false;
 #pragma unroll 1
     for (int a = 0; a < A - 1; a++) {
-        const uint32_t sma = (uint32_t)(selfw >> (8 * a)) & 0xffu;
+        const uint32_t sma = act ? (uint32_t)(selfw >> (8 * a)) & 0xffu : 0u;
+        const uint32_t uj = __reduce_or_sync(kFull, sma);
+        if (!uj) continue;
 #pragma unroll 1
         for (int b = a + 1; b < A; b++) {
-            const bool need = (pm >> (a * kMaxArms + b) & 1u) && !hit;
-            if (!__any_sync(kFull, need)) continue;
-            if (!need) continue;
-            const float4 bb = W.lanes.dbound[b][lane];
+            uint32_t qa = 0, qb = 0;
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                const int t = 32 * r + lane;
+                const int ga = t / kNumGroups, gb = t - kNumGroups * ga;
+                bool pass = false;
+                if (t < kNumGroups * kNumGroups && (uj >> grp_joint(ga) & 1u)) {
+                    const float4 u = W.lanes.gsw[a][ga];
+                    pass = near3(u.x, u.y, u.z, W.lanes.gsw[b][gb], u.w);
+                }
+                uint32_t bal = __ballot_sync(kFull, pass);
+                while (bal) {
+                    const int tt = 32 * r + __ffs(bal) - 1;
+                    bal &= bal - 1;
+                    qa |= 1u << (tt / kNumGroups);
+                    qb |= 1u << (tt % kNumGroups);
+                }
+            }
+            if (!qa || !act || hit) continue;
             int from = 0;
             while (from >= 0 && !hit) {
                 int n = 0, next = -1;
@@ -951,7 +965,7 @@ static __device__ __noinline__ bool cross_lane(const EdgeParams &P, WarpScratch 
 #pragma unroll 1
                     for (int j = 0; j < kNumJoints; j++) {
                         if (j > 0) joint_step_rt(T, sample_q1(W, P.rule, seg, 7 * a + j - 1, k), j);
-                        stash_joint(j, T, sma, bb, from, n, next, W, lane);
+                        stash_joint(j, T, sma, qa, from, n, next, W, lane);
                     }
                 }
                 from = next;
@@ -961,7 +975,7 @@ static __device__ __noinline__ bool cross_lane(const EdgeParams &P, WarpScratch 
 #pragma unroll 1
                 for (int j = 0; j < kNumJoints; j++) {
                     if (j > 0) joint_step_rt(T, sample_q1(W, P.rule, seg, 7 * b + j - 1, k), j);
-                    probe_joint(j, P, T, n, hit, W, lane);
+                    probe_joint(j, P, T, qb, n, hit, W, lane);
                 }
             }
         }
@@ -1103,23 +1117,24 @@ template <int A, int SPL>
 __device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &W, const float4 *S,
                                               const SceneLayout &L, const float4 *det_tab, int seg, int lane,
                                               const uint64_t (&envw)[SPL], const uint64_t (&selfw)[SPL],
-                                              uint64_t cand_env, uint64_t cand_self, float max_group_r) {
+                                              uint64_t cand_env, uint64_t cand_self) {
     MRPOP_PHASE_START();
     uint64_t hits = 0;
 #pragma unroll
     for (int s = 0; s < SPL; s++) {
         const int bit = lane + 32 * s;
         const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
-        uint32_t pm = 0;
         // every lane walks the arms (warp-wide screening inside); lanes
-        // without a candidate sample only keep the others company
-        bool h = narrow_lane<A>(P, W, S, L, det_tab, seg, bit + 1, envw[s], selfw[s], dE, dS, max_group_r);
-        if ((dE || dS) && !h && A > 1) pm = cross_pairs<A>(W, selfw[s], dS);
+        // without a candidate sample keep the others company on sample
+        // min(k, g), so that the warp's swept bounds stay on real samples
+        const int k = bit + 1 <= P.g ? bit + 1 : P.g;
+        const bool track = A > 1 && __any_sync(kFull, dS);
+        bool h = narrow_lane<A>(P, W, S, L, det_tab, seg, k, envw[s], selfw[s], dE, dS, track);
         MRPOP_PHASE(P, 5);
         MRPOP_COUNT_LANES(14, dE || dS);
-        if (A > 1 && __any_sync(kFull, pm != 0u)) {
+        if (track && __any_sync(kFull, dS && !h)) {
             MRPOP_COUNT_W(15, 1);
-            h |= cross_lane<A>(P, W, seg, bit + 1, selfw[s], pm);
+            h |= cross_swept<A>(P, W, seg, k, selfw[s], dS && !h);
         }
         MRPOP_PHASE(P, 6);
         hits |= (uint64_t)__ballot_sync(kFull, h) << (32 * s);
@@ -1143,10 +1158,7 @@ __device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &
     MRPOP_PHASE_BIND(P);                                                                               \
     const int g = P.g;                                                                                 \
     const int dof = 7 * (P.single ? 1 : A);                                                            \
-    float max_group_r = 0.f;                                                                           \
-    for (int j = 0; j < kNumJoints; j++) max_group_r = fmaxf(max_group_r, P.group_r[j]);               \
     const long long nwarps = (long long)gridDim.x * kWarpsPerBlock;                                    \
-    (void)max_group_r;                                                                                 \
     (void)det_tab;
 
 // ---------------------------------------------------------------------------
@@ -1173,7 +1185,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
             uint64_t envw[SPL], selfw[SPL], cand_env, cand_self;
             if (broad_decide<A, SPL>(P, W, S, L, seg, g, lane, envw, selfw, cand_env, cand_self, tally)) {
                 const int fb = narrow_segment<A, SPL>(P, W, S, L, det_tab, seg, lane, envw, selfw, cand_env,
-                                                      cand_self, max_group_r);
+                                                      cand_self);
                 if (fb < 64) first = seg * g + fb + 1;
             }
             if (P.rule == kRuleConnect) {
@@ -1262,7 +1274,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
             selfw[s] = P.sflags[o + 1];
         }
         const int fb =
-            narrow_segment<A, SPL>(P, W, S, L, det_tab, 0, lane, envw, selfw, cand_env, cand_self, max_group_r);
+            narrow_segment<A, SPL>(P, W, S, L, det_tab, 0, lane, envw, selfw, cand_env, cand_self);
         if (lane == 0) {
             P.valid[e] = fb < 64 ? 0 : 1;
             P.first_hit[e] = fb < 64 ? fb + 1 : -1;
