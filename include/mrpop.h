@@ -149,7 +149,7 @@ mrpop_status mrpop_validate_segments(const mrpop_scene *scene, const mrpop_robot
  * it, or a planner loop that may not enter the allocator.  No counterpart in the
  * reference (its planner keeps all scratch in fixed __device__ arrays).
  *   - Calls no allocation routine.  Its scratch is one fixed array in the
- *     library's device memory, about 16.3 MiB per device
+ *     library's device memory, about 27.5 MiB per device
  *     (MRPOP_NOALLOC_MAX_EDGES edges at granularity 64), held by every GPU that
  *     loads the library until the process exits.
  *   - n_edges above MRPOP_NOALLOC_MAX_EDGES is rejected (MRPOP_ERR_INVALID_ARGUMENT).

@@ -392,7 +392,7 @@ namespace {
 namespace mrpop {
 
 // ext_scratch: caller-provided device scratch for the single-segment pipeline
-// (at least n_edges * (32 * samples-per-lane + 1) * 16 bytes); nullptr = the
+// (at least n_edges * ((32 * samples-per-lane + 1) * 16 + arms * 144) bytes); nullptr = the
 // library's stream-ordered pool.
 mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
                            const float *q1, int64_t n_edges, int g, int rule, float range, uint32_t flags,
@@ -452,6 +452,9 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
             r = std::fmax(r, std::sqrt((d.x - cx) * (d.x - cx) + (d.y - cy) * (d.y - cy) + (d.z - cz) * (d.z - cz)) + d.r);
         }
         p.grp[g] = make_float4((float)cx, (float)cy, (float)cz, (float)(r * 1.001 + mrpop::kCullMargin));
+        const mrpop::SphereDef &ref = mrpop::kApprox[mrpop::grp_ref(g)];
+        const double ox = cx - ref.x, oy = cy - ref.y, oz = cz - ref.z;
+        p.gofs[g] = (float)(std::sqrt(ox * ox + oy * oy + oz * oz) * 1.001 + r * 1.001 + mrpop::kCullMargin);
     }
     const int A = arm >= 0 ? 1 : robots->n_arms;
     for (int a = 0; a < A; a++)
@@ -474,17 +477,20 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
         const int spl = g > 32 ? 2 : 1;
         const size_t flag_bytes = (size_t)n_edges * 32 * spl * 2 * sizeof(uint64_t);
         const size_t mask_bytes = (size_t)n_edges * 2 * sizeof(uint64_t);
+        const size_t bound_bytes = (size_t)n_edges * A * mrpop::kRefSpheres * sizeof(float4);
         void *scratch = ext_scratch;
         if (!scratch) {
             cudaMemPool_t pool;
             err = scratch_pool(&pool);
-            if (err == cudaSuccess) err = cudaMallocFromPoolAsync(&scratch, flag_bytes + mask_bytes, pool, stream);
+            if (err == cudaSuccess)
+                err = cudaMallocFromPoolAsync(&scratch, flag_bytes + mask_bytes + bound_bytes, pool, stream);
         } else {
             err = cudaSuccess;
         }
         if (err == cudaSuccess) {
             p.sflags = (uint64_t *)scratch;
             p.smasks = (uint64_t *)((char *)scratch + flag_bytes);
+            p.sbounds = (float4 *)((char *)scratch + flag_bytes + mask_bytes);
             err = timed_launch(A, mrpop::kBroad, p, smem, stream);
             if (err == cudaSuccess) err = timed_launch(A, mrpop::kNarrow, p, smem, stream);
             if (!ext_scratch) cudaFreeAsync(scratch, stream);

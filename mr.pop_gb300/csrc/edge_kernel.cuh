@@ -105,6 +105,10 @@ __host__ __device__ inline SceneLayout scene_layout(const SceneCounts &c) {
     return l;
 }
 
+// Approx spheres whose swept bounds the narrow phase reuses: 0..8 (the
+// reference sphere of every detailed sub-group, see grp_ref).
+constexpr int kRefSpheres = 9;
+
 struct EdgeParams {
     const float *q0;
     const float *q1;
@@ -126,6 +130,8 @@ struct EdgeParams {
     unsigned long long *phase;  // phase timers (MRPOP_PHASE_TIMERS builds only)
     uint64_t *sflags;           // split pipeline: per-sample {env, self} flag words
     uint64_t *smasks;           // split pipeline: per-edge {env, self} candidate masks
+    float4 *sbounds;            // split pipeline: per-edge swept reference-sphere bounds [A][kRefSpheres]
+    float gofs[11];             // sub-group g: |group centre - reference sphere centre| + group radius
     float4 grp[11];             // detailed sub-group bounds in their joint frame (+margin)
     const uint32_t *row5;       // forearm-hand rows table (kRow5N6 x kRow5N7 bits), or nullptr
     float base[kMaxArms][12];   // row-major 3x4 per arm of this check
@@ -137,6 +143,10 @@ struct WarpScratch {
     float base[kMaxDof];   // segment start (accumulated for CONNECT)
     float stepg[kMaxDof];  // per-sample step (delta/g or vec/g)
     float delta[kMaxDof];  // per-segment step (B-spline / shortcut accumulation)
+    // bound of the centres of approx spheres 0..kRefSpheres-1 of each arm over
+    // every sample of the segment ({centre, radius}, sphere radius excluded);
+    // written by the broad phase, read by the narrow phase's arm-vs-arm screen
+    float4 rsw[kMaxArms][kRefSpheres];
     union {
         struct {
             float4 swept[kMaxArms][kNumApprox]; // per-arm swept bound of each approx sphere
@@ -144,7 +154,6 @@ struct WarpScratch {
             float low[kNumApprox][3][32];   // per-lane approx spheres of a lower arm
         } broad;
         struct {
-            float4 gsw[kMaxArms][11];       // swept bound of each detailed sub-group over the warp's samples
             union {
                 float stash[kDetRows][3][32];        // first sphere of each detailed self row
                 float cstash[kCrossStash][4][32];    // arm-vs-arm candidates {x, y, z, r}
@@ -289,7 +298,8 @@ __device__ __forceinline__ float warp_max(float v) {
 // sphere radius + cull margin.  If the sphere touches something at any of the
 // samples, its swept bound touches it too (the margin covers FP rounding).
 static __device__ __noinline__ void fk_approx_lane(const float *base12, const WarpScratch &W, int rule, int seg,
-                                                   int qarm, int k, float (*dst)[3][32], int lane, float4 *swept) {
+                                                   int qarm, int k, float (*dst)[3][32], int lane, float4 *swept,
+                                                   float4 *rsw, bool merge) {
     float q[7];
     sample_q(W, rule, seg, qarm, k, q);
     ArmSpheres s;
@@ -310,6 +320,22 @@ static __device__ __noinline__ void fk_approx_lane(const float *base12, const Wa
             const float dx = hx - lx, dy = hy - ly, dz = hz - lz;
             swept[i] = make_float4(0.5f * (lx + hx), 0.5f * (ly + hy), 0.5f * (lz + hz),
                                    0.5f * sqrtf(dx * dx + dy * dy + dz * dz) * 1.004f + c_approx[i].w + kCullMargin);
+        }
+    }
+    __syncwarp();
+    // bounds of the reference spheres' centres for the narrow phase (sphere
+    // radius and margin taken off again, +1e-6 m for the rounding), grown
+    // over the segment's earlier samples when merging
+    if (lane < kRefSpheres) {
+        const float4 sv = swept[lane];
+        const float hd = sv.w - c_approx[lane].w - kCullMargin + 1e-6f;
+        if (!merge) {
+            rsw[lane] = make_float4(sv.x, sv.y, sv.z, hd);
+        } else {
+            const float4 o = rsw[lane];
+            const float ex = sv.x - o.x, ey = sv.y - o.y, ez = sv.z - o.z;
+            const float d = sqrtf(ex * ex + ey * ey + ez * ez) * 1.0001f;
+            rsw[lane] = make_float4(o.x, o.y, o.z, fmaxf(o.w, d + hd) + 1e-6f);
         }
     }
     __syncwarp();
@@ -424,7 +450,8 @@ static __constant__ uint8_t c_intra_pairs[21][2] = {
 // segment's last sample evaluate sample g and discard the result).
 template <int A>
 __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W, const float4 *S,
-                                             const SceneLayout &L, int seg, int k, uint64_t &envw, uint64_t &selfw) {
+                                             const SceneLayout &L, int seg, int k, bool merge, uint64_t &envw,
+                                             uint64_t &selfw) {
     const int lane = threadIdx.x & 31;
     envw = 0;
     selfw = 0;
@@ -435,7 +462,7 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
     for (int b = 0; b < A; b++) {
         MRPOP_PHASE_START();
         float4 *sw = W.broad.swept[b];
-        fk_approx_lane(P.base[b], W, P.rule, seg, P.single ? 0 : b, k, cur, lane, sw);
+        fk_approx_lane(P.base[b], W, P.rule, seg, P.single ? 0 : b, k, cur, lane, sw, W.rsw[b], merge);
         MRPOP_PHASE(P, 0);
         if (do_env) {
             const uint32_t m = env_mask_approx(S, L, P.sc, cur, lane, sw);
@@ -485,7 +512,7 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
                                                   near3(swa[i].x, swa[i].y, swa[i].z, sw[j], swa[i].w));
             }
             if (!(bal[0] | bal[1] | bal[2] | bal[3])) continue;
-            fk_approx_lane(P.base[a], W, P.rule, seg, a, k, low, lane, nullptr);
+            fk_approx_lane(P.base[a], W, P.rule, seg, a, k, low, lane, nullptr, nullptr, false);
             uint32_t am = 0;
 #pragma unroll
             for (int r = 0; r < 4; r++) {
@@ -799,13 +826,11 @@ __device__ __forceinline__ void lane_rows(int j, const EdgeParams &P, const Xf &
 // arm's chain is rebuilt in registers; env tests of env-flagged joints
 // (screened warp-wide per sub-group) and the intra-arm rows of self-flagged
 // joints run as the frames stream by (the first sphere of each row is stashed
-// until its targets come).  With track set it also writes the swept bound of
-// every sub-group over the warp's samples (W.lanes.gsw) for the arm-vs-arm
-// part.  Returns true if a test fired.
+// until its targets come).  Returns true if a test fired.
 template <int A>
 static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch &W, const float4 *S,
                                                 const SceneLayout &L, const float4 *det_tab, int seg, int k,
-                                                uint64_t envw, uint64_t selfw, bool de, bool ds, bool track) {
+                                                uint64_t envw, uint64_t selfw, bool de, bool ds) {
     const int lane = threadIdx.x & 31;
     LaneCtx c;
     c.quirk = (!P.single && !(P.flags & kExactBit)) ? 1 : 0;
@@ -826,22 +851,6 @@ static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch
 #pragma unroll 1
         for (int j = 0; j < kNumJoints; j++) {
             if (j > 0) joint_step_rt(T, sample_q1(W, P.rule, seg, qa + j - 1, k), j);
-            if (track) {
-                // swept bound of each sub-group of this joint over the warp's samples
-#pragma unroll 1
-                for (int g = jgrp_first(j); g < jgrp_first(j + 1); g++) {
-                    const float4 gl = P.grp[g];
-                    const float3 gc = place_reg(T, gl);
-                    const float gx = warp_min(gc.x), hx2 = warp_max(gc.x);
-                    const float gy = warp_min(gc.y), hy2 = warp_max(gc.y);
-                    const float gz = warp_min(gc.z), hz2 = warp_max(gc.z);
-                    if (lane == 0) {
-                        const float dx = hx2 - gx, dy = hy2 - gy, dz = hz2 - gz;
-                        W.lanes.gsw[a][g] = make_float4(0.5f * (gx + hx2), 0.5f * (gy + hy2), 0.5f * (gz + hz2),
-                                                        0.5f * sqrtf(dx * dx + dy * dy + dz * dz) * 1.004f + gl.w);
-                    }
-                }
-            }
             MRPOP_PHASE(P, 8);
             lane_env(j, P, T, c, S, L);
             MRPOP_PHASE(P, 9);
@@ -915,12 +924,19 @@ __device__ __forceinline__ void probe_joint(int j, const EdgeParams &P, const Xf
 
 // Joint of detailed sub-group g.
 __device__ __forceinline__ constexpr int grp_joint(int g) { return g < 5 ? g : g < 8 ? 5 : g < 9 ? 6 : 7; }
+// Reference approx sphere of sub-group g: an approx sphere on the same joint
+// (the nearest one for the hand), so that the group's centre is at a fixed
+// distance from it (EdgeParams::gofs adds that distance and the group radius).
+__host__ __device__ __forceinline__ constexpr int grp_ref(int g) {
+    return g < 5 ? g : g < 8 ? 5 : g < 9 ? 6 : g < 10 ? 7 : 8;
+}
 
 // Arm-vs-arm detailed test (panda_four.cuh:415-453) of this lane's sample;
 // every lane of the warp calls it, lanes with act set take part.  For each arm
 // pair (a, b) the 121 sub-group pairs are screened warp-wide, one per lane,
-// with the swept sub-group bounds of the warp's samples (W.lanes.gsw; groups
-// of a restricted to joints some active lane has self-flagged).  Pairs with no
+// with bounds over the segment's samples (the swept bound of the group's
+// reference approx sphere, W.rsw, grown by EdgeParams::gofs; groups of a
+// restricted to joints some active lane has self-flagged).  Pairs with no
 // surviving group pair are skipped by the whole warp.  Otherwise each active
 // lane stashes arm a's flagged spheres of the surviving groups that can reach
 // arm b's bound (chunks of kCrossStash) and streams arm b's surviving groups
@@ -944,8 +960,8 @@ static __device__ __noinline__ bool cross_swept(const EdgeParams &P, WarpScratch
                 const int ga = t / kNumGroups, gb = t - kNumGroups * ga;
                 bool pass = false;
                 if (t < kNumGroups * kNumGroups && (uj >> grp_joint(ga) & 1u)) {
-                    const float4 u = W.lanes.gsw[a][ga];
-                    pass = near3(u.x, u.y, u.z, W.lanes.gsw[b][gb], u.w);
+                    const float4 u = W.rsw[a][grp_ref(ga)], v = W.rsw[b][grp_ref(gb)];
+                    pass = near3(u.x, u.y, u.z, make_float4(v.x, v.y, v.z, v.w + P.gofs[gb]), u.w + P.gofs[ga]);
                 }
                 uint32_t bal = __ballot_sync(kFull, pass);
                 while (bal) {
@@ -1042,7 +1058,7 @@ __device__ __forceinline__ bool broad_decide(const EdgeParams &P, WarpScratch &W
 #pragma unroll
     for (int s = 0; s < SPL; s++) {
         const int k = lane + 1 + 32 * s;
-        broad_sample<A>(P, W, S, L, seg, k <= g ? k : g, envw[s], selfw[s]);
+        broad_sample<A>(P, W, S, L, seg, k <= g ? k : g, s > 0, envw[s], selfw[s]);
         if (k > g) envw[s] = selfw[s] = 0;
         envc[s] = flag_count(envw[s]);
         selfc[s] = flag_count(selfw[s]);
@@ -1126,13 +1142,12 @@ __device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &
         const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
         // every lane walks the arms (warp-wide screening inside); lanes
         // without a candidate sample keep the others company on sample
-        // min(k, g), so that the warp's swept bounds stay on real samples
+        // min(k, g), so that the warp's merged bounds stay on real samples
         const int k = bit + 1 <= P.g ? bit + 1 : P.g;
-        const bool track = A > 1 && __any_sync(kFull, dS);
-        bool h = narrow_lane<A>(P, W, S, L, det_tab, seg, k, envw[s], selfw[s], dE, dS, track);
+        bool h = narrow_lane<A>(P, W, S, L, det_tab, seg, k, envw[s], selfw[s], dE, dS);
         MRPOP_PHASE(P, 5);
         MRPOP_COUNT_LANES(14, dE || dS);
-        if (track && __any_sync(kFull, dS && !h)) {
+        if (A > 1 && __any_sync(kFull, dS && !h)) {
             MRPOP_COUNT_W(15, 1);
             h |= cross_swept<A>(P, W, seg, k, selfw[s], dS && !h);
         }
@@ -1235,6 +1250,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
                 P.sflags[o] = envw[s];
                 P.sflags[o + 1] = selfw[s];
             }
+            for (int t = lane; t < A * kRefSpheres; t += 32) P.sbounds[e * (A * kRefSpheres) + t] = (&W.rsw[0][0])[t];
         }
         if (lane == 0) {
             P.smasks[2 * e] = cand_env;
@@ -1273,6 +1289,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
             envw[s] = P.sflags[o];
             selfw[s] = P.sflags[o + 1];
         }
+        for (int t = lane; t < A * kRefSpheres; t += 32) (&W.rsw[0][0])[t] = P.sbounds[e * (A * kRefSpheres) + t];
+        __syncwarp();
         const int fb =
             narrow_segment<A, SPL>(P, W, S, L, det_tab, 0, lane, envw, selfw, cand_env, cand_self);
         if (lane == 0) {
