@@ -311,14 +311,35 @@ static __device__ __noinline__ void fk_approx_lane(const float *base12, const Wa
         dst[i][2][lane] = s.z[i];
     }
     if (!swept) return;
-#pragma unroll
-    for (int i = 0; i < kNumApprox; i++) {
-        const float lx = warp_min(s.x[i]), hx = warp_max(s.x[i]);
-        const float ly = warp_min(s.y[i]), hy = warp_max(s.y[i]);
-        const float lz = warp_min(s.z[i]), hz = warp_max(s.z[i]);
-        if (lane == 0) {
-            const float dx = hx - lx, dy = hy - ly, dz = hz - lz;
-            swept[i] = make_float4(0.5f * (lx + hx), 0.5f * (ly + hy), 0.5f * (lz + hz),
+    __syncwarp();
+    {
+        // spheres 1..10: lane t < 30 takes coordinate t % 3 of sphere 1 + t / 3
+        // over the 32 columns (start skewed by lane: conflict-free banks);
+        // sphere 0 (the base frame's) by warp reductions
+        float lo = 0.0f, hi = 0.0f;
+        if (lane < 30) {
+            const float *col = &dst[1 + lane / 3][lane % 3][0];
+            lo = hi = col[lane];
+#pragma unroll 8
+            for (int l = 1; l < 32; l++) {
+                const float v = col[(l + lane) & 31];
+                lo = fminf(lo, v);
+                hi = fmaxf(hi, v);
+            }
+        }
+        const float ly = __shfl_down_sync(kFull, lo, 1), hy = __shfl_down_sync(kFull, hi, 1);
+        const float lz = __shfl_down_sync(kFull, lo, 2), hz = __shfl_down_sync(kFull, hi, 2);
+        const float l0x = warp_min(s.x[0]), h0x = warp_max(s.x[0]);
+        const float l0y = warp_min(s.y[0]), h0y = warp_max(s.y[0]);
+        const float l0z = warp_min(s.z[0]), h0z = warp_max(s.z[0]);
+        const bool own = lane < 30 && lane % 3 == 0;
+        const int i = own ? 1 + lane / 3 : 0;
+        if (own || lane == 30) {
+            const float ax = own ? lo : l0x, bx = own ? hi : h0x;
+            const float ay = own ? ly : l0y, by = own ? hy : h0y;
+            const float az = own ? lz : l0z, bz = own ? hz : h0z;
+            const float dx = bx - ax, dy = by - ay, dz = bz - az;
+            swept[i] = make_float4(0.5f * (ax + bx), 0.5f * (ay + by), 0.5f * (az + bz),
                                    0.5f * sqrtf(dx * dx + dy * dy + dz * dz) * 1.004f + c_approx[i].w + kCullMargin);
         }
     }
