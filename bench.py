@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
-    ap.add_argument("--workload", choices=["config1", "config2", "config3"], default="config2")
+    ap.add_argument("--workload", choices=["config1", "config2", "config3", "config4"], default="config2")
+    ap.add_argument("--instances", type=int, default=512, help="config4: planning instances in the batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -228,6 +229,111 @@ def roofline(kt: dict, flops: dict, peak: float, workload: str, arms: int, spl: 
     return out
 
 
+def run_batch(args, world, rank, local, pkg, torch):
+    """Config 4: an uneven batch of planning instances (1-5 arms, lognormal
+    edge counts, g in {16, 32, 64}, config-1/2 scenes) through one captured
+    CUDA graph of the batch kernels (mrpop_batch_*), tuned launch shapes."""
+    W = pkg.workloads
+    insts = W.config4_instances(n_instances=args.instances, seed=rank)
+    sizes = [wl.q0.size for wl in insts]
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    n_edges = np.array([len(wl.q0) for wl in insts])
+    eoffs = np.concatenate([[0], np.cumsum(n_edges)])
+    # one flat buffer per input and output; instances are views into them
+    h0 = torch.empty(int(offs[-1]), dtype=torch.float32).pin_memory()
+    h1 = torch.empty(int(offs[-1]), dtype=torch.float32).pin_memory()
+    for i, wl in enumerate(insts):
+        h0[offs[i]:offs[i + 1]] = torch.from_numpy(wl.q0.ravel())
+        h1[offs[i]:offs[i + 1]] = torch.from_numpy(wl.q1.ravel())
+    d0, d1 = h0.cuda(), h1.cuda()
+    dv = torch.empty(int(eoffs[-1]), dtype=torch.uint8, device="cuda")
+    df = torch.empty(int(eoffs[-1]), dtype=torch.int32, device="cuda")
+    hv = torch.empty(int(eoffs[-1]), dtype=torch.uint8).pin_memory()
+    hf = torch.empty(int(eoffs[-1]), dtype=torch.int32).pin_memory()
+    items = []
+    for i, wl in enumerate(insts):
+        dof = wl.q0.shape[1]
+        q0 = d0[offs[i]:offs[i + 1]].view(-1, dof)
+        q1 = d1[offs[i]:offs[i + 1]].view(-1, dof)
+        items.append((pkg.Scene(wl.scene), pkg.RobotSet(len(wl.bases), wl.bases), q0, q1, wl.granularity, wl.flags,
+                      wl.arm, dv[eoffs[i]:eoffs[i + 1]], df[eoffs[i]:eoffs[i + 1]]))
+    samples = int(sum(len(wl.q0) * wl.granularity for wl in insts))
+    batch = pkg.Batch(items)
+    batch.run()
+    batch.tune()
+    batch.capture()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        flush.zero_()
+        batch.launch()
+    torch.cuda.synchronize()
+    ref_v = dv.clone()
+    # per-instance plain calls on the same buffers: the results must be equal
+    for it in items:
+        pkg.validate(*it[:7], valid=it[7], first_hit=it[8])
+    torch.cuda.synchronize()
+    assert torch.equal(ref_v, dv), "batch and per-instance results differ"
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    pkg.kernel_times()
+    barrier(world)
+    torch.cuda.synchronize()
+    for s_, e_ in ev:
+        flush.zero_()
+        s_.record(stream)
+        batch.launch()
+        e_.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    t_total = max_over_ranks(sum(s_.elapsed_time(e_) for s_, e_ in ev) / 1e3, world)
+    value = world * samples * args.steps / t_total
+    # the same work as one plain call per instance (no graph, no batching)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        for it in items:
+            pkg.validate(*it[:7], valid=it[7], first_hit=it[8])
+    torch.cuda.synchronize()
+    loop_value = samples * max(1, args.steps // 2) / (time.perf_counter() - t)
+    # end to end: host inputs in, verdicts out, every step
+    barrier(world)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        d0.copy_(h0, non_blocking=True)
+        d1.copy_(h1, non_blocking=True)
+        batch.launch()
+        hv.copy_(dv, non_blocking=True)
+        hf.copy_(df, non_blocking=True)
+        torch.cuda.synchronize()
+    dt = max_over_ranks(time.perf_counter() - t, world)
+    groups = batch.info()
+    arms_hist = np.bincount([len(wl.bases) if wl.arm < 0 else 1 for wl in insts], minlength=6)[1:].tolist()
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
+        "config": {"workload": f"config4_uneven_batch_{len(insts)}_instances", "instances": len(insts),
+                   "edges": int(eoffs[-1]), "samples": samples, "arms_histogram_1_to_5": arms_hist,
+                   "granularities": sorted({wl.granularity for wl in insts}),
+                   "kernel_groups": [{"arms": a, "samples_per_lane": s, "broad_grid": gb, "narrow_grid": gn}
+                                     for a, s, gb, gn in groups],
+                   "launch": "one CUDA graph of the batch kernels (tuned grids)",
+                   "per_instance_plain_calls_value": loop_value,
+                   "l2": "flushed (256 MiB write) before every step",
+                   "parallelism": f"replica x{world}, independent batches"},
+        "gpu_launches": 2 * len(groups) * args.steps,
+        "clocks": clk,
+        "e2e": {"value": world * samples * args.steps / dt, "unit": UNIT,
+                "h2d_bytes_per_step": int(h0.numel() * 4 * 2), "d2h_bytes_per_step": int(hv.numel() * 5),
+                "path": "pinned host buffers -> device, mrpop_batch_launch, verdicts -> host, synchronised per step"},
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def run_mine(args, world, rank, local):
     import torch
     import __graft_entry__ as ge
@@ -236,6 +342,8 @@ def run_mine(args, world, rank, local):
     if not lib.exists():
         pkg.build.build()
     pkg.library()
+    if args.workload == "config4":
+        return run_batch(args, world, rank, local, pkg, torch)
     wl = load_workload(pkg, args.workload)
     scene = pkg.Scene(wl.scene)
     robots = pkg.RobotSet(len(wl.bases), wl.bases)
@@ -317,6 +425,45 @@ def run_mine(args, world, rank, local):
         print(json.dumps(out), flush=True)
 
 
+def run_reference_batch(args, pkg, torch, ref_runner, out):
+    """Config 4 on the reference's kernels: one harness launch per instance
+    (the reference validates one planning instance at a time), over the 4- and
+    5-arm instances -- its composite kernels exist for those arm counts only,
+    and its single-arm form uses its own fixed bases."""
+    W = pkg.workloads
+    insts = [wl for wl in W.config4_instances(n_instances=args.instances, seed=0)
+             if len(wl.bases) in (4, 5) and wl.arm < 0]
+    R = ref_runner.RefHarness()
+    runs = []
+    for wl in insts:
+        runs.append((wl, R.make_env(wl.scene), torch.from_numpy(wl.q0).cuda(), torch.from_numpy(wl.q1).cuda()))
+    samples = sum(len(wl.q0) * wl.granularity for wl, *_ in runs)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+
+    def step():
+        for wl, env, q0, q1 in runs:
+            R.set_bases(len(wl.bases), wl.bases)
+            R.validate(env, q0, q1, wl.granularity, R.KIND_COMPOSITE, 0, 0.0, len(wl.bases), 0, blocks=sms * 8)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    value = samples * args.steps / dt
+    out.update({"value": value, "ms_per_step": dt / args.steps * 1e3, "gpu_launches": len(runs) * args.steps,
+                "config": {"workload": f"config4_uneven_batch_{args.instances}_instances",
+                           "subset": f"{len(runs)} instances with 4 or 5 arms", "samples": samples,
+                           "launch": f"one reference harness launch per instance, {sms * 8} blocks"},
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": None, "kind": "reference",
+                                 "sample": "the reference's own CUDA edge check per instance on this GB300"}})
+    out["e2e"] = {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(args, world, rank, local):
     if rank != 0:
         return
@@ -325,6 +472,15 @@ def run_reference(args, world, rank, local):
     pkg = ge.load_package()
     from oracle import oracle as orc
     from oracle import ref_runner
+    if args.workload == "config4":
+        out = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic (seeded generators)", "impl": "reference"}
+        if not ref_runner.available():
+            out["unavailable"] = "reference harness not built (oracle/_ref)"
+            print(json.dumps(out), flush=True)
+            return
+        return run_reference_batch(args, pkg, torch, ref_runner, out)
     wl = load_workload(pkg, args.workload)
     n = len(wl.q0)
     samples = n * wl.granularity

@@ -189,6 +189,49 @@ mrpop_status mrpop_validate_edges_host(mrpop_workspace *ws, const mrpop_scene *s
 mrpop_status mrpop_fk_spheres(const mrpop_robotset *robots, int arm, const float *q, int64_t n,
                               int detailed, float *out, void *stream);
 
+/*
+ * Batched validation of many independent planning instances (single-segment
+ * edges; no counterpart in the reference, whose planner validates one edge per
+ * 256-thread block).  Each item is one mrpop_validate_edges call: its scene,
+ * robot set, device endpoints [n_edges][7 * arms], granularity, check flags,
+ * arm selection and device outputs; the items may differ in all of them.
+ * Results equal the per-item calls bit for bit.
+ *
+ * mrpop_batch_create checks every item, allocates the device scratch and the
+ * per-group parameter tables (groups = arm count x (g <= 32 or not)), and
+ * keeps the item pointers: their buffers must outlive the batch.
+ * mrpop_batch_run launches one persistent broad-phase and one narrow-phase
+ * kernel per group on `stream`; it allocates nothing and reads the inputs as
+ * they are at execution time, so a batch can be rerun on refilled buffers.
+ * mrpop_batch_tune picks each launch's grid by timing (synchronous).
+ * mrpop_batch_capture records one run as a CUDA graph (each group on its own
+ * branch) and mrpop_batch_launch launches that graph on `stream`.
+ * mrpop_batch_info reports, per group, {arms, samples per lane, broad grid,
+ * narrow grid} into grids[4 * i ..] for up to max_groups groups.
+ */
+typedef struct mrpop_batch_item {
+    const mrpop_scene *scene;
+    const mrpop_robotset *robots;
+    const float *q0;
+    const float *q1;
+    int64_t n_edges;
+    int32_t granularity;
+    uint32_t flags;
+    int32_t arm;
+    uint8_t *valid;
+    int32_t *first_hit;
+} mrpop_batch_item;
+
+typedef struct mrpop_batch mrpop_batch;
+
+mrpop_status mrpop_batch_create(const mrpop_batch_item *items, int64_t n_items, mrpop_batch **out);
+mrpop_status mrpop_batch_run(mrpop_batch *batch, void *stream);
+mrpop_status mrpop_batch_tune(mrpop_batch *batch, void *stream);
+mrpop_status mrpop_batch_capture(mrpop_batch *batch);
+mrpop_status mrpop_batch_launch(mrpop_batch *batch, void *stream);
+mrpop_status mrpop_batch_info(const mrpop_batch *batch, int64_t *n_groups, int32_t *grids, int64_t max_groups);
+mrpop_status mrpop_batch_destroy(mrpop_batch *batch);
+
 /* Algorithmic flop count per edge (FMA = 2; the convention of the project's
  * roofline) for the same arguments as mrpop_validate_segments; writes
  * flops[e] (device, double).  Runs the validator with counting enabled. */

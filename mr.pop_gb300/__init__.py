@@ -6,7 +6,7 @@ and the seeded workload generators.
 """
 from . import build, mrpop, workloads  # noqa: F401
 from .mrpop import (CHECK_ENV, CHECK_SELF, MODE_EXACT, RULE_BSPLINE, RULE_CONNECT, RULE_PLAIN,  # noqa: F401
-                    RULE_SHORTCUT, MrpopError, RobotSet, Scene, SceneArrays, Workspace, broad_flops_per_sample,
+                    RULE_SHORTCUT, Batch, MrpopError, RobotSet, Scene, SceneArrays, Workspace, broad_flops_per_sample,
                     count_flops, debug_trig, fk_spheres, kernel_timing, kernel_times, library, validate)
 
 __version__ = "0.1.0"

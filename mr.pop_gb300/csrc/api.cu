@@ -391,17 +391,13 @@ namespace {
 
 namespace mrpop {
 
-// ext_scratch: caller-provided device scratch for the single-segment pipeline
-// (at least n_edges * ((32 * samples-per-lane + 1) * 16 + arms * 144) bytes); nullptr = the
-// library's stream-ordered pool.
-mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
-                           const float *q1, int64_t n_edges, int g, int rule, float range, uint32_t flags,
-                           int arm, uint8_t *valid, int32_t *first_hit, int32_t *n_seg_out, double *flops,
-                           cudaStream_t stream, void *ext_scratch) {
+mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0, const float *q1,
+                         int64_t n_edges, int g, int rule, float range, uint32_t flags, int arm, uint8_t *valid,
+                         int32_t *first_hit, int32_t *n_seg_out, double *flops, EdgeParams &p, int &A,
+                         size_t &smem) {
     if (!scene || !robots) return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: null scene or robots");
     if (n_edges < 0) return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: n_edges < 0");
-    if (n_edges == 0) return MRPOP_OK;
-    if (!q0 || !q1 || ((!valid || !first_hit) && !flops))
+    if (n_edges > 0 && (!q0 || !q1 || ((!valid || !first_hit) && !flops)))
         return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: null device pointer");
     if (g < 1 || g > MRPOP_MAX_GRANULARITY)
         return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: granularity must be 1..64");
@@ -416,7 +412,7 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
     cudaGetDevice(&dev);
     if (dev != scene->device) return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate: scene lives on another device");
 
-    mrpop::EdgeParams p{};
+    p = EdgeParams{};
     p.q0 = q0;
     p.q1 = q1;
     p.n_edges = n_edges;
@@ -436,10 +432,10 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
     p.env_test_flops = scene->env_test_flops;
     p.row5 = scene->row5;
     static const int kGroupFirst[12] = {0, 1, 5, 9, 13, 17, 19, 21, 29, 32, 37, 59};
-    for (int g = 0; g < 11; g++) {
+    for (int gi = 0; gi < 11; gi++) {
         double lo[3] = {1e9, 1e9, 1e9}, hi[3] = {-1e9, -1e9, -1e9};
-        for (int i = kGroupFirst[g]; i < kGroupFirst[g + 1]; i++) {
-            const double v[3] = {mrpop::kDet[i].x, mrpop::kDet[i].y, mrpop::kDet[i].z};
+        for (int i = kGroupFirst[gi]; i < kGroupFirst[gi + 1]; i++) {
+            const double v[3] = {kDet[i].x, kDet[i].y, kDet[i].z};
             for (int c = 0; c < 3; c++) {
                 lo[c] = std::fmin(lo[c], v[c]);
                 hi[c] = std::fmax(hi[c], v[c]);
@@ -447,19 +443,51 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
         }
         const double cx = 0.5 * (lo[0] + hi[0]), cy = 0.5 * (lo[1] + hi[1]), cz = 0.5 * (lo[2] + hi[2]);
         double r = 0.0;
-        for (int i = kGroupFirst[g]; i < kGroupFirst[g + 1]; i++) {
-            const mrpop::SphereDef &d = mrpop::kDet[i];
+        for (int i = kGroupFirst[gi]; i < kGroupFirst[gi + 1]; i++) {
+            const SphereDef &d = kDet[i];
             r = std::fmax(r, std::sqrt((d.x - cx) * (d.x - cx) + (d.y - cy) * (d.y - cy) + (d.z - cz) * (d.z - cz)) + d.r);
         }
-        p.grp[g] = make_float4((float)cx, (float)cy, (float)cz, (float)(r * 1.001 + mrpop::kCullMargin));
-        const mrpop::SphereDef &ref = mrpop::kApprox[mrpop::grp_ref(g)];
+        p.grp[gi] = make_float4((float)cx, (float)cy, (float)cz, (float)(r * 1.001 + kCullMargin));
+        const SphereDef &ref = kApprox[grp_ref(gi)];
         const double ox = cx - ref.x, oy = cy - ref.y, oz = cz - ref.z;
-        p.gofs[g] = (float)(std::sqrt(ox * ox + oy * oy + oz * oz) * 1.001 + r * 1.001 + mrpop::kCullMargin);
+        p.gofs[gi] = (float)(std::sqrt(ox * ox + oy * oy + oz * oz) * 1.001 + r * 1.001 + kCullMargin);
     }
-    const int A = arm >= 0 ? 1 : robots->n_arms;
+    A = arm >= 0 ? 1 : robots->n_arms;
     for (int a = 0; a < A; a++)
         for (int i = 0; i < 12; i++) p.base[a][i] = robots->base[arm >= 0 ? arm : a][i];
     p.fbp = broad_flops_per_sample(A, scene->env_test_flops, flags);
+    smem = (size_t)scene->total_f4 * sizeof(float4) + warp_scratch_bytes();
+    return MRPOP_OK;
+}
+
+size_t split_scratch_bytes(int64_t n_edges, int g, int A) {
+    const int spl = g > 32 ? 2 : 1;
+    return (size_t)n_edges * (32 * spl * 2 * sizeof(uint64_t) + 2 * sizeof(uint64_t) + A * kRefSpheres * sizeof(float4));
+}
+
+void set_split_scratch(EdgeParams &p, void *scratch, int64_t n_edges, int g, int A) {
+    const int spl = g > 32 ? 2 : 1;
+    const size_t flag_bytes = (size_t)n_edges * 32 * spl * 2 * sizeof(uint64_t);
+    const size_t mask_bytes = (size_t)n_edges * 2 * sizeof(uint64_t);
+    p.sflags = (uint64_t *)scratch;
+    p.smasks = (uint64_t *)((char *)scratch + flag_bytes);
+    p.sbounds = (float4 *)((char *)scratch + flag_bytes + mask_bytes);
+    (void)A;
+}
+
+// ext_scratch: caller-provided device scratch for the single-segment pipeline
+// (at least split_scratch_bytes(n_edges, g, arms) bytes); nullptr = the
+// library's stream-ordered pool.
+mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
+                           const float *q1, int64_t n_edges, int g, int rule, float range, uint32_t flags,
+                           int arm, uint8_t *valid, int32_t *first_hit, int32_t *n_seg_out, double *flops,
+                           cudaStream_t stream, void *ext_scratch) {
+    EdgeParams p;
+    int A = 0;
+    size_t smem = 0;
+    const mrpop_status st = make_params(scene, robots, q0, q1, n_edges, g, rule, range, flags, arm, valid, first_hit,
+                                        n_seg_out, flops, p, A, smem);
+    if (st != MRPOP_OK || n_edges == 0) return st;
 
     // scratch outputs when only the tally is wanted
     uint8_t *tmp_valid = nullptr;
@@ -470,33 +498,26 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
         p.valid = tmp_valid;
         p.first_hit = tmp_first;
     }
-    const size_t smem = (size_t)scene->total_f4 * sizeof(float4) + warp_scratch_bytes();
     cudaError_t err;
     if (rule == MRPOP_RULE_PLAIN) {
-        // split pipeline: flags of every sample and candidate masks in stream-ordered scratch
-        const int spl = g > 32 ? 2 : 1;
-        const size_t flag_bytes = (size_t)n_edges * 32 * spl * 2 * sizeof(uint64_t);
-        const size_t mask_bytes = (size_t)n_edges * 2 * sizeof(uint64_t);
-        const size_t bound_bytes = (size_t)n_edges * A * mrpop::kRefSpheres * sizeof(float4);
+        // split pipeline: staged flags, masks and bounds in stream-ordered scratch
         void *scratch = ext_scratch;
         if (!scratch) {
             cudaMemPool_t pool;
             err = scratch_pool(&pool);
             if (err == cudaSuccess)
-                err = cudaMallocFromPoolAsync(&scratch, flag_bytes + mask_bytes + bound_bytes, pool, stream);
+                err = cudaMallocFromPoolAsync(&scratch, split_scratch_bytes(n_edges, g, A), pool, stream);
         } else {
             err = cudaSuccess;
         }
         if (err == cudaSuccess) {
-            p.sflags = (uint64_t *)scratch;
-            p.smasks = (uint64_t *)((char *)scratch + flag_bytes);
-            p.sbounds = (float4 *)((char *)scratch + flag_bytes + mask_bytes);
-            err = timed_launch(A, mrpop::kBroad, p, smem, stream);
-            if (err == cudaSuccess) err = timed_launch(A, mrpop::kNarrow, p, smem, stream);
+            set_split_scratch(p, scratch, n_edges, g, A);
+            err = timed_launch(A, kBroad, p, smem, stream);
+            if (err == cudaSuccess) err = timed_launch(A, kNarrow, p, smem, stream);
             if (!ext_scratch) cudaFreeAsync(scratch, stream);
         }
     } else {
-        err = timed_launch(A, mrpop::kFused, p, smem, stream);
+        err = timed_launch(A, kFused, p, smem, stream);
     }
     if (tmp_valid) cudaFreeAsync(tmp_valid, stream);
     if (tmp_first) cudaFreeAsync(tmp_first, stream);
@@ -559,6 +580,29 @@ __global__ void trig_kernel(const float *x, long long n, float *c, float *s) {
 }  // namespace
 
 namespace mrpop {
+cudaError_t batch_occupancy(int arms, bool narrow, int spl, size_t smem_bytes, int *blocks_per_sm) {
+    switch (arms) {
+    case 1: return batch_occupancy_arms<1>(narrow, spl, smem_bytes, blocks_per_sm);
+    case 2: return batch_occupancy_arms<2>(narrow, spl, smem_bytes, blocks_per_sm);
+    case 3: return batch_occupancy_arms<3>(narrow, spl, smem_bytes, blocks_per_sm);
+    case 4: return batch_occupancy_arms<4>(narrow, spl, smem_bytes, blocks_per_sm);
+    case 5: return batch_occupancy_arms<5>(narrow, spl, smem_bytes, blocks_per_sm);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_batch(int arms, bool narrow, int spl, const BatchParams &b, size_t smem_bytes, int grid,
+                         cudaStream_t stream) {
+    switch (arms) {
+    case 1: return launch_batch_arms<1>(narrow, spl, b, smem_bytes, grid, stream);
+    case 2: return launch_batch_arms<2>(narrow, spl, b, smem_bytes, grid, stream);
+    case 3: return launch_batch_arms<3>(narrow, spl, b, smem_bytes, grid, stream);
+    case 4: return launch_batch_arms<4>(narrow, spl, b, smem_bytes, grid, stream);
+    case 5: return launch_batch_arms<5>(narrow, spl, b, smem_bytes, grid, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t launch_validate(int arms, KernelKind kind, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream) {
     switch (arms) {
     case 1: return launch_validate_arms<1>(kind, p, smem_bytes, stream);

@@ -1,0 +1,290 @@
+// batch.cu -- many independent single-segment validate calls (planning
+// instances of different arm counts, edge counts, granularities and scenes)
+// in one persistent launch per kernel variant, replayable as one CUDA graph.
+//
+// Instances are grouped by (arm count, samples per lane), the template
+// parameters of the kernels.  Each group gets a device array of parameter
+// blocks and a tile table (kWarpsPerBlock edges per tile, instances in order);
+// batch_kernel<A, SPL, NARROW> walks contiguous tile ranges per CTA.  A run is
+// every group's broad launch, then every group's narrow launch; the captured
+// graph runs each group's pair on its own branch so small groups overlap.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "launch.h"
+
+struct mrpop_batch {
+    struct Group {
+        int arms = 0, spl = 1;
+        int64_t n_items = 0;
+        mrpop::EdgeParams *d_items = nullptr;
+        long long *d_tiles = nullptr;
+        long long n_tiles = 0;
+        size_t smem = 0;
+        int grid[2] = {0, 0};      // CTAs of the broad / narrow launch
+        int max_grid[2] = {0, 0};  // SMs x resident CTAs
+    };
+    int device = 0;
+    std::vector<Group> groups;
+    void *d_scratch = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaStream_t> branch;  // capture-time branch streams
+};
+
+namespace {
+
+mrpop_status cuda_status(cudaError_t e, const char *what) {
+    return mrpop::fail_status(MRPOP_ERR_CUDA, (std::string(what) + ": " + cudaGetErrorString(e)).c_str());
+}
+
+void release(mrpop_batch *b) {
+    for (auto &g : b->groups) {
+        cudaFree(g.d_items);
+        cudaFree(g.d_tiles);
+    }
+    cudaFree(b->d_scratch);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    for (cudaStream_t s : b->branch) cudaStreamDestroy(s);
+    delete b;
+}
+
+mrpop::BatchParams params_of(const mrpop_batch::Group &g) {
+    mrpop::BatchParams p;
+    p.items = g.d_items;
+    p.tile_first = g.d_tiles;
+    p.n_items = (int)g.n_items;
+    p.n_tiles = g.n_tiles;
+    return p;
+}
+
+cudaError_t launch_group(const mrpop_batch::Group &g, bool narrow, int grid, cudaStream_t s) {
+    return mrpop::launch_batch(g.arms, narrow, g.spl, params_of(g), g.smem, grid, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+mrpop_status mrpop_batch_create(const mrpop_batch_item *items, int64_t n_items, mrpop_batch **out) {
+    if (!out) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_create: null out");
+    *out = nullptr;
+    if (n_items < 0 || (n_items > 0 && !items))
+        return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_create: bad item list");
+    mrpop_batch *b = new (std::nothrow) mrpop_batch();
+    if (!b) return mrpop::fail_status(MRPOP_ERR_OUT_OF_MEMORY, "batch_create: host allocation");
+    cudaGetDevice(&b->device);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+
+    // parameter blocks, grouped by (arms, samples per lane)
+    struct Entry {
+        mrpop::EdgeParams p;
+        int arms, spl;
+        size_t smem, scratch;
+    };
+    std::vector<Entry> ent;
+    size_t scratch_total = 0;
+    for (int64_t i = 0; i < n_items; i++) {
+        const mrpop_batch_item &it = items[i];
+        Entry e;
+        const mrpop_status st =
+            mrpop::make_params(it.scene, it.robots, it.q0, it.q1, it.n_edges, it.granularity, MRPOP_RULE_PLAIN, 0.0f,
+                               it.flags, it.arm, it.valid, it.first_hit, nullptr, nullptr, e.p, e.arms, e.smem);
+        if (st != MRPOP_OK) {
+            release(b);
+            return mrpop::fail_status(st, ("batch_create: item " + std::to_string(i) + ": " + mrpop_last_error()).c_str());
+        }
+        if (it.n_edges == 0) continue;
+        e.spl = it.granularity > 32 ? 2 : 1;
+        e.scratch = (mrpop::split_scratch_bytes(it.n_edges, it.granularity, e.arms) + 255) & ~(size_t)255;
+        scratch_total += e.scratch;
+        ent.push_back(e);
+    }
+    cudaError_t err = cudaSuccess;
+    if (scratch_total) err = cudaMalloc(&b->d_scratch, scratch_total);
+    if (err != cudaSuccess) {
+        release(b);
+        return cuda_status(err, "batch_create: scratch");
+    }
+    size_t off = 0;
+    for (Entry &e : ent) {
+        mrpop::set_split_scratch(e.p, (char *)b->d_scratch + off, e.p.n_edges, e.p.g, e.arms);
+        off += e.scratch;
+    }
+    for (int arms = 1; arms <= MRPOP_MAX_ARMS; arms++) {
+        for (int spl = 1; spl <= 2; spl++) {
+            mrpop_batch::Group g;
+            g.arms = arms;
+            g.spl = spl;
+            std::vector<mrpop::EdgeParams> ps;
+            std::vector<long long> tiles(1, 0);
+            for (const Entry &e : ent) {
+                if (e.arms != arms || e.spl != spl) continue;
+                ps.push_back(e.p);
+                tiles.push_back(tiles.back() + (e.p.n_edges + mrpop::kWarpsPerBlock - 1) / mrpop::kWarpsPerBlock);
+                g.smem = std::max(g.smem, e.smem);
+            }
+            if (ps.empty()) continue;
+            g.n_items = (int64_t)ps.size();
+            g.n_tiles = tiles.back();
+            err = cudaMalloc(&g.d_items, ps.size() * sizeof(mrpop::EdgeParams));
+            if (err == cudaSuccess) err = cudaMalloc(&g.d_tiles, tiles.size() * sizeof(long long));
+            if (err == cudaSuccess)
+                err = cudaMemcpy(g.d_items, ps.data(), ps.size() * sizeof(mrpop::EdgeParams), cudaMemcpyHostToDevice);
+            if (err == cudaSuccess)
+                err = cudaMemcpy(g.d_tiles, tiles.data(), tiles.size() * sizeof(long long), cudaMemcpyHostToDevice);
+            for (int k = 0; k < 2 && err == cudaSuccess; k++) {
+                int nb = 0;
+                err = mrpop::batch_occupancy(arms, k == 1, spl, g.smem, &nb);
+                const long long cap = (long long)sms * std::max(nb, 1);
+                g.max_grid[k] = (int)std::max(1LL, std::min(cap, g.n_tiles));
+                g.grid[k] = g.max_grid[k];
+            }
+            b->groups.push_back(g);
+            if (err != cudaSuccess) {
+                release(b);
+                return cuda_status(err, "batch_create: group set-up");
+            }
+        }
+    }
+    *out = b;
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_batch_run(mrpop_batch *b, void *stream) {
+    if (!b) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_run: null batch");
+    const cudaStream_t s = (cudaStream_t)stream;
+    for (int k = 0; k < 2; k++)
+        for (const auto &g : b->groups) {
+            const cudaError_t err = launch_group(g, k == 1, g.grid[k], s);
+            if (err != cudaSuccess) return cuda_status(err, "batch_run: launch");
+        }
+    return MRPOP_OK;
+}
+
+// Launch-shape tuner: per group and kernel, the grid (CTAs; multiples of the
+// SM count up to the resident maximum, and the tile count) with the shortest
+// device time over three runs.  Broad launches are tuned first (the narrow
+// kernel reads their output).  Synchronous; not for use during capture.
+mrpop_status mrpop_batch_tune(mrpop_batch *b, void *stream) {
+    if (!b) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_tune: null batch");
+    const cudaStream_t s = (cudaStream_t)stream;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        return cuda_status(cudaGetLastError(), "batch_tune: events");
+    cudaError_t err = cudaSuccess;
+    for (int k = 0; k < 2 && err == cudaSuccess; k++) {
+        for (auto &g : b->groups) {
+            std::vector<int> cand;
+            for (int m = 1; (long long)m * sms <= g.max_grid[k]; m++) cand.push_back(m * sms);
+            cand.push_back(g.max_grid[k]);
+            std::sort(cand.begin(), cand.end());
+            cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+            float best = 1e30f;
+            int best_grid = g.grid[k];
+            for (int grid : cand) {
+                if (k == 1) err = launch_group(g, false, g.grid[0], s);  // narrow reads the broad output
+                float tot = 0.0f;
+                for (int r = 0; r < 3 && err == cudaSuccess; r++) {
+                    err = cudaEventRecord(e0, s);
+                    if (err == cudaSuccess) err = launch_group(g, k == 1, grid, s);
+                    if (err == cudaSuccess) err = cudaEventRecord(e1, s);
+                    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+                    float ms = 0.0f;
+                    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+                    tot += ms;
+                }
+                if (err != cudaSuccess) break;
+                if (tot < best) {
+                    best = tot;
+                    best_grid = grid;
+                }
+            }
+            g.grid[k] = best_grid;
+            if (err != cudaSuccess) break;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err != cudaSuccess) return cuda_status(err, "batch_tune");
+    return MRPOP_OK;
+}
+
+// Captures one run into a CUDA graph: each group's broad and narrow launches
+// on a branch of their own, joined at the end.  Replaces an earlier capture.
+mrpop_status mrpop_batch_capture(mrpop_batch *b) {
+    if (!b) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_capture: null batch");
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    cudaError_t err = cudaSuccess;
+    while (b->branch.size() < b->groups.size() + 1 && err == cudaSuccess) {
+        cudaStream_t s;
+        err = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (err == cudaSuccess) b->branch.push_back(s);
+    }
+    if (err != cudaSuccess) return cuda_status(err, "batch_capture: streams");
+    cudaStream_t origin = b->branch[0];
+    std::vector<cudaEvent_t> ev(b->groups.size() + 1, nullptr);
+    for (auto &e : ev)
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    cudaGraph_t graph = nullptr;
+    if (err == cudaSuccess) err = cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal);
+    if (err == cudaSuccess) {
+        cudaError_t cerr = cudaEventRecord(ev[0], origin);
+        for (size_t i = 0; i < b->groups.size() && cerr == cudaSuccess; i++) {
+            cudaStream_t s = b->branch[i + 1];
+            cerr = cudaStreamWaitEvent(s, ev[0], 0);
+            if (cerr == cudaSuccess) cerr = launch_group(b->groups[i], false, b->groups[i].grid[0], s);
+            if (cerr == cudaSuccess) cerr = launch_group(b->groups[i], true, b->groups[i].grid[1], s);
+            if (cerr == cudaSuccess) cerr = cudaEventRecord(ev[i + 1], s);
+            if (cerr == cudaSuccess) cerr = cudaStreamWaitEvent(origin, ev[i + 1], 0);
+        }
+        err = cudaStreamEndCapture(origin, &graph);
+        if (err == cudaSuccess) err = cerr;
+    }
+    if (err == cudaSuccess) err = cudaGraphInstantiate(&b->exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    for (auto &e : ev)
+        if (e) cudaEventDestroy(e);
+    if (err != cudaSuccess) {
+        b->exec = nullptr;
+        return cuda_status(err, "batch_capture");
+    }
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_batch_launch(mrpop_batch *b, void *stream) {
+    if (!b) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_launch: null batch");
+    if (!b->exec) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_launch: no captured graph");
+    const cudaError_t err = cudaGraphLaunch(b->exec, (cudaStream_t)stream);
+    if (err != cudaSuccess) return cuda_status(err, "batch_launch");
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_batch_info(const mrpop_batch *b, int64_t *n_groups, int32_t *grids, int64_t max_groups) {
+    if (!b || !n_groups) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_info: null argument");
+    *n_groups = (int64_t)b->groups.size();
+    for (int64_t i = 0; grids && i < max_groups && i < (int64_t)b->groups.size(); i++) {
+        const auto &g = b->groups[i];
+        grids[4 * i + 0] = g.arms;
+        grids[4 * i + 1] = g.spl;
+        grids[4 * i + 2] = g.grid[0];
+        grids[4 * i + 3] = g.grid[1];
+    }
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_batch_destroy(mrpop_batch *b) {
+    if (b) release(b);
+    return MRPOP_OK;
+}
+
+}  // extern "C"

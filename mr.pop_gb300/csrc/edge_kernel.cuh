@@ -1242,83 +1242,200 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
 
 // ---------------------------------------------------------------------------
 // split pipeline for single-segment edges: the broad kernel writes every
-// sample's flag words and each edge's candidate masks to HBM (P.sflags,
-// P.smasks); the narrow kernel runs the detailed phase of edges with
-// candidates.  Each kernel's code fits the instruction cache on its own.
+// sample's flag words, each edge's candidate masks and reference-sphere
+// bounds to HBM (P.sflags, P.smasks, P.sbounds); the narrow kernel runs the
+// detailed phase of edges with candidates.  Each kernel's code fits the
+// instruction cache on its own.  broad_edge / narrow_edge are one warp's work
+// on edge e, shared by the plain kernels and the batch kernels.
 // ---------------------------------------------------------------------------
+template <int A, int SPL>
+__device__ __forceinline__ void broad_edge(const EdgeParams &P, WarpScratch &W, const float4 *S, const SceneLayout &L,
+                                           long long e, int dof, int g, int lane, bool staged) {
+    if (!staged) {
+        if (lane == 0) {
+            P.valid[e] = 0;
+            P.first_hit[e] = -2;
+            P.smasks[2 * e] = P.smasks[2 * e + 1] = 0;
+        }
+        return;
+    }
+    bool too_many;
+    edge_setup(P, W, e, dof, g, lane, too_many);
+    uint64_t envw[SPL], selfw[SPL], cand_env, cand_self;
+    double tally = 0.0;
+    const bool any = broad_decide<A, SPL>(P, W, S, L, 0, g, lane, envw, selfw, cand_env, cand_self, tally);
+    if (any) {
+#pragma unroll
+        for (int s = 0; s < SPL; s++) {
+            const long long o = (e * (32 * SPL) + lane + 32 * s) * 2;
+            P.sflags[o] = envw[s];
+            P.sflags[o + 1] = selfw[s];
+        }
+        for (int t = lane; t < A * kRefSpheres; t += 32) P.sbounds[e * (A * kRefSpheres) + t] = (&W.rsw[0][0])[t];
+    }
+    if (lane == 0) {
+        P.smasks[2 * e] = cand_env;
+        P.smasks[2 * e + 1] = cand_self;
+        if (!any) {
+            P.valid[e] = 1;
+            P.first_hit[e] = -1;
+        }
+        if (P.n_seg_out) P.n_seg_out[e] = 1;
+        if (P.flops) P.flops[e] = tally;
+    }
+    __syncwarp();
+}
+
+template <int A, int SPL>
+__device__ __forceinline__ void narrow_edge(const EdgeParams &P, WarpScratch &W, const float4 *S, const SceneLayout &L,
+                                            const float4 *det_tab, long long e, int dof, int g, int lane,
+                                            bool staged) {
+    const uint64_t cand_env = P.smasks[2 * e], cand_self = P.smasks[2 * e + 1];
+    if (!(cand_env | cand_self)) return; // verdict written by the broad kernel
+    if (!staged) {
+        if (lane == 0) {
+            P.valid[e] = 0;
+            P.first_hit[e] = -2;
+        }
+        return;
+    }
+    bool too_many;
+    edge_setup(P, W, e, dof, g, lane, too_many);
+    uint64_t envw[SPL], selfw[SPL];
+#pragma unroll
+    for (int s = 0; s < SPL; s++) {
+        const long long o = (e * (32 * SPL) + lane + 32 * s) * 2;
+        envw[s] = P.sflags[o];
+        selfw[s] = P.sflags[o + 1];
+    }
+    for (int t = lane; t < A * kRefSpheres; t += 32) (&W.rsw[0][0])[t] = P.sbounds[e * (A * kRefSpheres) + t];
+    __syncwarp();
+    const int fb = narrow_segment<A, SPL>(P, W, S, L, det_tab, 0, lane, envw, selfw, cand_env, cand_self);
+    if (lane == 0) {
+        P.valid[e] = fb < 64 ? 0 : 1;
+        P.first_hit[e] = fb < 64 ? fb + 1 : -1;
+    }
+    __syncwarp();
+}
+
 template <int A, int SPL>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
     broad_kernel(const __grid_constant__ EdgeParams P) {
     MRPOP_KERNEL_PROLOGUE()
-    for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps) {
-        if (!staged) {
-            if (lane == 0) {
-                P.valid[e] = 0;
-                P.first_hit[e] = -2;
-                P.smasks[2 * e] = P.smasks[2 * e + 1] = 0;
-            }
-            continue;
-        }
-        bool too_many;
-        edge_setup(P, W, e, dof, g, lane, too_many);
-        uint64_t envw[SPL], selfw[SPL], cand_env, cand_self;
-        double tally = 0.0;
-        const bool any = broad_decide<A, SPL>(P, W, S, L, 0, g, lane, envw, selfw, cand_env, cand_self, tally);
-        if (any) {
-#pragma unroll
-            for (int s = 0; s < SPL; s++) {
-                const long long o = (e * (32 * SPL) + lane + 32 * s) * 2;
-                P.sflags[o] = envw[s];
-                P.sflags[o + 1] = selfw[s];
-            }
-            for (int t = lane; t < A * kRefSpheres; t += 32) P.sbounds[e * (A * kRefSpheres) + t] = (&W.rsw[0][0])[t];
-        }
-        if (lane == 0) {
-            P.smasks[2 * e] = cand_env;
-            P.smasks[2 * e + 1] = cand_self;
-            if (!any) {
-                P.valid[e] = 1;
-                P.first_hit[e] = -1;
-            }
-            if (P.n_seg_out) P.n_seg_out[e] = 1;
-            if (P.flops) P.flops[e] = tally;
-        }
-        __syncwarp();
-    }
+    for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps)
+        broad_edge<A, SPL>(P, W, S, L, e, dof, g, lane, staged);
 }
 
 template <int A, int SPL>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
     narrow_kernel(const __grid_constant__ EdgeParams P) {
     MRPOP_KERNEL_PROLOGUE()
-    for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps) {
-        const uint64_t cand_env = P.smasks[2 * e], cand_self = P.smasks[2 * e + 1];
-        if (!(cand_env | cand_self)) continue; // verdict written by the broad kernel
-        if (!staged) {
-            if (lane == 0) {
-                P.valid[e] = 0;
-                P.first_hit[e] = -2;
+    for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps)
+        narrow_edge<A, SPL>(P, W, S, L, det_tab, e, dof, g, lane, staged);
+}
+
+// ---------------------------------------------------------------------------
+// batch kernels: many independent instances (each with its own scene, arm
+// layout, edges, granularity and outputs; one EdgeParams each, all of arm
+// count A and samples-per-lane SPL) in one persistent launch.  An instance's
+// edges form tiles of kWarpsPerBlock edges (one per warp); the tiles of all
+// instances are numbered in instance order and each CTA walks one contiguous
+// range of them, so it changes instance -- copying the instance's parameters
+// to shared memory and restaging its scene with the bulk-copy engine -- only
+// at instance boundaries.
+// ---------------------------------------------------------------------------
+struct BatchParams {
+    const EdgeParams *items;    // device array, one per instance
+    const long long *tile_first; // [n_items + 1]: first tile of each instance
+    int n_items;
+    long long n_tiles;
+};
+
+// One bulk copy of `bytes` from global to shared memory, completed on `bar`
+// in phase `parity`; bounded wait.  Every thread of the CTA calls it; returns
+// false (for the whole CTA) if the copy did not complete in time.
+__device__ __forceinline__ bool stage_bulk(float4 *dst, const float4 *src, uint32_t bytes, uint64_t *bar,
+                                           uint32_t parity, unsigned int *status) {
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_u32(dst)),
+            "l"(src), "r"(bytes), "r"(smem_u32(bar))
+            : "memory");
+    }
+    uint32_t done = 0;
+    for (int it = 0; it < (1 << 22) && !done; it++) {
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+    }
+    bool ok = true;
+    if (!done) {
+        atomicOr(status, 1u);
+        ok = false;
+    }
+    return __syncthreads_and(ok);
+}
+
+template <int A, int SPL, bool NARROW>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
+    batch_kernel(const __grid_constant__ BatchParams B) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ float4 det_tab[kNumDet];
+    __shared__ __align__(16) EdgeParams Ps;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < kNumDet; i += blockDim.x) det_tab[i] = c_det[i];
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const long long t0 = B.n_tiles * blockIdx.x / gridDim.x, t1 = B.n_tiles * (blockIdx.x + 1) / gridDim.x;
+    // instance of the first tile (binary search; then a forward cursor)
+    int cur = 0;
+    {
+        int lo = 0, hi = B.n_items - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (B.tile_first[mid] <= t0) lo = mid;
+            else hi = mid - 1;
+        }
+        cur = lo;
+    }
+    int item = -1;
+    uint32_t parity = 0;
+    bool staged = false;
+    for (long long t = t0; t < t1; t++) {
+        while (B.tile_first[cur + 1] <= t) cur++;
+        if (cur != item) {
+            __syncthreads(); // every warp is done with the previous instance
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(B.items + cur);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&Ps);
+            for (int i = threadIdx.x; i < (int)(sizeof(EdgeParams) / 4); i += blockDim.x) dst[i] = src[i];
+            __syncthreads();
+            const uint32_t bytes = (uint32_t)(scene_layout(Ps.sc).total * sizeof(float4));
+            staged = true;
+            if (bytes) {
+                staged = stage_bulk(reinterpret_cast<float4 *>(smem_raw), Ps.scene, bytes, &bar, parity, Ps.status);
+                parity ^= 1u;
             }
-            continue;
+            item = cur;
         }
-        bool too_many;
-        edge_setup(P, W, e, dof, g, lane, too_many);
-        uint64_t envw[SPL], selfw[SPL];
-#pragma unroll
-        for (int s = 0; s < SPL; s++) {
-            const long long o = (e * (32 * SPL) + lane + 32 * s) * 2;
-            envw[s] = P.sflags[o];
-            selfw[s] = P.sflags[o + 1];
+        const EdgeParams &P = Ps;
+        const SceneLayout L = scene_layout(P.sc);
+        const float4 *S = reinterpret_cast<const float4 *>(smem_raw);
+        WarpScratch &W = reinterpret_cast<WarpScratch *>(smem_raw + (size_t)L.total * sizeof(float4))[warp];
+        const long long e = (t - B.tile_first[cur]) * kWarpsPerBlock + warp;
+        const int dof = 7 * (P.single ? 1 : A);
+        if (e < P.n_edges) {
+            if (NARROW) narrow_edge<A, SPL>(P, W, S, L, det_tab, e, dof, P.g, lane, staged);
+            else broad_edge<A, SPL>(P, W, S, L, e, dof, P.g, lane, staged);
         }
-        for (int t = lane; t < A * kRefSpheres; t += 32) (&W.rsw[0][0])[t] = P.sbounds[e * (A * kRefSpheres) + t];
-        __syncwarp();
-        const int fb =
-            narrow_segment<A, SPL>(P, W, S, L, det_tab, 0, lane, envw, selfw, cand_env, cand_self);
-        if (lane == 0) {
-            P.valid[e] = fb < 64 ? 0 : 1;
-            P.first_hit[e] = fb < 64 ? fb + 1 : -1;
-        }
-        __syncwarp();
     }
 }
 

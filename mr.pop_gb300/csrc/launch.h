@@ -17,6 +17,18 @@ cudaError_t launch_validate(int arms, KernelKind kind, const EdgeParams &p, size
 template <int A>
 cudaError_t launch_validate_arms(KernelKind kind, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream);
 
+// Batch kernels (BatchParams: the instances of one arm count and samples per
+// lane): resident CTAs per SM at a shared-memory size, and a launch on `grid`
+// CTAs.  The dispatchers switch on the arm count (api.cu).
+cudaError_t batch_occupancy(int arms, bool narrow, int spl, size_t smem_bytes, int *blocks_per_sm);
+cudaError_t launch_batch(int arms, bool narrow, int spl, const BatchParams &b, size_t smem_bytes, int grid,
+                         cudaStream_t stream);
+template <int A>
+cudaError_t batch_occupancy_arms(bool narrow, int spl, size_t smem_bytes, int *blocks_per_sm);
+template <int A>
+cudaError_t launch_batch_arms(bool narrow, int spl, const BatchParams &b, size_t smem_bytes, int grid,
+                              cudaStream_t stream);
+
 }  // namespace mrpop
 
 #include "../../include/mrpop.h"
@@ -30,6 +42,19 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
                            const float *q1, int64_t n_edges, int g, int rule, float range, uint32_t flags,
                            int arm, uint8_t *valid, int32_t *first_hit, int32_t *n_seg_out, double *flops,
                            cudaStream_t stream, void *ext_scratch);
+
+// Argument checks and the parameter block of one validate call (run_validator
+// and the batch path).  A = arm count of the check, smem = dynamic shared
+// memory of its kernels.  n_edges == 0 passes.
+mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0, const float *q1,
+                         int64_t n_edges, int g, int rule, float range, uint32_t flags, int arm, uint8_t *valid,
+                         int32_t *first_hit, int32_t *n_seg_out, double *flops, EdgeParams &p, int &A,
+                         size_t &smem);
+
+// Scratch of the single-segment pipeline (staged flags, candidate masks and
+// reference-sphere bounds): its size, and its slices in p.
+size_t split_scratch_bytes(int64_t n_edges, int g, int A);
+void set_split_scratch(EdgeParams &p, void *scratch, int64_t n_edges, int g, int A);
 
 // Records msg as the calling thread's last error and returns st.
 mrpop_status fail_status(mrpop_status st, const char *msg);

@@ -1,0 +1,86 @@
+// launch_impl.cuh -- host launchers of the kernels for one arm count A,
+// included by validate_a{1..5}.cu (one translation unit per arm count, so the
+// instantiations compile in parallel).
+#pragma once
+#include "launch.h"
+
+namespace mrpop {
+
+template <int A, int SPL>
+const void *kernel_fn(KernelKind kind) {
+    switch (kind) {
+    case kBroad: return (const void *)broad_kernel<A, SPL>;
+    case kNarrow: return (const void *)narrow_kernel<A, SPL>;
+    default: return (const void *)validate_kernel<A, SPL>;
+    }
+}
+
+template <int A, int SPL>
+const void *batch_fn(bool narrow) {
+    return narrow ? (const void *)batch_kernel<A, SPL, true> : (const void *)batch_kernel<A, SPL, false>;
+}
+
+// Persistent grid: SMs x resident CTAs at this shared-memory size (cached per
+// kernel), no more CTAs than 4-edge tiles.
+template <int A>
+cudaError_t launch_validate_impl(KernelKind kind, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream) {
+    static int max_blocks[3][3] = {};
+    static size_t max_blocks_smem[3][3] = {};
+    const int spl = p.g > 32 ? 2 : 1;
+    const void *fn = spl == 2 ? kernel_fn<A, 2>(kind) : kernel_fn<A, 1>(kind);
+    cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    if (err != cudaSuccess) return err;
+    if (max_blocks_smem[kind][spl] != smem_bytes) {
+        int nb = 0;
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * kWarpsPerBlock, smem_bytes);
+        if (err != cudaSuccess) return err;
+        max_blocks[kind][spl] = nb > 0 ? nb : 1;
+        max_blocks_smem[kind][spl] = smem_bytes;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long need = (p.n_edges + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    long long grid = (long long)sms * max_blocks[kind][spl];
+    if (need < grid) grid = need;
+    if (grid < 1) grid = 1;
+    void *args[] = {(void *)&p};
+    return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(32 * kWarpsPerBlock), args, smem_bytes, stream);
+}
+
+template <int A>
+cudaError_t batch_occupancy_impl(bool narrow, int spl, size_t smem_bytes, int *blocks_per_sm) {
+    const void *fn = spl == 2 ? batch_fn<A, 2>(narrow) : batch_fn<A, 1>(narrow);
+    cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    if (err != cudaSuccess) return err;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, 32 * kWarpsPerBlock, smem_bytes);
+}
+
+template <int A>
+cudaError_t launch_batch_impl(bool narrow, int spl, const BatchParams &b, size_t smem_bytes, int grid,
+                              cudaStream_t stream) {
+    const void *fn = spl == 2 ? batch_fn<A, 2>(narrow) : batch_fn<A, 1>(narrow);
+    void *args[] = {(void *)&b};
+    return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(32 * kWarpsPerBlock), args, smem_bytes, stream);
+}
+
+}  // namespace mrpop
+
+// Defines the per-arm-count entry points declared in launch.h.
+#define MRPOP_DEFINE_ARM_LAUNCHERS(A)                                                                       \
+    namespace mrpop {                                                                                   \
+    template <>                                                                                         \
+    cudaError_t launch_validate_arms<A>(KernelKind kind, const EdgeParams &p, size_t smem_bytes,       \
+                                        cudaStream_t stream) {                                          \
+        return launch_validate_impl<A>(kind, p, smem_bytes, stream);                                    \
+    }                                                                                                   \
+    template <>                                                                                         \
+    cudaError_t batch_occupancy_arms<A>(bool narrow, int spl, size_t smem_bytes, int *blocks_per_sm) {  \
+        return batch_occupancy_impl<A>(narrow, spl, smem_bytes, blocks_per_sm);                         \
+    }                                                                                                   \
+    template <>                                                                                         \
+    cudaError_t launch_batch_arms<A>(bool narrow, int spl, const BatchParams &b, size_t smem_bytes,     \
+                                     int grid, cudaStream_t stream) {                                   \
+        return launch_batch_impl<A>(narrow, spl, b, smem_bytes, grid, stream);                          \
+    }                                                                                                   \
+    }

@@ -30,7 +30,8 @@ EXPORTED = [
     "mrpop_workspace_destroy", "mrpop_validate_edges_host", "mrpop_fk_spheres", "mrpop_count_flops",
     "mrpop_debug_trig", "mrpop_fp32_peak_probe", "mrpop_last_error", "mrpop_version",
     "mrpop_validate_edges_noalloc", "mrpop_broad_flops_per_sample", "mrpop_kernel_timing", "mrpop_kernel_times",
-    "mrpop_debug_row5_table",
+    "mrpop_debug_row5_table", "mrpop_batch_create", "mrpop_batch_run", "mrpop_batch_tune", "mrpop_batch_capture",
+    "mrpop_batch_launch", "mrpop_batch_info", "mrpop_batch_destroy",
 ]
 KERNEL_KINDS = ("fused", "broad", "narrow")
 NOALLOC_MAX_EDGES = 16384
@@ -50,6 +51,14 @@ class SceneDesc(C.Structure):
         ("cylinders", C.c_void_p), ("num_cylinders", C.c_uint32),
         ("cuboids", C.c_void_p), ("num_cuboids", C.c_uint32),
         ("z_cuboids", C.c_void_p), ("num_z_cuboids", C.c_uint32),
+    ]
+
+
+class BatchItem(C.Structure):
+    _fields_ = [
+        ("scene", C.c_void_p), ("robots", C.c_void_p), ("q0", C.c_void_p), ("q1", C.c_void_p),
+        ("n_edges", C.c_int64), ("granularity", C.c_int32), ("flags", C.c_uint32), ("arm", C.c_int32),
+        ("valid", C.c_void_p), ("first_hit", C.c_void_p),
     ]
 
 
@@ -86,6 +95,13 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
         "mrpop_kernel_timing": [i32],
         "mrpop_kernel_times": [C.POINTER(C.c_int64), C.POINTER(C.c_double)],
         "mrpop_debug_row5_table": [vp, i64, C.POINTER(C.c_int), C.POINTER(C.c_int)],
+        "mrpop_batch_create": [C.POINTER(BatchItem), i64, C.POINTER(vp)],
+        "mrpop_batch_run": [vp, vp],
+        "mrpop_batch_tune": [vp, vp],
+        "mrpop_batch_capture": [vp],
+        "mrpop_batch_launch": [vp, vp],
+        "mrpop_batch_info": [vp, C.POINTER(C.c_int64), vp, i64],
+        "mrpop_batch_destroy": [vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -292,6 +308,56 @@ def kernel_times(lib: C.CDLL | None = None) -> dict:
     ms = (C.c_double * 3)()
     _check(lib, lib.mrpop_kernel_times(n, ms))
     return {k: (int(n[i]), float(ms[i])) for i, k in enumerate(KERNEL_KINDS)}
+
+
+class Batch:
+    """Many independent validate calls in one launch per kernel variant
+    (mrpop_batch_*).  items: (scene, robots, q0, q1, granularity, flags, arm)
+    with q0/q1 CUDA tensors; outputs are allocated here (self.valid[i],
+    self.first_hit[i]) unless given as items[i][7:9]."""
+
+    def __init__(self, items, lib: C.CDLL | None = None):
+        import torch
+        self.lib = lib or library()
+        self.items = list(items)
+        self.valid, self.first_hit = [], []
+        arr = (BatchItem * max(1, len(self.items)))()
+        for i, it in enumerate(self.items):
+            scene, robots, q0, q1, g, flags, arm = it[:7]
+            n = q0.shape[0]
+            v = it[7] if len(it) > 7 else torch.empty(n, dtype=torch.uint8, device=q0.device)
+            f = it[8] if len(it) > 8 else torch.empty(n, dtype=torch.int32, device=q0.device)
+            self.valid.append(v)
+            self.first_hit.append(f)
+            arr[i] = BatchItem(scene.handle, robots.handle, q0.data_ptr() if n else None,
+                               q1.data_ptr() if n else None, n, g, flags, arm, v.data_ptr() if n else None,
+                               f.data_ptr() if n else None)
+        h = C.c_void_p()
+        _check(self.lib, self.lib.mrpop_batch_create(arr, len(self.items), C.byref(h)))
+        self.handle = h
+
+    def run(self, stream=None):
+        _check(self.lib, self.lib.mrpop_batch_run(self.handle, _stream_ptr(stream)))
+
+    def tune(self, stream=None):
+        _check(self.lib, self.lib.mrpop_batch_tune(self.handle, _stream_ptr(stream)))
+
+    def capture(self):
+        _check(self.lib, self.lib.mrpop_batch_capture(self.handle))
+
+    def launch(self, stream=None):
+        _check(self.lib, self.lib.mrpop_batch_launch(self.handle, _stream_ptr(stream)))
+
+    def info(self) -> list[tuple[int, int, int, int]]:
+        n = C.c_int64()
+        grids = np.zeros(4 * 16, np.int32)
+        _check(self.lib, self.lib.mrpop_batch_info(self.handle, C.byref(n), grids.ctypes.data, 16))
+        return [tuple(int(x) for x in grids[4 * i:4 * i + 4]) for i in range(n.value)]
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            self.lib.mrpop_batch_destroy(self.handle)
+            self.handle = None
 
 
 class Workspace:

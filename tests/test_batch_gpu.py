@@ -1,0 +1,102 @@
+"""Batched validation of many planning instances (mrpop_batch_*): results equal
+the per-instance plain calls bit for bit, through a plain run, after the
+launch-shape tuner, and through the captured CUDA graph."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _instances(pkg, cuda, n, scale, seed):
+    W = pkg.workloads
+    insts = W.config4_instances(n_instances=n, seed=seed, scale=scale)
+    items = []
+    keep = []
+    for k, wl in enumerate(insts):
+        scene = pkg.Scene(wl.scene)
+        rb = pkg.RobotSet(len(wl.bases), wl.bases)
+        q0 = cuda.from_numpy(wl.q0).cuda()
+        q1 = cuda.from_numpy(wl.q1).cuda()
+        arm = -1
+        if k % 7 == 3:  # a single-arm (roadmap) item on one arm's base
+            arm = len(wl.bases) - 1
+            q0 = q0[:, 7 * arm:7 * arm + 7].contiguous()
+            q1 = q1[:, 7 * arm:7 * arm + 7].contiguous()
+        flags = wl.flags if k % 5 else (pkg.CHECK_SELF | pkg.MODE_EXACT)
+        items.append((scene, rb, q0, q1, wl.granularity, flags, arm))
+        keep.append(wl)
+    # an empty item in the middle
+    items.insert(5, (items[0][0], items[0][1], items[0][2][:0], items[0][3][:0], 32, pkg.CHECK_SELF, -1))
+    return items
+
+
+def _reference(pkg, cuda, items):
+    out = []
+    for scene, rb, q0, q1, g, flags, arm in items:
+        v, f = pkg.validate(scene, rb, q0, q1, g, flags, arm)
+        out.append((v.cpu().numpy(), f.cpu().numpy()))
+    cuda.cuda.synchronize()
+    return out
+
+
+def _check(batch, ref):
+    for i, (v, f) in enumerate(ref):
+        assert np.array_equal(batch.valid[i].cpu().numpy(), v), i
+        assert np.array_equal(batch.first_hit[i].cpu().numpy(), f), i
+
+
+def test_batch_equals_per_instance_calls(cuda, pkg):
+    items = _instances(pkg, cuda, 48, 0.1, seed=1)
+    ref = _reference(pkg, cuda, items)
+    b = pkg.Batch(items)
+    groups = b.info()
+    assert len(groups) >= 5 and all(1 <= a <= 5 and s in (1, 2) for a, s, _, _ in groups)
+    b.run()
+    cuda.cuda.synchronize()
+    _check(b, ref)
+    # rerun on cleared outputs after tuning, then through the captured graph
+    for v, f in zip(b.valid, b.first_hit):
+        v.fill_(7)
+        f.fill_(-9)
+    b.tune()
+    b.run()
+    cuda.cuda.synchronize()
+    _check(b, ref)
+    for v, f in zip(b.valid, b.first_hit):
+        v.fill_(7)
+        f.fill_(-9)
+    b.capture()
+    b.launch()
+    b.launch()
+    cuda.cuda.synchronize()
+    _check(b, ref)
+    for it in items:
+        assert it[0].status() == 0
+
+
+def test_batch_refilled_inputs(cuda, pkg):
+    """A captured batch reads its input buffers at execution time."""
+    items = _instances(pkg, cuda, 12, 0.05, seed=2)
+    b = pkg.Batch(items)
+    b.capture()
+    W = pkg.workloads
+    rng = np.random.default_rng(9)
+    for scene, rb, q0, q1, g, flags, arm in items:
+        if q0.shape[0] == 0:
+            continue
+        arms = q0.shape[1] // 7
+        a0, a1 = W.random_edges(rng, q0.shape[0], arms, 1.5)
+        q0.copy_(cuda.from_numpy(a0))
+        q1.copy_(cuda.from_numpy(a1))
+    b.launch()
+    cuda.cuda.synchronize()
+    _check(b, _reference(pkg, cuda, items))
+
+
+def test_batch_rejects_bad_items(cuda, pkg):
+    items = _instances(pkg, cuda, 4, 0.02, seed=3)
+    scene, rb, q0, q1, g, flags, arm = items[1]
+    bad = list(items)
+    bad[1] = (scene, rb, q0, q1, 65, flags, arm)
+    with pytest.raises(pkg.MrpopError, match="item 1"):
+        pkg.Batch(bad)
