@@ -218,6 +218,13 @@ def roofline(kt: dict, flops: dict, peak: float, workload: str, arms: int, spl: 
                           "MEASURED_PEAKS.json has no FP32 figure",
            "achieved_basis": f"{flops[dom]:.4g} algorithmic flops per launch (FMA=2, unculled per-test costs) / "
                              f"CUDA-event launch time on the launching stream"}
+    if out["traffic"]:
+        hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs") \
+            if (ROOT / "MEASURED_PEAKS.json").exists() else None
+        bw = out["traffic"] / launch_s / 1e9
+        out["hbm_check"] = {"achieved_gbs": bw, "peak_gbs": hbm, "frac": bw / hbm if hbm else None,
+                            "basis": "ncu DRAM bytes of one launch / live launch time, against the measured copy "
+                                     "bandwidth (MEASURED_PEAKS.json): HBM is not the bound"}
     if prof.get("executed_fp32_flops_per_launch"):
         ex = prof["executed_fp32_flops_per_launch"] / launch_s / 1e12
         out["executed"] = {"achieved": ex, "frac": ex / peak,
