@@ -613,13 +613,19 @@ __device__ __forceinline__ int nth_bit(uint64_t m, int n) {
 }
 
 // bit r set: detailed self row r is checked for an arm with self flags sm
+// Rows whose first-read sphere is on joint j (quirk: sphere r, else first(r)).
+__host__ __device__ constexpr uint32_t joint_rows(int j, bool quirk) {
+    uint32_t m = 0;
+    for (int r = 0; r < kDetRows; r++)
+        if (det_joint(quirk ? r : det_row_first(r)) == j) m |= 1u << r;
+    return m;
+}
+
 __device__ __forceinline__ uint32_t row_mask(uint32_t sm, bool quirk) {
     uint32_t m = 0;
 #pragma unroll
-    for (int r = 0; r < kDetRows; r++) {
-        const int pi = quirk ? r : det_row_first(r);
-        if (sm >> det_joint(pi) & 1u) m |= 1u << r;
-    }
+    for (int j = 0; j < kNumJoints; j++)
+        if (sm >> j & 1u) m |= quirk ? joint_rows(j, true) : joint_rows(j, false);
     return m;
 }
 
@@ -867,6 +873,8 @@ static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch
         if (P.row5 && (c.rm & row5_rows(c.quirk)) &&
             row5_apart(P.row5, sample_q1(W, P.rule, seg, qa + 5, k), sample_q1(W, P.rule, seg, qa + 6, k)))
             c.rm &= ~row5_rows(c.quirk);
+        // the arm's chain is walked only if some lane has env or row tests on it
+        if (!__any_sync(kFull, !c.hit && (c.em | c.rm))) continue;
         Xf T;
         load_base(T, P.base[a]);
 #pragma unroll 1
