@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
-    ap.add_argument("--workload", choices=["config1", "config2", "config3", "config4"], default="config2")
+    ap.add_argument("--workload", choices=["config1", "config2", "config3", "config3s", "config4"], default="config2")
     ap.add_argument("--instances", type=int, default=512, help="config4: planning instances in the batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -133,7 +133,8 @@ def max_over_ranks(x: float, world: int) -> float:
 
 def load_workload(pkg, name):
     W = pkg.workloads
-    return {"config1": W.config1, "config2": W.config2, "config3": W.config3}[name]()
+    return {"config1": W.config1, "config2": W.config2, "config3": W.config3,
+            "config3s": W.config3_shortcuts}[name]()
 
 
 def workload_config(wl, extra):
@@ -143,6 +144,9 @@ def workload_config(wl, extra):
            "arms": int(len(wl.bases)) if wl.arm < 0 else 1, "dof": int(wl.q0.shape[1]), "obstacles": n_obst,
            "checks": "env+self" if wl.flags & 3 == 3 else ("self" if wl.flags & 2 else "env"),
            "semantics": "reference verdicts (thread split included)", "l2": "flushed (256 MiB write) before every step"}
+    if wl.rule:
+        cfg.update({"rule": {1: "connect", 2: "bspline", 3: "shortcut"}[wl.rule], "range": wl.range_,
+                    "samples": "segments up to the first colliding one x granularity"})
     cfg.update(extra)
     return cfg
 
@@ -200,24 +204,25 @@ def committed_profile(kernel: str, workload: str) -> dict:
     return {}
 
 
-def roofline(kt: dict, flops: dict, peak: float, workload: str, arms: int, spl: int) -> dict:
+def roofline(kt: dict, flops: dict, peak: float, workload: str, arms: int, spl: int, steps: int) -> dict:
     """Roofline of the kernel with the largest share of device time.
-    kt: {kind: (launches, total ms)} from the library's event timing;
-    flops: algorithmic flops per launch of each kind."""
+    kt: {kind: (launches, total ms)} from the library's event timing over
+    `steps` steps; flops: algorithmic flops per step of each kind (a kind may
+    launch more than once per step: segment rounds)."""
     ran = {k: v for k, v in kt.items() if v[0] > 0}
     total_ms = sum(v[1] for v in ran.values())
     dom = max(ran, key=lambda k: ran[k][1])
     launches, ms = ran[dom]
     launch_s = ms / launches / 1e3
-    achieved = flops[dom] / launch_s / 1e12
+    achieved = flops[dom] / (ms / steps / 1e3) / 1e12
     prof = committed_profile(KERNEL_NAMES[dom], workload)
     out = {"bound": "fp32", "kernel": f"{KERNEL_NAMES[dom]}<{arms},{spl}>", "achieved": achieved, "peak": peak,
            "unit": "TFLOP/s", "frac": achieved / peak, "traffic": prof.get("dram_bytes_per_launch"),
-           "launch_ms": launch_s * 1e3, "share": ms / total_ms,
+           "launch_ms": launch_s * 1e3, "launches_per_step": launches / steps, "share": ms / total_ms,
            "peak_source": "measured: FP32 FMA loop (mrpop_fp32_peak_probe) timed in this run; "
                           "MEASURED_PEAKS.json has no FP32 figure",
-           "achieved_basis": f"{flops[dom]:.4g} algorithmic flops per launch (FMA=2, unculled per-test costs) / "
-                             f"CUDA-event launch time on the launching stream"}
+           "achieved_basis": f"{flops[dom]:.4g} algorithmic flops per step (FMA=2, unculled per-test costs) / "
+                             f"the kernel's CUDA-event time per step on the launching stream"}
     if out["traffic"]:
         hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs") \
             if (ROOT / "MEASURED_PEAKS.json").exists() else None
@@ -231,7 +236,7 @@ def roofline(kt: dict, flops: dict, peak: float, workload: str, arms: int, spl: 
                            "basis": "FP32 flops the kernel executed (ncu: 2*ffma + fadd + fmul thread "
                                     "instructions) / live launch time; culling skips algorithmic work"}
     out["kernels"] = {KERNEL_NAMES[k]: {"launches": v[0], "avg_ms": v[1] / v[0], "share": v[1] / total_ms,
-                                        "algorithmic_tflops": flops[k] / (v[1] / v[0] / 1e3) / 1e12}
+                                        "algorithmic_tflops": flops[k] / (v[1] / steps / 1e3) / 1e12}
                       for k, v in ran.items()}
     return out
 
@@ -363,12 +368,26 @@ def run_mine(args, world, rank, local):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
 
-    def step():
-        pkg.validate(scene, robots, q0, q1, wl.granularity, wl.flags, wl.arm, valid=valid, first_hit=first)
+    nseg = torch.empty(n, dtype=torch.int32, device="cuda") if wl.rule else None
 
-    flops_launch = float(pkg.count_flops(scene, robots, q0, q1, wl.granularity, wl.flags, wl.arm).sum().item())
+    def step():
+        pkg.validate(scene, robots, q0, q1, wl.granularity, wl.flags, wl.arm, wl.rule, wl.range_, valid=valid,
+                     first_hit=first, n_seg=nseg)
+
+    if wl.rule:
+        # segmented rule: the samples a validation checks are the segments up
+        # to the first colliding one (the reference's loop stops there) x g
+        step()
+        torch.cuda.synchronize()
+        v, f, ns = valid.cpu().numpy(), first.cpu().numpy().astype(np.int64), nseg.cpu().numpy().astype(np.int64)
+        segs = np.where(v == 1, np.maximum(ns, 0), np.where(f > 0, (f - 1) // wl.granularity + 1, 0))
+        samples = int(segs.sum()) * wl.granularity
+    flops_launch = float(pkg.count_flops(scene, robots, q0, q1, wl.granularity, wl.flags, wl.arm, wl.rule,
+                                         wl.range_).sum().item())
     broad_launch = pkg.broad_flops_per_sample(scene, robots, wl.flags, wl.arm) * samples
     flops = {"fused": flops_launch, "broad": broad_launch, "narrow": flops_launch - broad_launch}
+    if wl.rule:  # the tail kernel does both phases of the few edges with more segments than the rounds
+        flops["fused"] = 0.0
     for _ in range(args.warmup):
         flush.zero_()
         step()
@@ -404,7 +423,7 @@ def run_mine(args, world, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
         "config": workload_config(wl, {"parallelism": f"replica x{world}, independent edge batches"}),
         "gpu_launches": sum(v[0] for v in kt.values()),
-        "roofline": roofline(kt, flops, peak, args.workload, arms, spl),
+        "roofline": roofline(kt, flops, peak, args.workload, arms, spl, args.steps),
         "clocks": clk,
     }
     if not args.no_e2e:
@@ -415,11 +434,13 @@ def run_mine(args, world, rank, local):
         hf = torch.empty(n, dtype=torch.int32).pin_memory()
         a0, a1, av, af = hq0.numpy(), hq1.numpy(), hv.numpy(), hf.numpy()
         for _ in range(2):
-            ws.validate(scene, robots, a0, a1, wl.granularity, wl.flags, wl.arm, valid=av, first_hit=af)
+            ws.validate(scene, robots, a0, a1, wl.granularity, wl.flags, wl.arm, wl.rule, wl.range_, valid=av,
+                        first_hit=af)
         barrier(world)
         t = time.perf_counter()
         for _ in range(args.steps):
-            ws.validate(scene, robots, a0, a1, wl.granularity, wl.flags, wl.arm, valid=av, first_hit=af)
+            ws.validate(scene, robots, a0, a1, wl.granularity, wl.flags, wl.arm, wl.rule, wl.range_, valid=av,
+                        first_hit=af)
         dt = max_over_ranks(time.perf_counter() - t, world)
         out["e2e"] = {"value": world * samples * args.steps / dt, "unit": UNIT,
                       "h2d_bytes_per_step": int(a0.nbytes + a1.nbytes), "d2h_bytes_per_step": int(av.nbytes + af.nbytes),
@@ -494,7 +515,7 @@ def run_reference(args, world, rank, local):
     out = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded generators)", "impl": "reference"}
-    if ref_runner.available() and args.workload in ("config1", "config2", "config3"):
+    if ref_runner.available() and args.workload in ("config1", "config2", "config3", "config3s"):
         R = ref_runner.RefHarness()
         kind = R.KIND_SINGLE if wl.arm >= 0 else R.KIND_COMPOSITE
         arms = len(wl.bases)
@@ -509,8 +530,18 @@ def run_reference(args, world, rank, local):
         res = (torch.empty(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda"))
 
         def step():
-            R.validate(env, q0, q1, wl.granularity, kind, 0, 0.0, arms if kind == R.KIND_COMPOSITE else 1,
+            R.validate(env, q0, q1, wl.granularity, kind, wl.rule, wl.range_, arms if kind == R.KIND_COMPOSITE else 1,
                        max(wl.arm, 0), blocks=blocks, out=res)
+
+        if wl.rule:
+            # segmented rule: segments up to the first failing one, x g
+            step()
+            torch.cuda.synchronize()
+            v, sf = res[0].cpu().numpy(), res[1].cpu().numpy().astype(np.int64)
+            L = orc.lib()
+            ns = np.array([L.oracle_segment_count(a.ctypes.data, b.ctypes.data, a.shape[0], wl.rule, float(wl.range_))
+                           for a, b in zip(wl.q0, wl.q1)], np.int64)
+            samples = int(np.where(v == 1, np.maximum(ns, 0), sf + 1).sum()) * wl.granularity
 
         for _ in range(args.warmup):
             flush.zero_()

@@ -149,7 +149,7 @@ mrpop_status mrpop_validate_segments(const mrpop_scene *scene, const mrpop_robot
  * it, or a planner loop that may not enter the allocator.  No counterpart in the
  * reference (its planner keeps all scratch in fixed __device__ arrays).
  *   - Calls no allocation routine.  Its scratch is one fixed array in the
- *     library's device memory, about 27.5 MiB per device
+ *     library's device memory, about 27.6 MiB per device
  *     (MRPOP_NOALLOC_MAX_EDGES edges at granularity 64), held by every GPU that
  *     loads the library until the process exits.
  *   - n_edges above MRPOP_NOALLOC_MAX_EDGES is rejected (MRPOP_ERR_INVALID_ARGUMENT).
@@ -256,9 +256,9 @@ mrpop_status mrpop_broad_flops_per_sample(const mrpop_scene *scene, const mrpop_
  * summed device time in ms since the previous read, and releases the events.
  * Read on the device the launches ran on. */
 #define MRPOP_KERNEL_KINDS 3
-#define MRPOP_KERNEL_FUSED 0  /* segmented rules: broad and narrow phase in one kernel */
-#define MRPOP_KERNEL_BROAD 1  /* single-segment edges: broad phase */
-#define MRPOP_KERNEL_NARROW 2 /* single-segment edges: narrow phase */
+#define MRPOP_KERNEL_FUSED 0  /* segmented rules, segments after the split rounds: both phases in one kernel */
+#define MRPOP_KERNEL_BROAD 1  /* broad phase (single-segment edges, or one segment round) */
+#define MRPOP_KERNEL_NARROW 2 /* narrow phase (single-segment edges, or one segment round) */
 mrpop_status mrpop_kernel_timing(int enable);
 mrpop_status mrpop_kernel_times(int64_t *launches, double *ms);
 

@@ -462,17 +462,21 @@ mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots,
 
 size_t split_scratch_bytes(int64_t n_edges, int g, int A) {
     const int spl = g > 32 ? 2 : 1;
-    return (size_t)n_edges * (32 * spl * 2 * sizeof(uint64_t) + 2 * sizeof(uint64_t) + A * kRefSpheres * sizeof(float4));
+    return (size_t)n_edges * (32 * spl * 2 * sizeof(uint64_t) + 2 * sizeof(uint64_t) + A * kRefSpheres * sizeof(float4) +
+                              2 * sizeof(int32_t));
 }
 
 void set_split_scratch(EdgeParams &p, void *scratch, int64_t n_edges, int g, int A) {
     const int spl = g > 32 ? 2 : 1;
     const size_t flag_bytes = (size_t)n_edges * 32 * spl * 2 * sizeof(uint64_t);
     const size_t mask_bytes = (size_t)n_edges * 2 * sizeof(uint64_t);
-    p.sflags = (uint64_t *)scratch;
-    p.smasks = (uint64_t *)((char *)scratch + flag_bytes);
-    p.sbounds = (float4 *)((char *)scratch + flag_bytes + mask_bytes);
-    (void)A;
+    const size_t bound_bytes = (size_t)n_edges * A * kRefSpheres * sizeof(float4);
+    char *b = (char *)scratch;
+    p.sflags = (uint64_t *)b;
+    p.smasks = (uint64_t *)(b + flag_bytes);
+    p.sbounds = (float4 *)(b + flag_bytes + mask_bytes);
+    p.snseg = (int32_t *)(b + flag_bytes + mask_bytes + bound_bytes);
+    p.sdone = p.snseg + n_edges;
 }
 
 // ext_scratch: caller-provided device scratch for the single-segment pipeline
@@ -498,26 +502,33 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
         p.valid = tmp_valid;
         p.first_hit = tmp_first;
     }
+    // split pipeline: staged flags, masks, bounds and segment state in
+    // stream-ordered scratch.  Single-segment edges: one broad and one narrow
+    // launch.  Segmented rules: segment r of every undecided edge per round
+    // (broad + narrow), kSegRounds rounds, then the fused kernel for the edges
+    // that still have segments left, from segment kSegRounds on.
     cudaError_t err;
-    if (rule == MRPOP_RULE_PLAIN) {
-        // split pipeline: staged flags, masks and bounds in stream-ordered scratch
-        void *scratch = ext_scratch;
-        if (!scratch) {
-            cudaMemPool_t pool;
-            err = scratch_pool(&pool);
-            if (err == cudaSuccess)
-                err = cudaMallocFromPoolAsync(&scratch, split_scratch_bytes(n_edges, g, A), pool, stream);
-        } else {
-            err = cudaSuccess;
-        }
-        if (err == cudaSuccess) {
-            set_split_scratch(p, scratch, n_edges, g, A);
+    void *scratch = ext_scratch;
+    if (!scratch) {
+        cudaMemPool_t pool;
+        err = scratch_pool(&pool);
+        if (err == cudaSuccess) err = cudaMallocFromPoolAsync(&scratch, split_scratch_bytes(n_edges, g, A), pool, stream);
+    } else {
+        err = cudaSuccess;
+    }
+    if (err == cudaSuccess) {
+        set_split_scratch(p, scratch, n_edges, g, A);
+        const int rounds = rule == MRPOP_RULE_PLAIN ? 1 : kSegRounds;
+        for (int r = 0; r < rounds && err == cudaSuccess; r++) {
+            p.seg0 = r;
             err = timed_launch(A, kBroad, p, smem, stream);
             if (err == cudaSuccess) err = timed_launch(A, kNarrow, p, smem, stream);
-            if (!ext_scratch) cudaFreeAsync(scratch, stream);
         }
-    } else {
-        err = timed_launch(A, kFused, p, smem, stream);
+        if (err == cudaSuccess && rule != MRPOP_RULE_PLAIN) {
+            p.seg0 = kSegRounds;
+            err = timed_launch(A, kFused, p, smem, stream);
+        }
+        if (!ext_scratch) cudaFreeAsync(scratch, stream);
     }
     if (tmp_valid) cudaFreeAsync(tmp_valid, stream);
     if (tmp_first) cudaFreeAsync(tmp_first, stream);

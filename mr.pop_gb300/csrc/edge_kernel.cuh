@@ -108,6 +108,9 @@ __host__ __device__ inline SceneLayout scene_layout(const SceneCounts &c) {
 // Approx spheres whose swept bounds the narrow phase reuses: 0..8 (the
 // reference sphere of every detailed sub-group, see grp_ref).
 constexpr int kRefSpheres = 9;
+// Segmented rules: segments checked by rounds of the split kernels before the
+// fused kernel takes the remaining ones.
+constexpr int kSegRounds = 4;
 
 struct EdgeParams {
     const float *q0;
@@ -117,6 +120,7 @@ struct EdgeParams {
     int flags;       // MRPOP_CHECK_* | MRPOP_MODE_EXACT
     int single;      // 1: single-arm (fkcc_single_buffer_mr) semantics
     int rule;        // MRPOP_RULE_*
+    int seg0;        // segmented rules: the segment this launch checks (split kernels) or starts at (fused)
     float range;
     uint8_t *valid;
     int32_t *first_hit;
@@ -131,6 +135,8 @@ struct EdgeParams {
     uint64_t *sflags;           // split pipeline: per-sample {env, self} flag words
     uint64_t *smasks;           // split pipeline: per-edge {env, self} candidate masks
     float4 *sbounds;            // split pipeline: per-edge swept reference-sphere bounds [A][kRefSpheres]
+    int32_t *snseg;             // segmented rules: per-edge segment count (-1: too many), from segment 0
+    int32_t *sdone;             // segmented rules: per-edge verdict written
     float gofs[11];             // sub-group g: |group centre - reference sphere centre| + group radius
     float4 grp[11];             // detailed sub-group bounds in their joint frame (+margin)
     const uint32_t *row5;       // forearm-hand rows table (kRow5N6 x kRow5N7 bits), or nullptr
@@ -147,6 +153,9 @@ struct WarpScratch {
     // every sample of the segment ({centre, radius}, sphere radius excluded);
     // written by the broad phase, read by the narrow phase's arm-vs-arm screen
     float4 rsw[kMaxArms][kRefSpheres];
+    // sub-group bounds over the segment's samples derived from rsw (the
+    // narrow phase's arm-vs-arm screen)
+    float4 gbd[kMaxArms][11];
     union {
         struct {
             float4 swept[kMaxArms][kNumApprox]; // per-arm swept bound of each approx sphere
@@ -809,7 +818,7 @@ __device__ __forceinline__ void lane_rows(int j, const EdgeParams &P, const Xf &
     while (m1) {
         const int r = __ffs(m1) - 1;
         m1 &= m1 - 1;
-        const float3 p = place_reg(T, c_det[c.quirk ? r : det_row_first(r)]);
+        const float3 p = place_reg(T, det_tab[c.quirk ? r : det_row_first(r)]);
         W.lanes.stash[r][0][lane] = p.x;
         W.lanes.stash[r][1][lane] = p.y;
         W.lanes.stash[r][2][lane] = p.z;
@@ -989,8 +998,8 @@ static __device__ __noinline__ bool cross_swept(const EdgeParams &P, WarpScratch
                 const int ga = t / kNumGroups, gb = t - kNumGroups * ga;
                 bool pass = false;
                 if (t < kNumGroups * kNumGroups && (uj >> grp_joint(ga) & 1u)) {
-                    const float4 u = W.rsw[a][grp_ref(ga)], v = W.rsw[b][grp_ref(gb)];
-                    pass = near3(u.x, u.y, u.z, make_float4(v.x, v.y, v.z, v.w + P.gofs[gb]), u.w + P.gofs[ga]);
+                    const float4 u = W.gbd[a][ga];
+                    pass = near3(u.x, u.y, u.z, W.gbd[b][gb], u.w);
                 }
                 uint32_t bal = __ballot_sync(kFull, pass);
                 while (bal) {
@@ -1071,6 +1080,17 @@ __device__ __forceinline__ int edge_setup(const EdgeParams &P, WarpScratch &W, l
     }
     __syncwarp();
     return nseg;
+}
+
+// CONNECT: the segment start of segment `seg` (the caller's loop adds the
+// per-segment step once per finished segment, pop_planner.cu:697).
+__device__ __forceinline__ void connect_advance(WarpScratch &W, int dof, int seg, int lane) {
+    for (int d = lane; d < dof; d += 32) {
+        float b = W.base[d];
+        for (int s = 0; s < seg; s++) b = __fadd_rn(b, W.delta[d]);
+        W.base[d] = b;
+    }
+    __syncwarp();
 }
 
 // Broad phase of one segment for this lane's samples plus the decision: which
@@ -1164,6 +1184,13 @@ __device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &
                                               const uint64_t (&envw)[SPL], const uint64_t (&selfw)[SPL],
                                               uint64_t cand_env, uint64_t cand_self) {
     MRPOP_PHASE_START();
+    // sub-group bounds over the segment's samples, from the reference-sphere bounds
+    for (int t = lane; t < A * kNumGroups; t += 32) {
+        const int a = t / kNumGroups, g = t - kNumGroups * a;
+        const float4 u = W.rsw[a][grp_ref(g)];
+        W.gbd[a][g] = make_float4(u.x, u.y, u.z, u.w + P.gofs[g]);
+    }
+    __syncwarp();
     uint64_t hits = 0;
 #pragma unroll
     for (int s = 0; s < SPL; s++) {
@@ -1220,12 +1247,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
             }
             continue;
         }
+        if (P.seg0 > 0 && (P.sdone[e] || P.snseg[e] <= P.seg0)) continue; // decided by the split rounds
         bool too_many;
         const int nseg = edge_setup(P, W, e, dof, g, lane, too_many);
         int first = 0;
         double tally = 0.0;
         const int nseg_run = too_many ? 0 : nseg;
-        for (int seg = 0; seg < nseg_run && first == 0; seg++) {
+        if (P.rule == kRuleConnect && P.seg0 > 0) connect_advance(W, dof, P.seg0, lane);
+        for (int seg = P.seg0; seg < nseg_run && first == 0; seg++) {
             uint64_t envw[SPL], selfw[SPL], cand_env, cand_self;
             if (broad_decide<A, SPL>(P, W, S, L, seg, g, lane, envw, selfw, cand_env, cand_self, tally)) {
                 const int fb = narrow_segment<A, SPL>(P, W, S, L, det_tab, seg, lane, envw, selfw, cand_env,
@@ -1242,7 +1271,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
             P.valid[e] = (first == 0 && !too_many) ? 1 : 0;
             P.first_hit[e] = too_many ? -2 : (first ? first : -1);
             if (P.n_seg_out) P.n_seg_out[e] = nseg;
-            if (P.flops) P.flops[e] = tally;
+            if (P.flops) P.flops[e] = P.seg0 > 0 ? P.flops[e] + tally : tally;
         }
         __syncwarp();
     }
@@ -1256,7 +1285,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
 // instruction cache on its own.  broad_edge / narrow_edge are one warp's work
 // on edge e, shared by the plain kernels and the batch kernels.
 // ---------------------------------------------------------------------------
-template <int A, int SPL>
+template <int A, int SPL, bool SEG>
 __device__ __forceinline__ void broad_edge(const EdgeParams &P, WarpScratch &W, const float4 *S, const SceneLayout &L,
                                            long long e, int dof, int g, int lane, bool staged) {
     if (!staged) {
@@ -1267,11 +1296,43 @@ __device__ __forceinline__ void broad_edge(const EdgeParams &P, WarpScratch &W, 
         }
         return;
     }
+    // SEG: a segment round of a segmented rule (r = P.seg0); otherwise a
+    // single-segment edge (r = 0, compiled as a constant)
+    const int r = SEG ? P.seg0 : 0;
+    constexpr bool segmented = SEG;
+    if (segmented && r > 0 && (P.sdone[e] || P.snseg[e] <= r)) {
+        if (lane == 0) P.smasks[2 * e] = P.smasks[2 * e + 1] = 0;
+        return;
+    }
     bool too_many;
-    edge_setup(P, W, e, dof, g, lane, too_many);
+    const int nseg = edge_setup(P, W, e, dof, g, lane, too_many);
+    if (segmented) {
+        if (r == 0) {
+            const bool none = too_many || nseg <= 0; // decided without a check
+            if (lane == 0) {
+                P.snseg[e] = too_many ? -1 : nseg;
+                if (P.n_seg_out) P.n_seg_out[e] = nseg;
+                P.sdone[e] = none ? 1 : 0;
+                if (none) {
+                    P.valid[e] = too_many ? 0 : 1;
+                    P.first_hit[e] = too_many ? -2 : -1;
+                    P.smasks[2 * e] = P.smasks[2 * e + 1] = 0;
+                    if (P.flops) P.flops[e] = 0.0;
+                }
+            }
+            if (none) {
+                __syncwarp();
+                return;
+            }
+        } else if (P.rule == kRuleConnect) {
+            connect_advance(W, dof, r, lane);
+        }
+    } else {
+        (void)nseg;
+    }
     uint64_t envw[SPL], selfw[SPL], cand_env, cand_self;
     double tally = 0.0;
-    const bool any = broad_decide<A, SPL>(P, W, S, L, 0, g, lane, envw, selfw, cand_env, cand_self, tally);
+    const bool any = broad_decide<A, SPL>(P, W, S, L, r, g, lane, envw, selfw, cand_env, cand_self, tally);
     if (any) {
 #pragma unroll
         for (int s = 0; s < SPL; s++) {
@@ -1284,17 +1345,18 @@ __device__ __forceinline__ void broad_edge(const EdgeParams &P, WarpScratch &W, 
     if (lane == 0) {
         P.smasks[2 * e] = cand_env;
         P.smasks[2 * e + 1] = cand_self;
-        if (!any) {
+        if (!any && (!segmented || r == nseg - 1)) { // the last segment passed the broad phase
             P.valid[e] = 1;
             P.first_hit[e] = -1;
+            if (segmented) P.sdone[e] = 1;
         }
-        if (P.n_seg_out) P.n_seg_out[e] = 1;
-        if (P.flops) P.flops[e] = tally;
+        if (!segmented && P.n_seg_out) P.n_seg_out[e] = 1;
+        if (P.flops) P.flops[e] = (segmented && r > 0) ? P.flops[e] + tally : tally;
     }
     __syncwarp();
 }
 
-template <int A, int SPL>
+template <int A, int SPL, bool SEG>
 __device__ __forceinline__ void narrow_edge(const EdgeParams &P, WarpScratch &W, const float4 *S, const SceneLayout &L,
                                             const float4 *det_tab, long long e, int dof, int g, int lane,
                                             bool staged) {
@@ -1307,8 +1369,11 @@ __device__ __forceinline__ void narrow_edge(const EdgeParams &P, WarpScratch &W,
         }
         return;
     }
+    const int r = SEG ? P.seg0 : 0;
+    constexpr bool segmented = SEG;
     bool too_many;
-    edge_setup(P, W, e, dof, g, lane, too_many);
+    const int nseg = edge_setup(P, W, e, dof, g, lane, too_many);
+    if (SEG && P.rule == kRuleConnect && r > 0) connect_advance(W, dof, r, lane);
     uint64_t envw[SPL], selfw[SPL];
 #pragma unroll
     for (int s = 0; s < SPL; s++) {
@@ -1318,28 +1383,35 @@ __device__ __forceinline__ void narrow_edge(const EdgeParams &P, WarpScratch &W,
     }
     for (int t = lane; t < A * kRefSpheres; t += 32) (&W.rsw[0][0])[t] = P.sbounds[e * (A * kRefSpheres) + t];
     __syncwarp();
-    const int fb = narrow_segment<A, SPL>(P, W, S, L, det_tab, 0, lane, envw, selfw, cand_env, cand_self);
+    const int fb = narrow_segment<A, SPL>(P, W, S, L, det_tab, r, lane, envw, selfw, cand_env, cand_self);
     if (lane == 0) {
-        P.valid[e] = fb < 64 ? 0 : 1;
-        P.first_hit[e] = fb < 64 ? fb + 1 : -1;
+        if (fb < 64) {
+            P.valid[e] = 0;
+            P.first_hit[e] = r * g + fb + 1;
+            if (segmented) P.sdone[e] = 1;
+        } else if (!segmented || r == nseg - 1) {
+            P.valid[e] = 1;
+            P.first_hit[e] = -1;
+            if (segmented) P.sdone[e] = 1;
+        }
     }
     __syncwarp();
 }
 
-template <int A, int SPL>
+template <int A, int SPL, bool SEG>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
     broad_kernel(const __grid_constant__ EdgeParams P) {
     MRPOP_KERNEL_PROLOGUE()
     for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps)
-        broad_edge<A, SPL>(P, W, S, L, e, dof, g, lane, staged);
+        broad_edge<A, SPL, SEG>(P, W, S, L, e, dof, g, lane, staged);
 }
 
-template <int A, int SPL>
+template <int A, int SPL, bool SEG>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
     narrow_kernel(const __grid_constant__ EdgeParams P) {
     MRPOP_KERNEL_PROLOGUE()
     for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps)
-        narrow_edge<A, SPL>(P, W, S, L, det_tab, e, dof, g, lane, staged);
+        narrow_edge<A, SPL, SEG>(P, W, S, L, det_tab, e, dof, g, lane, staged);
 }
 
 // ---------------------------------------------------------------------------
@@ -1441,8 +1513,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
         const long long e = (t - B.tile_first[cur]) * kWarpsPerBlock + warp;
         const int dof = 7 * (P.single ? 1 : A);
         if (e < P.n_edges) {
-            if (NARROW) narrow_edge<A, SPL>(P, W, S, L, det_tab, e, dof, P.g, lane, staged);
-            else broad_edge<A, SPL>(P, W, S, L, e, dof, P.g, lane, staged);
+            if (NARROW) narrow_edge<A, SPL, false>(P, W, S, L, det_tab, e, dof, P.g, lane, staged);
+            else broad_edge<A, SPL, false>(P, W, S, L, e, dof, P.g, lane, staged);
         }
     }
 }

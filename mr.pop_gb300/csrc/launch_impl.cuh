@@ -6,11 +6,12 @@
 
 namespace mrpop {
 
+// seg: segment-round variant of the split kernels (segmented rules)
 template <int A, int SPL>
-const void *kernel_fn(KernelKind kind) {
+const void *kernel_fn(KernelKind kind, bool seg) {
     switch (kind) {
-    case kBroad: return (const void *)broad_kernel<A, SPL>;
-    case kNarrow: return (const void *)narrow_kernel<A, SPL>;
+    case kBroad: return seg ? (const void *)broad_kernel<A, SPL, true> : (const void *)broad_kernel<A, SPL, false>;
+    case kNarrow: return seg ? (const void *)narrow_kernel<A, SPL, true> : (const void *)narrow_kernel<A, SPL, false>;
     default: return (const void *)validate_kernel<A, SPL>;
     }
 }
@@ -24,24 +25,25 @@ const void *batch_fn(bool narrow) {
 // kernel), no more CTAs than 4-edge tiles.
 template <int A>
 cudaError_t launch_validate_impl(KernelKind kind, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream) {
-    static int max_blocks[3][3] = {};
-    static size_t max_blocks_smem[3][3] = {};
+    static int max_blocks[3][3][2] = {};
+    static size_t max_blocks_smem[3][3][2] = {};
     const int spl = p.g > 32 ? 2 : 1;
-    const void *fn = spl == 2 ? kernel_fn<A, 2>(kind) : kernel_fn<A, 1>(kind);
+    const int seg = p.rule != 0 ? 1 : 0;
+    const void *fn = spl == 2 ? kernel_fn<A, 2>(kind, seg) : kernel_fn<A, 1>(kind, seg);
     cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     if (err != cudaSuccess) return err;
-    if (max_blocks_smem[kind][spl] != smem_bytes) {
+    if (max_blocks_smem[kind][spl][seg] != smem_bytes) {
         int nb = 0;
         err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * kWarpsPerBlock, smem_bytes);
         if (err != cudaSuccess) return err;
-        max_blocks[kind][spl] = nb > 0 ? nb : 1;
-        max_blocks_smem[kind][spl] = smem_bytes;
+        max_blocks[kind][spl][seg] = nb > 0 ? nb : 1;
+        max_blocks_smem[kind][spl][seg] = smem_bytes;
     }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long need = (p.n_edges + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    long long grid = (long long)sms * max_blocks[kind][spl];
+    long long grid = (long long)sms * max_blocks[kind][spl][seg];
     if (need < grid) grid = need;
     if (grid < 1) grid = 1;
     void *args[] = {(void *)&p};

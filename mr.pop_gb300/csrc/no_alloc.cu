@@ -25,9 +25,9 @@
 namespace {
 
 // per edge: 64 samples x {env, self} flag words + {env, self} candidate masks
-// + the swept bounds of 5 arms' reference spheres
+// + the swept bounds of 5 arms' reference spheres + segment state
 constexpr size_t kNoAllocBytesPerEdge =
-    (64 * 2 + 2) * sizeof(uint64_t) + mrpop::kMaxArms * mrpop::kRefSpheres * sizeof(float4);
+    (64 * 2 + 2) * sizeof(uint64_t) + mrpop::kMaxArms * mrpop::kRefSpheres * sizeof(float4) + 2 * sizeof(int32_t);
 constexpr size_t kNoAllocBytes = (size_t)MRPOP_NOALLOC_MAX_EDGES * kNoAllocBytesPerEdge;
 
 // Host code must not use this name as a device address (on the host it is only
