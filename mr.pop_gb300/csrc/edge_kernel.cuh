@@ -409,8 +409,10 @@ static __device__ __noinline__ uint32_t env_mask_approx(const float4 *S, const S
     env_pairs(
         C.n_cub, lane, sw, sp, m,
         [&](int o, float4 u) {
+            const float4 bs = S[L.b_cub + o];
+            if (!near3(u.x, u.y, u.z, bs, u.w)) return false;
             const float4 *r = S + L.cub + 4 * o;
-            return S[L.b_cub + o].w > 1e17f || hit_cuboid(r[0], r[1], r[2], r[3], u.x, u.y, u.z, u.w * u.w);
+            return bs.w > 1e17f || hit_cuboid(r[0], r[1], r[2], r[3], u.x, u.y, u.z, u.w * u.w);
         },
         [&](int o, float x, float y, float z, float rad) {
             const float4 *r = S + L.cub + 4 * o;
@@ -419,8 +421,10 @@ static __device__ __noinline__ uint32_t env_mask_approx(const float4 *S, const S
     env_pairs(
         C.n_zcub, lane, sw, sp, m,
         [&](int o, float4 u) {
+            const float4 bs = S[L.b_zcub + o];
+            if (!near3(u.x, u.y, u.z, bs, u.w)) return false;
             const float4 *r = S + L.zcub + 4 * o;
-            return S[L.b_zcub + o].w > 1e17f || hit_zcuboid(r[0], r[1], r[2], u.x, u.y, u.z, u.w * u.w);
+            return bs.w > 1e17f || hit_zcuboid(r[0], r[1], r[2], u.x, u.y, u.z, u.w * u.w);
         },
         [&](int o, float x, float y, float z, float rad) {
             const float4 *r = S + L.zcub + 4 * o;
