@@ -103,15 +103,21 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def dist_setup():
+def dist_setup(backend: str = "nccl"):
+    """Rank, world size and local GPU from the launcher's environment; one
+    process per GPU.  backend "gloo" (CPU, tests) skips the device binding."""
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
+    if backend == "nccl":
+        torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        if backend == "nccl":
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:
+            dist.init_process_group(backend)
     return world, rank, local
 
 
@@ -122,13 +128,22 @@ def barrier(world):
 
 
 def max_over_ranks(x: float, world: int) -> float:
+    """The slowest rank's time (every rank gets it)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(units_per_rank: int, steps: int, seconds: list, world: int) -> float:
+    """Whole-job units/s of independent replicas: every rank's units over the
+    slowest rank's time (weak scaling, no data exchange)."""
+    t = max_over_ranks(sum(seconds), world)
+    return world * units_per_rank * steps / t
 
 
 def load_workload(pkg, name):
@@ -411,7 +426,7 @@ def run_mine(args, world, rank, local):
     kt = pkg.kernel_times()
     step_ms = [s.elapsed_time(e) for s, e in ev]
     t_total = max_over_ranks(sum(step_ms) / 1e3, world)
-    value = world * samples * args.steps / t_total
+    value = replica_throughput(samples, args.steps, [t_total], 1) * world
     assert scene.status() == 0, "device status word set during the bench"
 
     peak = fp32_peak(pkg, torch)
