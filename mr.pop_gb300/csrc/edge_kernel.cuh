@@ -743,7 +743,7 @@ __device__ __forceinline__ bool screen_obstacle(const float4 *S, const SceneLayo
 // group bounds are merged into one ball U (box of their centres, half
 // diagonal + group radius); obstacles are screened against U one per lane, 32
 // at a time, and each active lane tests its spheres against the survivors.
-static __device__ __noinline__ bool env_group_warp(const float4 *S, const SceneLayout &L, const SceneCounts &C,
+__device__ __forceinline__ bool env_group_warp(const float4 *S, const SceneLayout &L, const SceneCounts &C,
                                                    const Xf &T, int g, float4 gl, bool act) {
     const int lane = threadIdx.x & 31;
     const float3 gc = place_reg(T, gl);
@@ -868,7 +868,7 @@ __device__ __forceinline__ void lane_rows(int j, const EdgeParams &P, const Xf &
 // joints run as the frames stream by (the first sphere of each row is stashed
 // until its targets come).  Returns true if a test fired.
 template <int A>
-static __device__ __noinline__ bool narrow_lane(const EdgeParams &P, WarpScratch &W, const float4 *S,
+__device__ __forceinline__ bool narrow_lane(const EdgeParams &P, WarpScratch &W, const float4 *S,
                                                 const SceneLayout &L, const float4 *det_tab, int seg, int k,
                                                 uint64_t envw, uint64_t selfw, bool de, bool ds) {
     const int lane = threadIdx.x & 31;
@@ -984,8 +984,8 @@ __host__ __device__ __forceinline__ constexpr int grp_ref(int g) {
 // arm b's bound (chunks of kCrossStash) and streams arm b's surviving groups
 // against them.  Returns true if a test fired.
 template <int A>
-static __device__ __noinline__ bool cross_swept(const EdgeParams &P, WarpScratch &W, int seg, int k, uint64_t selfw,
-                                                bool act) {
+__device__ __forceinline__ bool cross_swept(const EdgeParams &P, WarpScratch &W, int seg, int k, uint64_t selfw,
+                                            bool act) {
     const int lane = threadIdx.x & 31;
     bool hit = false;
 #pragma unroll 1
@@ -1180,6 +1180,21 @@ __device__ __forceinline__ bool broad_decide(const EdgeParams &P, WarpScratch &W
     return true;
 }
 
+// Out-of-line copies for kernels that check two samples per lane (SPL = 2):
+// there the per-sample code is used twice, and one copy keeps the kernel's
+// code within the instruction cache; with one sample per lane it is inlined.
+template <int A>
+static __device__ __noinline__ bool narrow_lane_call(const EdgeParams &P, WarpScratch &W, const float4 *S,
+                                                     const SceneLayout &L, const float4 *det_tab, int seg, int k,
+                                                     uint64_t envw, uint64_t selfw, bool de, bool ds) {
+    return narrow_lane<A>(P, W, S, L, det_tab, seg, k, envw, selfw, de, ds);
+}
+template <int A>
+static __device__ __noinline__ bool cross_swept_call(const EdgeParams &P, WarpScratch &W, int seg, int k,
+                                                     uint64_t selfw, bool act) {
+    return cross_swept<A>(P, W, seg, k, selfw, act);
+}
+
 // Detailed phase of one segment: every candidate sample in parallel, one lane
 // each.  Returns the 0-based index of the first colliding sample, or 64.
 template <int A, int SPL>
@@ -1204,12 +1219,14 @@ __device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &
         // without a candidate sample keep the others company on sample
         // min(k, g), so that the warp's merged bounds stay on real samples
         const int k = bit + 1 <= P.g ? bit + 1 : P.g;
-        bool h = narrow_lane<A>(P, W, S, L, det_tab, seg, k, envw[s], selfw[s], dE, dS);
+        bool h = SPL == 1 ? narrow_lane<A>(P, W, S, L, det_tab, seg, k, envw[s], selfw[s], dE, dS)
+                          : narrow_lane_call<A>(P, W, S, L, det_tab, seg, k, envw[s], selfw[s], dE, dS);
         MRPOP_PHASE(P, 5);
         MRPOP_COUNT_LANES(14, dE || dS);
         if (A > 1 && __any_sync(kFull, dS && !h)) {
             MRPOP_COUNT_W(15, 1);
-            h |= cross_swept<A>(P, W, seg, k, selfw[s], dS && !h);
+            h |= SPL == 1 ? cross_swept<A>(P, W, seg, k, selfw[s], dS && !h)
+                          : cross_swept_call<A>(P, W, seg, k, selfw[s], dS && !h);
         }
         MRPOP_PHASE(P, 6);
         hits |= (uint64_t)__ballot_sync(kFull, h) << (32 * s);
