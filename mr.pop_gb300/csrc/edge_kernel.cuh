@@ -306,7 +306,7 @@ __device__ __forceinline__ float warp_max(float v) {
 // the box around its 32 centres, radius = half the box diagonal (+0.4 %) +
 // sphere radius + cull margin.  If the sphere touches something at any of the
 // samples, its swept bound touches it too (the margin covers FP rounding).
-static __device__ __noinline__ void fk_approx_lane(const float *base12, const WarpScratch &W, int rule, int seg,
+__device__ __forceinline__ void fk_approx_lane(const float *base12, const WarpScratch &W, int rule, int seg,
                                                    int qarm, int k, float (*dst)[3][32], int lane, float4 *swept,
                                                    float4 *rsw, bool merge) {
     float q[7];
@@ -403,7 +403,7 @@ __device__ __forceinline__ void env_pairs(int n, int lane, const float4 *sw, con
     }
 }
 
-static __device__ __noinline__ uint32_t env_mask_approx(const float4 *S, const SceneLayout &L, const SceneCounts &C,
+__device__ __forceinline__ uint32_t env_mask_approx(const float4 *S, const SceneLayout &L, const SceneCounts &C,
                                                         const float (*sp)[3][32], int lane, const float4 *sw) {
     uint32_t m = 0;
     env_pairs(
@@ -475,6 +475,20 @@ static __device__ __noinline__ bool env_hit_one(const float4 *S, const SceneLayo
     return false;
 }
 
+// Out-of-line copies for kernels with two samples per lane (the broad phase
+// runs twice per edge there, and one copy keeps the code within the
+// instruction cache); with one sample per lane the code is inlined.
+static __device__ __noinline__ void fk_approx_lane_call(const float *base12, const WarpScratch &W, int rule, int seg,
+                                                        int qarm, int k, float (*dst)[3][32], int lane,
+                                                        float4 *swept, float4 *rsw, bool merge) {
+    fk_approx_lane(base12, W, rule, seg, qarm, k, dst, lane, swept, rsw, merge);
+}
+static __device__ __noinline__ uint32_t env_mask_approx_call(const float4 *S, const SceneLayout &L,
+                                                             const SceneCounts &C, const float (*sp)[3][32],
+                                                             int lane, const float4 *sw) {
+    return env_mask_approx(S, L, C, sp, lane, sw);
+}
+
 // Broad-phase intra-arm rows (panda_multi_geometry.cuh:133-139) as 21 pairs.
 static __constant__ uint8_t c_intra_pairs[21][2] = {
     {0, 5}, {0, 6}, {0, 7}, {0, 8}, {0, 9}, {0, 10}, {1, 5}, {1, 6}, {1, 7}, {1, 8}, {1, 9},
@@ -482,7 +496,7 @@ static __constant__ uint8_t c_intra_pairs[21][2] = {
 
 // Broad phase of one sample (every lane of the warp calls it; lanes past the
 // segment's last sample evaluate sample g and discard the result).
-template <int A>
+template <int A, bool INL>
 __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W, const float4 *S,
                                              const SceneLayout &L, int seg, int k, bool merge, uint64_t &envw,
                                              uint64_t &selfw) {
@@ -496,10 +510,12 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
     for (int b = 0; b < A; b++) {
         MRPOP_PHASE_START();
         float4 *sw = W.broad.swept[b];
-        fk_approx_lane(P.base[b], W, P.rule, seg, P.single ? 0 : b, k, cur, lane, sw, W.rsw[b], merge);
+        if (INL) fk_approx_lane(P.base[b], W, P.rule, seg, P.single ? 0 : b, k, cur, lane, sw, W.rsw[b], merge);
+        else fk_approx_lane_call(P.base[b], W, P.rule, seg, P.single ? 0 : b, k, cur, lane, sw, W.rsw[b], merge);
         MRPOP_PHASE(P, 0);
         if (do_env) {
-            const uint32_t m = env_mask_approx(S, L, P.sc, cur, lane, sw);
+            const uint32_t m =
+                INL ? env_mask_approx(S, L, P.sc, cur, lane, sw) : env_mask_approx_call(S, L, P.sc, cur, lane, sw);
             uint32_t jm = 0;
 #pragma unroll
             for (int i = 1; i < kNumApprox; i++)
@@ -546,7 +562,8 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
                                                   near3(swa[i].x, swa[i].y, swa[i].z, sw[j], swa[i].w));
             }
             if (!(bal[0] | bal[1] | bal[2] | bal[3])) continue;
-            fk_approx_lane(P.base[a], W, P.rule, seg, a, k, low, lane, nullptr, nullptr, false);
+            if (INL) fk_approx_lane(P.base[a], W, P.rule, seg, a, k, low, lane, nullptr, nullptr, false);
+            else fk_approx_lane_call(P.base[a], W, P.rule, seg, a, k, low, lane, nullptr, nullptr, false);
             uint32_t am = 0;
 #pragma unroll
             for (int r = 0; r < 4; r++) {
@@ -1111,7 +1128,7 @@ __device__ __forceinline__ bool broad_decide(const EdgeParams &P, WarpScratch &W
 #pragma unroll
     for (int s = 0; s < SPL; s++) {
         const int k = lane + 1 + 32 * s;
-        broad_sample<A>(P, W, S, L, seg, k <= g ? k : g, s > 0, envw[s], selfw[s]);
+        broad_sample<A, SPL == 1>(P, W, S, L, seg, k <= g ? k : g, s > 0, envw[s], selfw[s]);
         if (k > g) envw[s] = selfw[s] = 0;
         envc[s] = flag_count(envw[s]);
         selfc[s] = flag_count(selfw[s]);
