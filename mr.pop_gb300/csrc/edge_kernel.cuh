@@ -475,20 +475,6 @@ static __device__ __noinline__ bool env_hit_one(const float4 *S, const SceneLayo
     return false;
 }
 
-// Out-of-line copies for kernels with two samples per lane (the broad phase
-// runs twice per edge there, and one copy keeps the code within the
-// instruction cache); with one sample per lane the code is inlined.
-static __device__ __noinline__ void fk_approx_lane_call(const float *base12, const WarpScratch &W, int rule, int seg,
-                                                        int qarm, int k, float (*dst)[3][32], int lane,
-                                                        float4 *swept, float4 *rsw, bool merge) {
-    fk_approx_lane(base12, W, rule, seg, qarm, k, dst, lane, swept, rsw, merge);
-}
-static __device__ __noinline__ uint32_t env_mask_approx_call(const float4 *S, const SceneLayout &L,
-                                                             const SceneCounts &C, const float (*sp)[3][32],
-                                                             int lane, const float4 *sw) {
-    return env_mask_approx(S, L, C, sp, lane, sw);
-}
-
 // Broad-phase intra-arm rows (panda_multi_geometry.cuh:133-139) as 21 pairs.
 static __constant__ uint8_t c_intra_pairs[21][2] = {
     {0, 5}, {0, 6}, {0, 7}, {0, 8}, {0, 9}, {0, 10}, {1, 5}, {1, 6}, {1, 7}, {1, 8}, {1, 9},
@@ -496,7 +482,7 @@ static __constant__ uint8_t c_intra_pairs[21][2] = {
 
 // Broad phase of one sample (every lane of the warp calls it; lanes past the
 // segment's last sample evaluate sample g and discard the result).
-template <int A, bool INL>
+template <int A>
 __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W, const float4 *S,
                                              const SceneLayout &L, int seg, int k, bool merge, uint64_t &envw,
                                              uint64_t &selfw) {
@@ -510,12 +496,10 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
     for (int b = 0; b < A; b++) {
         MRPOP_PHASE_START();
         float4 *sw = W.broad.swept[b];
-        if (INL) fk_approx_lane(P.base[b], W, P.rule, seg, P.single ? 0 : b, k, cur, lane, sw, W.rsw[b], merge);
-        else fk_approx_lane_call(P.base[b], W, P.rule, seg, P.single ? 0 : b, k, cur, lane, sw, W.rsw[b], merge);
+        fk_approx_lane(P.base[b], W, P.rule, seg, P.single ? 0 : b, k, cur, lane, sw, W.rsw[b], merge);
         MRPOP_PHASE(P, 0);
         if (do_env) {
-            const uint32_t m =
-                INL ? env_mask_approx(S, L, P.sc, cur, lane, sw) : env_mask_approx_call(S, L, P.sc, cur, lane, sw);
+            const uint32_t m = env_mask_approx(S, L, P.sc, cur, lane, sw);
             uint32_t jm = 0;
 #pragma unroll
             for (int i = 1; i < kNumApprox; i++)
@@ -562,8 +546,7 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
                                                   near3(swa[i].x, swa[i].y, swa[i].z, sw[j], swa[i].w));
             }
             if (!(bal[0] | bal[1] | bal[2] | bal[3])) continue;
-            if (INL) fk_approx_lane(P.base[a], W, P.rule, seg, a, k, low, lane, nullptr, nullptr, false);
-            else fk_approx_lane_call(P.base[a], W, P.rule, seg, a, k, low, lane, nullptr, nullptr, false);
+            fk_approx_lane(P.base[a], W, P.rule, seg, a, k, low, lane, nullptr, nullptr, false);
             uint32_t am = 0;
 #pragma unroll
             for (int r = 0; r < 4; r++) {
@@ -1125,15 +1108,28 @@ __device__ __forceinline__ bool broad_decide(const EdgeParams &P, WarpScratch &W
     MRPOP_PHASE_START();
     int envc[SPL], selfc[SPL];
     int tot_env = 0, tot_self = 0;
-#pragma unroll
+    // one copy of the per-sample code for both slots (not unrolled); slot
+    // arrays are written by constant index so they stay in registers
+#pragma unroll 1
     for (int s = 0; s < SPL; s++) {
         const int k = lane + 1 + 32 * s;
-        broad_sample<A, SPL == 1>(P, W, S, L, seg, k <= g ? k : g, s > 0, envw[s], selfw[s]);
-        if (k > g) envw[s] = selfw[s] = 0;
-        envc[s] = flag_count(envw[s]);
-        selfc[s] = flag_count(selfw[s]);
-        tot_env += envc[s];
-        tot_self += selfc[s];
+        uint64_t ew, sw;
+        broad_sample<A>(P, W, S, L, seg, k <= g ? k : g, s > 0, ew, sw);
+        if (k > g) ew = sw = 0;
+        const int ec = flag_count(ew), sc = flag_count(sw);
+        if (s == 0) {
+            envw[0] = ew;
+            selfw[0] = sw;
+            envc[0] = ec;
+            selfc[0] = sc;
+        } else {
+            envw[SPL - 1] = ew;
+            selfw[SPL - 1] = sw;
+            envc[SPL - 1] = ec;
+            selfc[SPL - 1] = sc;
+        }
+        tot_env += ec;
+        tot_self += sc;
     }
     __syncwarp();
 #pragma unroll
@@ -1197,21 +1193,6 @@ __device__ __forceinline__ bool broad_decide(const EdgeParams &P, WarpScratch &W
     return true;
 }
 
-// Out-of-line copies for kernels that check two samples per lane (SPL = 2):
-// there the per-sample code is used twice, and one copy keeps the kernel's
-// code within the instruction cache; with one sample per lane it is inlined.
-template <int A>
-static __device__ __noinline__ bool narrow_lane_call(const EdgeParams &P, WarpScratch &W, const float4 *S,
-                                                     const SceneLayout &L, const float4 *det_tab, int seg, int k,
-                                                     uint64_t envw, uint64_t selfw, bool de, bool ds) {
-    return narrow_lane<A>(P, W, S, L, det_tab, seg, k, envw, selfw, de, ds);
-}
-template <int A>
-static __device__ __noinline__ bool cross_swept_call(const EdgeParams &P, WarpScratch &W, int seg, int k,
-                                                     uint64_t selfw, bool act) {
-    return cross_swept<A>(P, W, seg, k, selfw, act);
-}
-
 // Detailed phase of one segment: every candidate sample in parallel, one lane
 // each.  Returns the 0-based index of the first colliding sample, or 64.
 template <int A, int SPL>
@@ -1228,22 +1209,22 @@ __device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &
     }
     __syncwarp();
     uint64_t hits = 0;
-#pragma unroll
+    // one copy of the per-sample code for both slots (not unrolled)
+#pragma unroll 1
     for (int s = 0; s < SPL; s++) {
         const int bit = lane + 32 * s;
         const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
+        const uint64_t ew = s == 0 ? envw[0] : envw[SPL - 1], sw = s == 0 ? selfw[0] : selfw[SPL - 1];
         // every lane walks the arms (warp-wide screening inside); lanes
         // without a candidate sample keep the others company on sample
         // min(k, g), so that the warp's merged bounds stay on real samples
         const int k = bit + 1 <= P.g ? bit + 1 : P.g;
-        bool h = SPL == 1 ? narrow_lane<A>(P, W, S, L, det_tab, seg, k, envw[s], selfw[s], dE, dS)
-                          : narrow_lane_call<A>(P, W, S, L, det_tab, seg, k, envw[s], selfw[s], dE, dS);
+        bool h = narrow_lane<A>(P, W, S, L, det_tab, seg, k, ew, sw, dE, dS);
         MRPOP_PHASE(P, 5);
         MRPOP_COUNT_LANES(14, dE || dS);
         if (A > 1 && __any_sync(kFull, dS && !h)) {
             MRPOP_COUNT_W(15, 1);
-            h |= SPL == 1 ? cross_swept<A>(P, W, seg, k, selfw[s], dS && !h)
-                          : cross_swept_call<A>(P, W, seg, k, selfw[s], dS && !h);
+            h |= cross_swept<A>(P, W, seg, k, sw, dS && !h);
         }
         MRPOP_PHASE(P, 6);
         hits |= (uint64_t)__ballot_sync(kFull, h) << (32 * s);
