@@ -168,10 +168,6 @@ struct WarpScratch {
                 float cstash[kCrossStash][4][32];    // arm-vs-arm candidates {x, y, z, r}
             };
         } lanes;
-        struct {
-            float T[kMaxArms][kNumJoints][12];
-            float4 P[kMaxArms][kNumDet];     // detailed sphere centres (w = radius)
-        } coop;
     };
 };
 
@@ -447,32 +443,6 @@ __device__ __forceinline__ uint32_t env_mask_approx(const float4 *S, const Scene
             return hit_sphere_sphere(c0.x, c0.y, c0.z, c0.w, x, y, z, rad);
         });
     return m;
-}
-
-// One sphere against the whole scene (narrow phase), with per-obstacle bounds.
-static __device__ __noinline__ bool env_hit_one(const float4 *S, const SceneLayout &L, const SceneCounts &C, float x,
-                                                float y, float z, float r) {
-    const float rsq = __fmul_rn(r, r);
-    for (int o = 0; o < C.n_cub; o++)
-        if (near3(x, y, z, S[L.b_cub + o], r) &&
-            hit_cuboid(S[L.cub + 4 * o], S[L.cub + 4 * o + 1], S[L.cub + 4 * o + 2], S[L.cub + 4 * o + 3], x, y, z,
-                       rsq))
-            return true;
-    for (int o = 0; o < C.n_zcub; o++)
-        if (near3(x, y, z, S[L.b_zcub + o], r) &&
-            hit_zcuboid(S[L.zcub + 4 * o], S[L.zcub + 4 * o + 1], S[L.zcub + 4 * o + 2], x, y, z, rsq))
-            return true;
-    for (int o = 0; o < C.n_cap; o++)
-        if (near3(x, y, z, S[L.b_cap + o], r) && hit_capsule(S[L.cap + 2 * o], S[L.cap + 2 * o + 1], x, y, z, r))
-            return true;
-    for (int o = 0; o < C.n_zcap; o++)
-        if (near3(x, y, z, S[L.b_zcap + o], r) && hit_zcapsule(S[L.zcap + 2 * o], S[L.zcap + 2 * o + 1], x, y, z, r))
-            return true;
-    for (int o = 0; o < C.n_sph; o++) {
-        const float4 c0 = S[L.sph + o];
-        if (near3(x, y, z, S[L.b_sph + o], r) && hit_sphere_sphere(c0.x, c0.y, c0.z, c0.w, x, y, z, r)) return true;
-    }
-    return false;
 }
 
 // Broad-phase intra-arm rows (panda_multi_geometry.cuh:133-139) as 21 pairs.
