@@ -26,7 +26,7 @@
 namespace mrpop {
 
 #ifndef MRPOP_MIN_BLOCKS
-#define MRPOP_MIN_BLOCKS 4
+#define MRPOP_MIN_BLOCKS 3
 #endif
 // Optional per-phase warp timers (development builds with
 // -DMRPOP_PHASE_TIMERS; compiled out otherwise): clock64() deltas of lane 0
@@ -69,7 +69,7 @@ static __device__ unsigned long long *g_dev_phase;
 #define MRPOP_COUNT(P, i, v) do { } while (0)
 #endif
 
-constexpr int kWarpsPerBlock = 4;
+constexpr int kWarpsPerBlock = 6;
 constexpr int kMaxArms = 5;
 constexpr int kMaxDof = 7 * kMaxArms;
 constexpr int kCrossStash = 16;        // per-lane arm-vs-arm candidate spheres

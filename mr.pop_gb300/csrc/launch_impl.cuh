@@ -22,7 +22,7 @@ const void *batch_fn(bool narrow) {
 }
 
 // Persistent grid: SMs x resident CTAs at this shared-memory size (cached per
-// kernel), no more CTAs than 4-edge tiles.
+// kernel), no more CTAs than tiles of kWarpsPerBlock edges.
 template <int A>
 cudaError_t launch_validate_impl(KernelKind kind, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream) {
     static int max_blocks[3][3][2] = {};
