@@ -370,43 +370,54 @@ __device__ __forceinline__ void fk_approx_lane(const float *base12, const WarpSc
 // ---------------------------------------------------------------------------
 // broad phase: approx spheres 1..10 of one arm (lane column `lane` of sp)
 // against the scene.  Returns a bitmask over sphere index (bit i = sphere i
-// of this lane's sample touches some obstacle).  The (sphere, obstacle) pairs
-// of each obstacle class are screened lane-parallel, one pair per lane, with
-// the sphere's swept bound (sw) against the obstacle: the exact test of the
-// class for cuboids with orthonormal axes, the obstacle's bounding sphere for
-// the other classes (both conservative).  Exact per-sample tests then run,
-// for the whole warp, only for the pairs that survive.
+// of this lane's sample touches some obstacle).  The obstacles of each class
+// are screened one per lane against the 10 spheres' swept bounds (sw, shared
+// by the warp): the obstacle's bounding sphere, then for cuboids with
+// orthonormal axes the exact sphere-cuboid test (both conservative; for
+// spheres the record is its own bound).  Exact per-sample tests then run, for
+// the whole warp, only for the (sphere, obstacle) pairs that survive.
 // ---------------------------------------------------------------------------
-template <typename PreFn, typename ExactFn>
-__device__ __forceinline__ void env_pairs(int n, int lane, const float4 *sw, const float (*sp)[3][32], uint32_t &m,
-                                          PreFn pre, ExactFn exact) {
-    const int pairs = n * (kNumApprox - 1);
+template <typename BoundFn, typename RefineFn, typename ExactFn>
+__device__ __forceinline__ void env_class(int n, int lane, const float4 *sw, const float (*sp)[3][32], uint32_t &m,
+                                          BoundFn bound, RefineFn refine, ExactFn exact) {
 #pragma unroll 1
-    for (int t0 = 0; t0 < pairs; t0 += 32) {
-        const int t = t0 + lane;
-        bool c = false;
-        if (t < pairs) {
-            const int o = t / (kNumApprox - 1);
-            c = pre(o, sw[t - (kNumApprox - 1) * o + 1]);
+    for (int o0 = 0; o0 < n; o0 += 32) {
+        // one obstacle per lane: which swept sphere bounds reach it
+        const int o = o0 + lane;
+        uint32_t cand = 0;
+        if (o < n) {
+            const float4 bs = bound(o);
+#pragma unroll
+            for (int i = 1; i < kNumApprox; i++) {
+                const float4 u = sw[i];
+                if (near3(u.x, u.y, u.z, bs, u.w)) cand |= 1u << i;
+            }
+            for (uint32_t c = cand; c; c &= c - 1) {
+                const int i = __ffs(c) - 1;
+                if (!refine(o, bs, sw[i])) cand &= ~(1u << i);
+            }
         }
-        uint32_t bal = __ballot_sync(kFull, c);
-        while (bal) {
-            const int tt = t0 + __ffs(bal) - 1;
-            bal &= bal - 1;
-            const int o = tt / (kNumApprox - 1), i = tt - (kNumApprox - 1) * o + 1;
-            if (exact(o, sp[i][0][lane], sp[i][1][lane], sp[i][2][lane], c_approx[i].w)) m |= 1u << i;
+        // exact per-sample tests of the surviving (sphere, obstacle) pairs
+        uint32_t obal = __ballot_sync(kFull, cand != 0);
+        while (obal) {
+            const int src = __ffs(obal) - 1;
+            obal &= obal - 1;
+            uint32_t cm = __shfl_sync(kFull, cand, src);
+            while (cm) {
+                const int i = __ffs(cm) - 1;
+                cm &= cm - 1;
+                if (exact(o0 + src, sp[i][0][lane], sp[i][1][lane], sp[i][2][lane], c_approx[i].w)) m |= 1u << i;
+            }
         }
     }
 }
 
 __device__ __forceinline__ uint32_t env_mask_approx(const float4 *S, const SceneLayout &L, const SceneCounts &C,
-                                                        const float (*sp)[3][32], int lane, const float4 *sw) {
+                                                    const float (*sp)[3][32], int lane, const float4 *sw) {
     uint32_t m = 0;
-    env_pairs(
-        C.n_cub, lane, sw, sp, m,
-        [&](int o, float4 u) {
-            const float4 bs = S[L.b_cub + o];
-            if (!near3(u.x, u.y, u.z, bs, u.w)) return false;
+    env_class(
+        C.n_cub, lane, sw, sp, m, [&](int o) { return S[L.b_cub + o]; },
+        [&](int o, float4 bs, float4 u) {
             const float4 *r = S + L.cub + 4 * o;
             return bs.w > 1e17f || hit_cuboid(r[0], r[1], r[2], r[3], u.x, u.y, u.z, u.w * u.w);
         },
@@ -414,11 +425,9 @@ __device__ __forceinline__ uint32_t env_mask_approx(const float4 *S, const Scene
             const float4 *r = S + L.cub + 4 * o;
             return hit_cuboid(r[0], r[1], r[2], r[3], x, y, z, __fmul_rn(rad, rad));
         });
-    env_pairs(
-        C.n_zcub, lane, sw, sp, m,
-        [&](int o, float4 u) {
-            const float4 bs = S[L.b_zcub + o];
-            if (!near3(u.x, u.y, u.z, bs, u.w)) return false;
+    env_class(
+        C.n_zcub, lane, sw, sp, m, [&](int o) { return S[L.b_zcub + o]; },
+        [&](int o, float4 bs, float4 u) {
             const float4 *r = S + L.zcub + 4 * o;
             return bs.w > 1e17f || hit_zcuboid(r[0], r[1], r[2], u.x, u.y, u.z, u.w * u.w);
         },
@@ -426,18 +435,18 @@ __device__ __forceinline__ uint32_t env_mask_approx(const float4 *S, const Scene
             const float4 *r = S + L.zcub + 4 * o;
             return hit_zcuboid(r[0], r[1], r[2], x, y, z, __fmul_rn(rad, rad));
         });
-    env_pairs(
-        C.n_cap, lane, sw, sp, m, [&](int o, float4 u) { return near3(u.x, u.y, u.z, S[L.b_cap + o], u.w); },
+    env_class(
+        C.n_cap, lane, sw, sp, m, [&](int o) { return S[L.b_cap + o]; }, [&](int, float4, float4) { return true; },
         [&](int o, float x, float y, float z, float rad) {
             return hit_capsule(S[L.cap + 2 * o], S[L.cap + 2 * o + 1], x, y, z, rad);
         });
-    env_pairs(
-        C.n_zcap, lane, sw, sp, m, [&](int o, float4 u) { return near3(u.x, u.y, u.z, S[L.b_zcap + o], u.w); },
+    env_class(
+        C.n_zcap, lane, sw, sp, m, [&](int o) { return S[L.b_zcap + o]; }, [&](int, float4, float4) { return true; },
         [&](int o, float x, float y, float z, float rad) {
             return hit_zcapsule(S[L.zcap + 2 * o], S[L.zcap + 2 * o + 1], x, y, z, rad);
         });
-    env_pairs(
-        C.n_sph, lane, sw, sp, m, [&](int o, float4 u) { return near3(u.x, u.y, u.z, S[L.sph + o], u.w); },
+    env_class(
+        C.n_sph, lane, sw, sp, m, [&](int o) { return S[L.sph + o]; }, [&](int, float4, float4) { return true; },
         [&](int o, float x, float y, float z, float rad) {
             const float4 c0 = S[L.sph + o];
             return hit_sphere_sphere(c0.x, c0.y, c0.z, c0.w, x, y, z, rad);
