@@ -287,3 +287,41 @@ def test_forearm_hand_rows_near_contact(cuda, pkg, orc):
             ref = orc.validate(sc, bases, qa0, qa1, 32, flags, arm=a, trig=trig)
             assert np.array_equal(got[0], ref["valid"]) and np.array_equal(got[1], ref["first_hit"])
     assert fired > 0
+
+
+def test_concurrent_host_threads(cuda, pkg):
+    """Several host threads validating at once, each on its own stream with its
+    own scene size (different shared-memory sizes), give the sequential results."""
+    import threading
+    W = pkg.workloads
+    jobs = []
+    for k, wl in enumerate([W.config1(n_edges=512, seed=21), W.config2(n_edges=512, seed=22),
+                            W.config3(n_edges=256, seed=23), W.config2(n_edges=300, seed=24)]):
+        scene = pkg.Scene(wl.scene)
+        rb = pkg.RobotSet(len(wl.bases), wl.bases)
+        q0, q1 = cuda.from_numpy(wl.q0).cuda(), cuda.from_numpy(wl.q1).cuda()
+        ref = pkg.validate(scene, rb, q0, q1, wl.granularity, wl.flags, wl.arm)
+        cuda.cuda.synchronize()
+        jobs.append((scene, rb, q0, q1, wl, [r.cpu().numpy() for r in ref]))
+    errors = []
+
+    def work(job):
+        scene, rb, q0, q1, wl, ref = job
+        s = cuda.cuda.Stream()
+        try:
+            for _ in range(20):
+                with cuda.cuda.stream(s):
+                    v, f = pkg.validate(scene, rb, q0, q1, wl.granularity, wl.flags, wl.arm, stream=s)
+                s.synchronize()
+                if not (np.array_equal(v.cpu().numpy(), ref[0]) and np.array_equal(f.cpu().numpy(), ref[1])):
+                    errors.append(wl.name)
+                    return
+        except Exception as e:  # noqa: BLE001 - reported below
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=work, args=(j,)) for j in jobs]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
