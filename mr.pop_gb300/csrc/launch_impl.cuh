@@ -8,6 +8,61 @@
 
 namespace mrpop {
 
+namespace {
+
+// Per-kernel launch state of this translation unit (internal linkage, so that
+// two builds of the library loaded into one process never share it): the
+// largest dynamic shared-memory size the kernel's attribute allows, and the
+// resident CTAs per SM at the last size asked.  Guarded by launch_mu.
+struct LaunchState {
+    const void *fn = nullptr;
+    size_t attr_bytes = 0;
+    size_t occ_bytes = 0;
+    int occ_blocks = 0;
+};
+std::mutex launch_mu;
+LaunchState launch_states[64];
+
+LaunchState *launch_state(const void *fn) {
+    for (LaunchState &s : launch_states) {
+        if (s.fn == fn) return &s;
+        if (!s.fn) {
+            s.fn = fn;
+            return &s;
+        }
+    }
+    return nullptr;
+}
+
+// Raises the kernel's dynamic shared-memory attribute to smem_bytes if it is
+// lower (it only grows, so launches racing on other threads stay valid), and
+// returns the resident CTAs per SM at that size when blocks_per_sm is given.
+cudaError_t prepare_kernel(const void *fn, size_t smem_bytes, int *blocks_per_sm) {
+    std::lock_guard<std::mutex> lk(launch_mu);
+    LaunchState *st = launch_state(fn);
+    if (!st || smem_bytes > st->attr_bytes) {
+        const cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+        if (err != cudaSuccess) return err;
+        if (st) st->attr_bytes = smem_bytes;
+    }
+    if (!blocks_per_sm) return cudaSuccess;
+    if (!st || st->occ_bytes != smem_bytes || st->occ_blocks == 0) {
+        int nb = 0;
+        const cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * kWarpsPerBlock, smem_bytes);
+        if (err != cudaSuccess) return err;
+        *blocks_per_sm = nb > 0 ? nb : 1;
+        if (st) {
+            st->occ_blocks = *blocks_per_sm;
+            st->occ_bytes = smem_bytes;
+        }
+        return cudaSuccess;
+    }
+    *blocks_per_sm = st->occ_blocks;
+    return cudaSuccess;
+}
+
+}  // namespace
+
 // seg: segment-round variant of the split kernels (segmented rules)
 template <int A, int SPL>
 const void *kernel_fn(KernelKind kind, bool seg) {
@@ -23,35 +78,16 @@ const void *batch_fn(bool narrow) {
     return narrow ? (const void *)batch_kernel<A, SPL, true> : (const void *)batch_kernel<A, SPL, false>;
 }
 
-// Persistent grid: SMs x resident CTAs at this shared-memory size (cached per
-// kernel), no more CTAs than tiles of kWarpsPerBlock edges.  The kernel's
-// shared-memory attribute only grows, so a launch racing with another host
-// thread's never finds it below its own size; the cache is guarded.
+// Persistent grid: SMs x resident CTAs at this shared-memory size, no more
+// CTAs than tiles of kWarpsPerBlock edges.
 template <int A>
 cudaError_t launch_validate_impl(KernelKind kind, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream) {
-    static std::mutex mu;
-    static int max_blocks[3][3][2] = {};
-    static size_t max_blocks_smem[3][3][2] = {};
-    static size_t set_bytes[3][3][2] = {};
     const int spl = p.g > 32 ? 2 : 1;
-    const int seg = p.rule != 0 ? 1 : 0;
+    const bool seg = p.rule != 0;
     const void *fn = spl == 2 ? kernel_fn<A, 2>(kind, seg) : kernel_fn<A, 1>(kind, seg);
-    std::unique_lock<std::mutex> lk(mu);
-    cudaError_t err = cudaSuccess;
-    if (smem_bytes > set_bytes[kind][spl][seg]) {
-        err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
-        if (err != cudaSuccess) return err;
-        set_bytes[kind][spl][seg] = smem_bytes;
-    }
-    if (max_blocks_smem[kind][spl][seg] != smem_bytes) {
-        int nb = 0;
-        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * kWarpsPerBlock, smem_bytes);
-        if (err != cudaSuccess) return err;
-        max_blocks[kind][spl][seg] = nb > 0 ? nb : 1;
-        max_blocks_smem[kind][spl][seg] = smem_bytes;
-    }
-    const int per_sm = max_blocks[kind][spl][seg];
-    lk.unlock();
+    int per_sm = 0;
+    const cudaError_t err = prepare_kernel(fn, smem_bytes, &per_sm);
+    if (err != cudaSuccess) return err;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -63,21 +99,12 @@ cudaError_t launch_validate_impl(KernelKind kind, const EdgeParams &p, size_t sm
     return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(32 * kWarpsPerBlock), args, smem_bytes, stream);
 }
 
-// Batch kernels: the shared-memory attribute is raised (never lowered) when a
-// batch is created, so every batch created so far stays launchable; launches
-// themselves (and graph capture) do not touch it.
+// Batch kernels: the attribute is raised when a batch is created, so launches
+// (and graph capture) do not touch it.
 template <int A>
 cudaError_t batch_occupancy_impl(bool narrow, int spl, size_t smem_bytes, int *blocks_per_sm) {
-    static std::mutex mu;
-    static size_t set_bytes[2][3] = {};
     const void *fn = spl == 2 ? batch_fn<A, 2>(narrow) : batch_fn<A, 1>(narrow);
-    std::lock_guard<std::mutex> lk(mu);
-    if (smem_bytes > set_bytes[narrow][spl]) {
-        const cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
-        if (err != cudaSuccess) return err;
-        set_bytes[narrow][spl] = smem_bytes;
-    }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, 32 * kWarpsPerBlock, smem_bytes);
+    return prepare_kernel(fn, smem_bytes, blocks_per_sm);
 }
 
 template <int A>
