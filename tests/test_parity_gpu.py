@@ -225,6 +225,20 @@ def test_host_buffer_path_equals_device_path(cuda, pkg, wls):
     assert np.array_equal(v, dev[0]) and np.array_equal(f, dev[1])
 
 
+def test_host_buffer_path_large_batches(cuda, pkg):
+    """Full-size batches through the host-buffer path give the device-path
+    results, plain and segmented, on a reused workspace."""
+    W = pkg.workloads
+    for wl in (W.config2(n_edges=70001, seed=41), W.config3_shortcuts(n_paths=1100, pairs=64, seed=42)):
+        scene = pkg.Scene(wl.scene)
+        rb = pkg.RobotSet(len(wl.bases), wl.bases)
+        dev = _run(cuda, pkg, scene, rb, wl)
+        ws = pkg.Workspace()
+        for _ in range(2):  # the workspace's buffers are reused
+            v, f = ws.validate(scene, rb, wl.q0, wl.q1, wl.granularity, wl.flags, wl.arm, wl.rule, wl.range_)
+            assert np.array_equal(v, dev[0]) and np.array_equal(f, dev[1])
+
+
 def test_full_size_properties(cuda, pkg, orc):
     """Config 2 at its full size (65536 edges x 32): repeatability, batch-order and
     chunking invariance, and oracle agreement on a random subset."""
