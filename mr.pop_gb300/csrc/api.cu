@@ -460,9 +460,12 @@ mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots,
     return MRPOP_OK;
 }
 
+// 16 bytes of work counters, then per edge: flag words, candidate masks,
+// reference-sphere bounds and segment state.
 size_t split_scratch_bytes(int64_t n_edges, int g, int A) {
     const int spl = g > 32 ? 2 : 1;
-    return (size_t)n_edges * (32 * spl * 2 * sizeof(uint64_t) + 2 * sizeof(uint64_t) + A * kRefSpheres * sizeof(float4) +
+    return 2 * sizeof(unsigned long long) +
+           (size_t)n_edges * (32 * spl * 2 * sizeof(uint64_t) + 2 * sizeof(uint64_t) + A * kRefSpheres * sizeof(float4) +
                               2 * sizeof(int32_t));
 }
 
@@ -471,7 +474,8 @@ void set_split_scratch(EdgeParams &p, void *scratch, int64_t n_edges, int g, int
     const size_t flag_bytes = (size_t)n_edges * 32 * spl * 2 * sizeof(uint64_t);
     const size_t mask_bytes = (size_t)n_edges * 2 * sizeof(uint64_t);
     const size_t bound_bytes = (size_t)n_edges * A * kRefSpheres * sizeof(float4);
-    char *b = (char *)scratch;
+    p.work = (unsigned long long *)scratch;
+    char *b = (char *)scratch + 2 * sizeof(unsigned long long);
     p.sflags = (uint64_t *)b;
     p.smasks = (uint64_t *)(b + flag_bytes);
     p.sbounds = (float4 *)(b + flag_bytes + mask_bytes);
@@ -521,7 +525,8 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
         const int rounds = rule == MRPOP_RULE_PLAIN ? 1 : kSegRounds;
         for (int r = 0; r < rounds && err == cudaSuccess; r++) {
             p.seg0 = r;
-            err = timed_launch(A, kBroad, p, smem, stream);
+            err = cudaMemsetAsync(p.work, 0, 2 * sizeof(unsigned long long), stream);
+            if (err == cudaSuccess) err = timed_launch(A, kBroad, p, smem, stream);
             if (err == cudaSuccess) err = timed_launch(A, kNarrow, p, smem, stream);
         }
         if (err == cudaSuccess && rule != MRPOP_RULE_PLAIN) {

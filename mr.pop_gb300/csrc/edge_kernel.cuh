@@ -137,6 +137,7 @@ struct EdgeParams {
     float4 *sbounds;            // split pipeline: per-edge swept reference-sphere bounds [A][kRefSpheres]
     int32_t *snseg;             // segmented rules: per-edge segment count (-1: too many), from segment 0
     int32_t *sdone;             // segmented rules: per-edge verdict written
+    unsigned long long *work;   // split kernels: next-edge counters {broad, narrow}, zero before each launch
     float gofs[11];             // sub-group g: |group centre - reference sphere centre| + group radius
     float4 grp[11];             // detailed sub-group bounds in their joint frame (+margin)
     const uint32_t *row5;       // forearm-hand rows table (kRow5N6 x kRow5N7 bits), or nullptr
@@ -1396,11 +1397,21 @@ __device__ __forceinline__ void narrow_edge(const EdgeParams &P, WarpScratch &W,
     __syncwarp();
 }
 
+// Next edge for this warp: a shared counter handed out one edge at a time, so
+// that warps whose edges finish early take more (edge costs vary by orders of
+// magnitude: an edge without candidates skips the narrow phase entirely).
+__device__ __forceinline__ long long next_edge(unsigned long long *counter, int lane) {
+    unsigned long long e = 0;
+    if (lane == 0) e = atomicAdd(counter, 1ull);
+    return (long long)__shfl_sync(kFull, e, 0);
+}
+
 template <int A, int SPL, bool SEG>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
     broad_kernel(const __grid_constant__ EdgeParams P) {
     MRPOP_KERNEL_PROLOGUE()
-    for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps)
+    (void)nwarps;
+    for (long long e = next_edge(P.work, lane); e < P.n_edges; e = next_edge(P.work, lane))
         broad_edge<A, SPL, SEG>(P, W, S, L, e, dof, g, lane, staged);
 }
 
@@ -1408,7 +1419,8 @@ template <int A, int SPL, bool SEG>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
     narrow_kernel(const __grid_constant__ EdgeParams P) {
     MRPOP_KERNEL_PROLOGUE()
-    for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps)
+    (void)nwarps;
+    for (long long e = next_edge(P.work + 1, lane); e < P.n_edges; e = next_edge(P.work + 1, lane))
         narrow_edge<A, SPL, SEG>(P, W, S, L, det_tab, e, dof, g, lane, staged);
 }
 

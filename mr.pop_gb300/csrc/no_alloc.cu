@@ -28,7 +28,7 @@ namespace {
 // + the swept bounds of 5 arms' reference spheres + segment state
 constexpr size_t kNoAllocBytesPerEdge =
     (64 * 2 + 2) * sizeof(uint64_t) + mrpop::kMaxArms * mrpop::kRefSpheres * sizeof(float4) + 2 * sizeof(int32_t);
-constexpr size_t kNoAllocBytes = (size_t)MRPOP_NOALLOC_MAX_EDGES * kNoAllocBytesPerEdge;
+constexpr size_t kNoAllocBytes = 2 * sizeof(unsigned long long) + (size_t)MRPOP_NOALLOC_MAX_EDGES * kNoAllocBytesPerEdge;
 
 // Host code must not use this name as a device address (on the host it is only
 // a stand-in); the device address comes from cudaGetSymbolAddress below.
