@@ -4,10 +4,11 @@
 //
 // Instances are grouped by (arm count, samples per lane), the template
 // parameters of the kernels.  Each group gets a device array of parameter
-// blocks and a tile table (kWarpsPerBlock edges per tile, instances in order);
-// batch_kernel<A, SPL, NARROW> walks contiguous tile ranges per CTA.  A run is
-// every group's broad launch, then every group's narrow launch; the captured
-// graph runs each group's pair on its own branch so small groups overlap.
+// blocks, a chunk table (up to kChunkEdges edges of one instance per chunk,
+// instances in order) and two work counters; batch_kernel<A, SPL, NARROW>
+// hands chunks to CTAs and edges to warps.  A run is every group's counter
+// reset, broad launch and narrow launch; the captured graph runs each group on
+// its own branch so small groups overlap.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -22,8 +23,9 @@ struct mrpop_batch {
         int arms = 0, spl = 1;
         int64_t n_items = 0;
         mrpop::EdgeParams *d_items = nullptr;
-        long long *d_tiles = nullptr;
-        long long n_tiles = 0;
+        int4 *d_chunks = nullptr;
+        int n_chunks = 0;
+        unsigned long long *d_work = nullptr;  // {broad, narrow} chunk counters
         size_t smem = 0;
         int grid[2] = {0, 0};      // CTAs of the broad / narrow launch
         int max_grid[2] = {0, 0};  // SMs x resident CTAs
@@ -37,6 +39,8 @@ struct mrpop_batch {
 
 namespace {
 
+constexpr int kChunkEdges = 96;
+
 mrpop_status cuda_status(cudaError_t e, const char *what) {
     return mrpop::fail_status(MRPOP_ERR_CUDA, (std::string(what) + ": " + cudaGetErrorString(e)).c_str());
 }
@@ -44,7 +48,8 @@ mrpop_status cuda_status(cudaError_t e, const char *what) {
 void release(mrpop_batch *b) {
     for (auto &g : b->groups) {
         cudaFree(g.d_items);
-        cudaFree(g.d_tiles);
+        cudaFree(g.d_chunks);
+        cudaFree(g.d_work);
     }
     cudaFree(b->d_scratch);
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -52,17 +57,20 @@ void release(mrpop_batch *b) {
     delete b;
 }
 
-mrpop::BatchParams params_of(const mrpop_batch::Group &g) {
+mrpop::BatchParams params_of(const mrpop_batch::Group &g, bool narrow) {
     mrpop::BatchParams p;
     p.items = g.d_items;
-    p.tile_first = g.d_tiles;
-    p.n_items = (int)g.n_items;
-    p.n_tiles = g.n_tiles;
+    p.chunks = g.d_chunks;
+    p.n_chunks = g.n_chunks;
+    p.work = g.d_work + (narrow ? 1 : 0);
     return p;
 }
 
+// One kernel of a group: its chunk counter is zeroed first (in stream order).
 cudaError_t launch_group(const mrpop_batch::Group &g, bool narrow, int grid, cudaStream_t s) {
-    return mrpop::launch_batch(g.arms, narrow, g.spl, params_of(g), g.smem, grid, s);
+    cudaError_t err = cudaMemsetAsync(g.d_work + (narrow ? 1 : 0), 0, sizeof(unsigned long long), s);
+    if (err == cudaSuccess) err = mrpop::launch_batch(g.arms, narrow, g.spl, params_of(g, narrow), g.smem, grid, s);
+    return err;
 }
 
 }  // namespace
@@ -121,27 +129,34 @@ mrpop_status mrpop_batch_create(const mrpop_batch_item *items, int64_t n_items, 
             g.arms = arms;
             g.spl = spl;
             std::vector<mrpop::EdgeParams> ps;
-            std::vector<long long> tiles(1, 0);
+            std::vector<int4> chunks;
             for (const Entry &e : ent) {
                 if (e.arms != arms || e.spl != spl) continue;
+                if (e.p.n_edges > INT32_MAX) {
+                    release(b);
+                    return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_create: an item has 2^31 edges or more");
+                }
+                const int item = (int)ps.size();
+                for (int64_t e0 = 0; e0 < e.p.n_edges; e0 += kChunkEdges)
+                    chunks.push_back(make_int4(item, (int)e0, (int)std::min<int64_t>(kChunkEdges, e.p.n_edges - e0), 0));
                 ps.push_back(e.p);
-                tiles.push_back(tiles.back() + (e.p.n_edges + mrpop::kWarpsPerBlock - 1) / mrpop::kWarpsPerBlock);
                 g.smem = std::max(g.smem, e.smem);
             }
             if (ps.empty()) continue;
             g.n_items = (int64_t)ps.size();
-            g.n_tiles = tiles.back();
+            g.n_chunks = (int)chunks.size();
             err = cudaMalloc(&g.d_items, ps.size() * sizeof(mrpop::EdgeParams));
-            if (err == cudaSuccess) err = cudaMalloc(&g.d_tiles, tiles.size() * sizeof(long long));
+            if (err == cudaSuccess) err = cudaMalloc(&g.d_chunks, chunks.size() * sizeof(int4));
+            if (err == cudaSuccess) err = cudaMalloc(&g.d_work, 2 * sizeof(unsigned long long));
             if (err == cudaSuccess)
                 err = cudaMemcpy(g.d_items, ps.data(), ps.size() * sizeof(mrpop::EdgeParams), cudaMemcpyHostToDevice);
             if (err == cudaSuccess)
-                err = cudaMemcpy(g.d_tiles, tiles.data(), tiles.size() * sizeof(long long), cudaMemcpyHostToDevice);
+                err = cudaMemcpy(g.d_chunks, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice);
             for (int k = 0; k < 2 && err == cudaSuccess; k++) {
                 int nb = 0;
                 err = mrpop::batch_occupancy(arms, k == 1, spl, g.smem, &nb);
                 const long long cap = (long long)sms * std::max(nb, 1);
-                g.max_grid[k] = (int)std::max(1LL, std::min(cap, g.n_tiles));
+                g.max_grid[k] = (int)std::max(1LL, std::min<long long>(cap, g.n_chunks));
                 g.grid[k] = g.max_grid[k];
             }
             b->groups.push_back(g);
@@ -167,7 +182,7 @@ mrpop_status mrpop_batch_run(mrpop_batch *b, void *stream) {
 }
 
 // Launch-shape tuner: per group and kernel, the grid (CTAs; multiples of the
-// SM count up to the resident maximum, and the tile count) with the shortest
+// SM count up to the resident maximum, and the chunk count) with the shortest
 // device time over three runs.  Broad launches are tuned first (the narrow
 // kernel reads their output).  Synchronous; not for use during capture.
 mrpop_status mrpop_batch_tune(mrpop_batch *b, void *stream) {

@@ -1428,25 +1428,27 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
 // batch kernels: many independent instances (each with its own scene, arm
 // layout, edges, granularity and outputs; one EdgeParams each, all of arm
 // count A and samples-per-lane SPL) in one persistent launch.  An instance's
-// edges form tiles of kWarpsPerBlock edges (one per warp); the tiles of all
-// instances are numbered in instance order and each CTA walks one contiguous
-// range of them, so it changes instance -- copying the instance's parameters
-// to shared memory and restaging its scene with the bulk-copy engine -- only
-// at instance boundaries.
+// edges form chunks; CTAs take chunks from a counter, in instance order, and
+// copy the instance's parameters to shared memory and restage its scene with
+// the bulk-copy engine when the instance changes; the CTA's warps then take
+// the chunk's edges one at a time.
 // ---------------------------------------------------------------------------
 struct BatchParams {
-    const EdgeParams *items;    // device array, one per instance
-    const long long *tile_first; // [n_items + 1]: first tile of each instance
-    int n_items;
-    long long n_tiles;
+    const EdgeParams *items;      // device array, one per instance
+    const int4 *chunks;           // {instance, first edge, edge count, -}, instances in order
+    int n_chunks;
+    unsigned long long *work;     // next-chunk counter, zero before each launch
 };
 
 // One bulk copy of `bytes` from global to shared memory, completed on `bar`
-// in phase `parity`; bounded wait.  Every thread of the CTA calls it; returns
-// false (for the whole CTA) if the copy did not complete in time.
+// in phase `parity`; bounded wait.  Every thread of the CTA calls it after a
+// barrier that follows its last read of `dst`; the proxy fence orders those
+// reads before the copy's writes.  Returns false (for the whole CTA) if the
+// copy did not complete in time.
 __device__ __forceinline__ bool stage_bulk(float4 *dst, const float4 *src, uint32_t bytes, uint64_t *bar,
                                            uint32_t parity, unsigned int *status) {
     if (threadIdx.x == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                      : "memory");
         asm volatile(
@@ -1485,26 +1487,23 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    const long long t0 = B.n_tiles * blockIdx.x / gridDim.x, t1 = B.n_tiles * (blockIdx.x + 1) / gridDim.x;
-    // instance of the first tile (binary search; then a forward cursor)
-    int cur = 0;
-    {
-        int lo = 0, hi = B.n_items - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (B.tile_first[mid] <= t0) lo = mid;
-            else hi = mid - 1;
-        }
-        cur = lo;
-    }
+    __shared__ int s_chunk;
+    __shared__ unsigned int s_next;
     int item = -1;
     uint32_t parity = 0;
     bool staged = false;
-    for (long long t = t0; t < t1; t++) {
-        while (B.tile_first[cur + 1] <= t) cur++;
-        if (cur != item) {
-            __syncthreads(); // every warp is done with the previous instance
-            const uint32_t *src = reinterpret_cast<const uint32_t *>(B.items + cur);
+    for (;;) {
+        // the CTA takes the next chunk of one instance's edges ...
+        if (threadIdx.x == 0) {
+            s_chunk = (int)atomicAdd(B.work, 1ull);
+            s_next = 0;
+        }
+        __syncthreads();
+        const int c = s_chunk;
+        if (c >= B.n_chunks) break;
+        const int4 ch = B.chunks[c];
+        if (ch.x != item) {
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(B.items + ch.x);
             uint32_t *dst = reinterpret_cast<uint32_t *>(&Ps);
             for (int i = threadIdx.x; i < (int)(sizeof(EdgeParams) / 4); i += blockDim.x) dst[i] = src[i];
             __syncthreads();
@@ -1514,18 +1513,24 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
                 staged = stage_bulk(reinterpret_cast<float4 *>(smem_raw), Ps.scene, bytes, &bar, parity, Ps.status);
                 parity ^= 1u;
             }
-            item = cur;
+            item = ch.x;
         }
         const EdgeParams &P = Ps;
         const SceneLayout L = scene_layout(P.sc);
         const float4 *S = reinterpret_cast<const float4 *>(smem_raw);
         WarpScratch &W = reinterpret_cast<WarpScratch *>(smem_raw + (size_t)L.total * sizeof(float4))[warp];
-        const long long e = (t - B.tile_first[cur]) * kWarpsPerBlock + warp;
         const int dof = 7 * (P.single ? 1 : A);
-        if (e < P.n_edges) {
+        // ... and its warps take the chunk's edges one at a time
+        for (;;) {
+            unsigned int k = 0;
+            if (lane == 0) k = atomicAdd(&s_next, 1u);
+            k = __shfl_sync(kFull, k, 0);
+            if ((int)k >= ch.z) break;
+            const long long e = (long long)ch.y + k;
             if (NARROW) narrow_edge<A, SPL, false>(P, W, S, L, det_tab, e, dof, P.g, lane, staged);
             else broad_edge<A, SPL, false>(P, W, S, L, e, dof, P.g, lane, staged);
         }
+        __syncthreads(); // every warp is done with this chunk (and instance)
     }
 }
 
