@@ -208,6 +208,9 @@ mrpop_status mrpop_fk_spheres(const mrpop_robotset *robots, int arm, const float
  * branch) and mrpop_batch_launch launches that graph on `stream`.
  * mrpop_batch_info reports, per group, {arms, samples per lane, broad grid,
  * narrow grid} into grids[4 * i ..] for up to max_groups groups.
+ * A batch's staged scratch and work counters serve every run of it, so runs
+ * and graph launches of one batch must be ordered (one stream, or events
+ * between streams); different batches are independent.
  */
 typedef struct mrpop_batch_item {
     const mrpop_scene *scene;
