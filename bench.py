@@ -219,11 +219,13 @@ def committed_profile(kernel: str, workload: str) -> dict:
     return {}
 
 
-def roofline(kt: dict, flops: dict, peak: float, workload: str, arms: int, spl: int, steps: int) -> dict:
+def roofline(kt: dict, flops: dict, peak: float, workload: str, arms: int, spl: int, steps: int,
+             sm_mhz: float | None = None) -> dict:
     """Roofline of the kernel with the largest share of device time.
     kt: {kind: (launches, total ms)} from the library's event timing over
     `steps` steps; flops: algorithmic flops per step of each kind (a kind may
-    launch more than once per step: segment rounds)."""
+    launch more than once per step: segment rounds); sm_mhz: the median SM
+    clock sampled over the timed region (for the issue-rate figure)."""
     ran = {k: v for k, v in kt.items() if v[0] > 0}
     total_ms = sum(v[1] for v in ran.values())
     dom = max(ran, key=lambda k: ran[k][1])
@@ -250,6 +252,17 @@ def roofline(kt: dict, flops: dict, peak: float, workload: str, arms: int, spl: 
         out["executed"] = {"achieved": ex, "frac": ex / peak,
                            "basis": "FP32 flops the kernel executed (ncu: 2*ffma + fadd + fmul thread "
                                     "instructions) / live launch time; culling skips algorithmic work"}
+    if prof.get("warp_instructions") and sm_mhz:
+        # every SM has four schedulers that issue at most one warp instruction per clock
+        import torch
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        rate = prof["warp_instructions"] / launch_s
+        cap = 4 * sms * sm_mhz * 1e6
+        out["issue"] = {"achieved": rate, "peak": cap, "unit": "warp instructions/s", "frac": rate / cap,
+                        "basis": "warp instructions of one launch (ncu smsp__inst_executed.sum, committed profile) / "
+                                 "live launch time, against 4 schedulers x SMs x the median SM clock sampled "
+                                 "in the timed region: the kernel is bound by instruction issue and latency, "
+                                 "not by FP32 throughput or HBM"}
     out["kernels"] = {KERNEL_NAMES[k]: {"launches": v[0], "avg_ms": v[1] / v[0], "share": v[1] / total_ms,
                                         "algorithmic_tflops": flops[k] / (v[1] / steps / 1e3) / 1e12}
                       for k, v in ran.items()}
@@ -438,7 +451,7 @@ def run_mine(args, world, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
         "config": workload_config(wl, {"parallelism": f"replica x{world}, independent edge batches"}),
         "gpu_launches": sum(v[0] for v in kt.values()),
-        "roofline": roofline(kt, flops, peak, args.workload, arms, spl, args.steps),
+        "roofline": roofline(kt, flops, peak, args.workload, arms, spl, args.steps, (clk or {}).get("sm_mhz")),
         "clocks": clk,
     }
     if not args.no_e2e:
