@@ -100,3 +100,31 @@ def test_batch_rejects_bad_items(cuda, pkg):
     bad[1] = (scene, rb, q0, q1, 65, flags, arm)
     with pytest.raises(pkg.MrpopError, match="item 1"):
         pkg.Batch(bad)
+
+
+def test_batch_chunk_boundaries(cuda, pkg):
+    """One group (4 arms, g = 32) whose instances end just before, at and just
+    after the 96-edge chunks, with the scene changing between neighbours, so
+    that CTAs restage scenes between chunks of different instances."""
+    W = pkg.workloads
+    rng = np.random.default_rng(11)
+    bases = W.bases_facing_centre(4, 0.71)
+    rb = pkg.RobotSet(4, bases)
+    scenes = [pkg.Scene(W.scene_config1(3)), pkg.Scene(W.scene_config2(4))]
+    items = []
+    for k, n in enumerate([1, 95, 96, 97, 191, 192, 193, 2, 288, 1]):
+        a0, a1 = W.random_edges(rng, n, 4, 1.5)
+        items.append((scenes[k % 2], rb, cuda.from_numpy(a0).cuda(), cuda.from_numpy(a1).cuda(), 32,
+                      pkg.CHECK_ENV | pkg.CHECK_SELF, -1))
+    ref = _reference(pkg, cuda, items)
+    b = pkg.Batch(items)
+    assert len(b.info()) == 1
+    for _ in range(2):  # a second run starts from re-zeroed chunk counters
+        for v, f in zip(b.valid, b.first_hit):
+            v.fill_(7)
+            f.fill_(-9)
+        b.run()
+        cuda.cuda.synchronize()
+        _check(b, ref)
+    for s in scenes:
+        assert s.status() == 0
