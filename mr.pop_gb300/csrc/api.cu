@@ -452,6 +452,25 @@ mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots,
         const double ox = cx - ref.x, oy = cy - ref.y, oz = cz - ref.z;
         p.gofs[gi] = (float)(std::sqrt(ox * ox + oy * oy + oz * oz) * 1.001 + r * 1.001 + kCullMargin);
     }
+    // the hand group's three parts (bits of hand_part over spheres kHandFirst..)
+    for (int s = 0; s < kHandParts; s++) {
+        double lo[3] = {1e9, 1e9, 1e9}, hi[3] = {-1e9, -1e9, -1e9};
+        for (uint32_t m = hand_part(s); m; m &= m - 1) {
+            const SphereDef &d = kDet[kHandFirst + __builtin_ctz(m)];
+            const double v[3] = {d.x, d.y, d.z};
+            for (int c = 0; c < 3; c++) {
+                lo[c] = std::fmin(lo[c], v[c]);
+                hi[c] = std::fmax(hi[c], v[c]);
+            }
+        }
+        const double cx = 0.5 * (lo[0] + hi[0]), cy = 0.5 * (lo[1] + hi[1]), cz = 0.5 * (lo[2] + hi[2]);
+        double r = 0.0;
+        for (uint32_t m = hand_part(s); m; m &= m - 1) {
+            const SphereDef &d = kDet[kHandFirst + __builtin_ctz(m)];
+            r = std::fmax(r, std::sqrt((d.x - cx) * (d.x - cx) + (d.y - cy) * (d.y - cy) + (d.z - cz) * (d.z - cz)) + d.r);
+        }
+        p.hsub[s] = make_float4((float)cx, (float)cy, (float)cz, (float)(r * 1.001 + kCullMargin));
+    }
     A = arm >= 0 ? 1 : robots->n_arms;
     for (int a = 0; a < A; a++)
         for (int i = 0; i < 12; i++) p.base[a][i] = robots->base[arm >= 0 ? arm : a][i];

@@ -140,6 +140,7 @@ struct EdgeParams {
     unsigned long long *work;   // split kernels: next-edge counters {broad, narrow}, zero before each launch
     float gofs[11];             // sub-group g: |group centre - reference sphere centre| + group radius
     float4 grp[11];             // detailed sub-group bounds in their joint frame (+margin)
+    float4 hsub[3];             // bounds of the hand group's three parts in the joint-7 frame (+margin)
     const uint32_t *row5;       // forearm-hand rows table (kRow5N6 x kRow5N7 bits), or nullptr
     float base[kMaxArms][12];   // row-major 3x4 per arm of this check
 };
@@ -675,6 +676,16 @@ __host__ __device__ __forceinline__ constexpr int grp_first(int g) {
 __host__ __device__ __forceinline__ constexpr int jgrp_first(int j) {
     return j < 5 ? j : j == 5 ? 5 : j == 6 ? 8 : j == 7 ? 9 : 11;
 }
+// The hand group (spheres 37..58: a 6 x 3 grid along the gripper's diagonal
+// plus four finger-tip spheres) is screened in three parts along the diagonal:
+// the two columns and finger tips on each side, and the two middle columns.
+// Bits are sphere index - kHandFirst; EdgeParams::hsub holds each part's bound.
+constexpr int kHandGroup = 10;
+constexpr int kHandFirst = 37;
+constexpr int kHandParts = 3;
+__host__ __device__ __forceinline__ constexpr uint32_t hand_part(int s) {
+    return s == 0 ? 0x3030C3u : s == 1 ? 0x00C30Cu : 0x0F0C30u;
+}
 
 // Exact env test of one sphere against obstacle o (index over all classes in
 // the bound order cuboids, z-cuboids, capsules, z-capsules, spheres).
@@ -795,6 +806,7 @@ __device__ __forceinline__ void lane_env(int j, const EdgeParams &P, const Xf &T
     }
 }
 
+template <int A>
 __device__ __forceinline__ void lane_rows(int j, const EdgeParams &P, const Xf &T, LaneCtx &c, WarpScratch &W,
                                           const float4 *det_tab, int lane) {
     if (c.hit || !c.rm) return;
@@ -823,15 +835,45 @@ __device__ __forceinline__ void lane_rows(int j, const EdgeParams &P, const Xf &
         }
         if (!nr) continue;
         bool h = false;
-        for (int i = grp_first(g); i < grp_first(g + 1); i++) {
-            const float4 sd = c_det[i];
-            const float3 p = place_reg(T, sd);
-            uint32_t m = nr;
-            while (m) {
-                const int r = __ffs(m) - 1;
-                m &= m - 1;
-                h |= hit_sphere_sphere(W.lanes.stash[r][0][lane], W.lanes.stash[r][1][lane],
-                                       W.lanes.stash[r][2][lane], det_tab[det_row_first(r)].w, p.x, p.y, p.z, sd.w);
+        if (A == 1 && g == kHandGroup) {
+            // single-arm form: the hand's parts screened per row first, then
+            // their spheres (in the composite forms the extra screens cost
+            // more than they save)
+#pragma unroll 1
+            for (int s = 0; s < kHandParts; s++) {
+                const float4 sl = P.hsub[s];
+                const float3 sc = place_reg(T, sl);
+                uint32_t ns = 0;
+                for (uint32_t m = nr; m; m &= m - 1) {
+                    const int r = __ffs(m) - 1;
+                    if (near3(W.lanes.stash[r][0][lane], W.lanes.stash[r][1][lane], W.lanes.stash[r][2][lane],
+                              make_float4(sc.x, sc.y, sc.z, sl.w), det_tab[det_row_first(r)].w))
+                        ns |= 1u << r;
+                }
+                if (!ns) continue;
+                for (uint32_t pm = hand_part(s); pm; pm &= pm - 1) {
+                    const float4 sd = c_det[kHandFirst + __ffs(pm) - 1];
+                    const float3 p = place_reg(T, sd);
+                    for (uint32_t m = ns; m; m &= m - 1) {
+                        const int r = __ffs(m) - 1;
+                        h |= hit_sphere_sphere(W.lanes.stash[r][0][lane], W.lanes.stash[r][1][lane],
+                                               W.lanes.stash[r][2][lane], det_tab[det_row_first(r)].w, p.x, p.y,
+                                               p.z, sd.w);
+                    }
+                }
+            }
+        } else {
+            for (int i = grp_first(g); i < grp_first(g + 1); i++) {
+                const float4 sd = c_det[i];
+                const float3 p = place_reg(T, sd);
+                uint32_t m = nr;
+                while (m) {
+                    const int r = __ffs(m) - 1;
+                    m &= m - 1;
+                    h |= hit_sphere_sphere(W.lanes.stash[r][0][lane], W.lanes.stash[r][1][lane],
+                                           W.lanes.stash[r][2][lane], det_tab[det_row_first(r)].w, p.x, p.y, p.z,
+                                           sd.w);
+                }
             }
         }
         if (h) {
@@ -876,7 +918,7 @@ __device__ __forceinline__ bool narrow_lane(const EdgeParams &P, WarpScratch &W,
             MRPOP_PHASE(P, 8);
             lane_env(j, P, T, c, S, L);
             MRPOP_PHASE(P, 9);
-            lane_rows(j, P, T, c, W, det_tab, lane);
+            lane_rows<A>(j, P, T, c, W, det_tab, lane);
             MRPOP_PHASE(P, 10);
         }
     }
