@@ -472,7 +472,8 @@ def run_mine(args, world, rank, local):
         dt = max_over_ranks(time.perf_counter() - t, world)
         out["e2e"] = {"value": world * samples * args.steps / dt, "unit": UNIT,
                       "h2d_bytes_per_step": int(a0.nbytes + a1.nbytes), "d2h_bytes_per_step": int(av.nbytes + af.nbytes),
-                      "path": "mrpop_validate_edges_host (pinned host buffers, copies and sync inside)"}
+                      "path": "mrpop_validate_edges_host with pinned host buffers, which the kernels read "
+                              "(endpoints) and write (verdicts) in place over NVLink-C2C; sync inside"}
         assert np.array_equal(av, valid.cpu().numpy())
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as orc

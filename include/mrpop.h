@@ -168,9 +168,12 @@ mrpop_status mrpop_validate_edges_noalloc(const mrpop_scene *scene, const mrpop_
 
 /*
  * Host-buffer form for callers without device memory (the reference's host
- * API, dRRT::solve in Planners.hh:57-64, hands host arrays across): copies
- * q0/q1 from host memory, validates, copies valid/first_hit back and waits.
- * The workspace owns pinned staging and device buffers and grows on demand.
+ * API, dRRT::solve in Planners.hh:57-64, hands host arrays across): validates
+ * q0/q1 in host memory, writes valid/first_hit there and waits.  When all four
+ * buffers are page-locked (cudaHostAlloc, cudaHostRegister, a pinned tensor)
+ * the kernels read and write them in place (over NVLink-C2C on a Grace host);
+ * otherwise the call copies through the workspace's device buffers, which
+ * grow on demand.  A workspace belongs to one host thread.
  */
 mrpop_status mrpop_workspace_create(mrpop_workspace **out);
 mrpop_status mrpop_workspace_destroy(mrpop_workspace *ws);

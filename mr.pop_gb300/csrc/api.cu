@@ -781,6 +781,17 @@ mrpop_status mrpop_workspace_destroy(mrpop_workspace *ws) {
     return MRPOP_OK;
 }
 
+// Device address of a page-locked host buffer (mapped into the GPU's address
+// space), or nullptr for any other memory.
+static void *mapped_host(const void *h) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 mrpop_status mrpop_validate_edges_host(mrpop_workspace *ws, const mrpop_scene *scene, const mrpop_robotset *robots,
                                        const float *q0, const float *q1, int64_t n_edges, int granularity,
                                        uint32_t flags, int arm, int rule, float range, uint8_t *valid,
@@ -791,6 +802,21 @@ mrpop_status mrpop_validate_edges_host(mrpop_workspace *ws, const mrpop_scene *s
         return fail(MRPOP_ERR_INVALID_ARGUMENT, "validate_edges_host: null host pointer");
     const int dof = 7 * (arm >= 0 ? 1 : robots->n_arms);
     const size_t ncfg = (size_t)n_edges * dof;
+    // Page-locked host buffers are used in place: the kernels read the
+    // endpoints from host memory and write the verdicts there (over NVLink-C2C
+    // on a Grace host), so no staging copy precedes or follows them.  Other
+    // buffers go through the workspace's device arrays.
+    const float *m_q0 = static_cast<const float *>(mapped_host(q0));
+    const float *m_q1 = static_cast<const float *>(mapped_host(q1));
+    uint8_t *m_valid = static_cast<uint8_t *>(mapped_host(valid));
+    int32_t *m_first = static_cast<int32_t *>(mapped_host(first_hit));
+    if (m_q0 && m_q1 && m_valid && m_first) {
+        mrpop_status s = mrpop::run_validator(scene, robots, m_q0, m_q1, n_edges, granularity, rule, range, flags,
+                                              arm, m_valid, m_first, nullptr, nullptr, ws->stream, nullptr);
+        if (s != MRPOP_OK) return s;
+        MRPOP_CUDA(cudaStreamSynchronize(ws->stream), "validate_edges_host: sync");
+        return MRPOP_OK;
+    }
     if (ncfg > ws->cap_cfg) {
         cudaFree(ws->d_q0);
         cudaFree(ws->d_q1);

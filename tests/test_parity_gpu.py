@@ -239,6 +239,28 @@ def test_host_buffer_path_large_batches(cuda, pkg):
             assert np.array_equal(v, dev[0]) and np.array_equal(f, dev[1])
 
 
+def test_host_buffer_path_pinned_in_place(cuda, pkg):
+    """Page-locked host buffers are used in place (the kernels read the
+    endpoints and write the verdicts in host memory): same results as the
+    device path, plain and segmented, and with only some buffers pinned (those
+    calls take the copying path)."""
+    W = pkg.workloads
+    for wl in (W.config2(n_edges=9001, seed=43), W.config3_shortcuts(n_paths=200, pairs=64, seed=44)):
+        scene = pkg.Scene(wl.scene)
+        rb = pkg.RobotSet(len(wl.bases), wl.bases)
+        dev = _run(cuda, pkg, scene, rb, wl)
+        n = len(wl.q0)
+        pinned = [cuda.from_numpy(wl.q0).pin_memory(), cuda.from_numpy(wl.q1).pin_memory(),
+                  cuda.full((n,), 7, dtype=cuda.uint8).pin_memory(), cuda.full((n,), -9, dtype=cuda.int32).pin_memory()]
+        a0, a1, av, af = (t.numpy() for t in pinned)
+        ws = pkg.Workspace()
+        for outs in ((av, af), (None, None)):
+            v, f = ws.validate(scene, rb, a0, a1, wl.granularity, wl.flags, wl.arm, wl.rule, wl.range_,
+                               valid=outs[0], first_hit=outs[1])
+            assert np.array_equal(v, dev[0]) and np.array_equal(f, dev[1])
+        assert np.array_equal(av, dev[0]) and np.array_equal(af, dev[1])
+
+
 def test_full_size_properties(cuda, pkg, orc):
     """Config 2 at its full size (65536 edges x 32): repeatability, batch-order and
     chunking invariance, and oracle agreement on a random subset."""
