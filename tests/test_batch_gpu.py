@@ -128,3 +128,21 @@ def test_batch_chunk_boundaries(cuda, pkg):
         _check(b, ref)
     for s in scenes:
         assert s.status() == 0
+
+
+def test_batch_items_in_page_locked_host_memory(cuda, pkg):
+    """Items whose endpoints and outputs are page-locked host buffers are read
+    and written in place by the batch kernels: same verdicts as device items."""
+    items = _instances(pkg, cuda, 16, 0.05, seed=5)
+    ref = _reference(pkg, cuda, items)
+    host = []
+    for scene, rb, q0, q1, g, flags, arm in items:
+        n = q0.shape[0]
+        host.append((scene, rb, q0.cpu().pin_memory(), q1.cpu().pin_memory(), g, flags, arm,
+                     cuda.full((n,), 7, dtype=cuda.uint8).pin_memory(),
+                     cuda.full((n,), -9, dtype=cuda.int32).pin_memory()))
+    b = pkg.Batch(host)
+    b.capture()
+    b.launch()
+    cuda.cuda.synchronize()
+    _check(b, ref)
