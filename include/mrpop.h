@@ -196,9 +196,11 @@ mrpop_status mrpop_fk_spheres(const mrpop_robotset *robots, int arm, const float
  * Batched validation of many independent planning instances (single-segment
  * edges; no counterpart in the reference, whose planner validates one edge per
  * 256-thread block).  Each item is one mrpop_validate_edges call: its scene,
- * robot set, device endpoints [n_edges][7 * arms], granularity, check flags,
- * arm selection and device outputs; the items may differ in all of them.
- * Results equal the per-item calls bit for bit.
+ * robot set, endpoints [n_edges][7 * arms], granularity, check flags, arm
+ * selection and outputs; the items may differ in all of them.  Endpoints and
+ * outputs may live in device memory or in page-locked host memory, which the
+ * kernels read and write in place.  Results equal the per-item calls bit for
+ * bit.
  *
  * mrpop_batch_create checks every item, allocates the device scratch and the
  * per-group parameter tables (groups = arm count x (g <= 32 or not)), and
