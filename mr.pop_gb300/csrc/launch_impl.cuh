@@ -79,7 +79,7 @@ const void *batch_fn(bool narrow) {
 }
 
 // Persistent grid: SMs x resident CTAs at this shared-memory size, no more
-// CTAs than tiles of kWarpsPerBlock edges.
+// CTAs than edges / kWarpsPerBlock.
 template <int A>
 cudaError_t launch_validate_impl(KernelKind kind, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream) {
     const int spl = p.g > 32 ? 2 : 1;
