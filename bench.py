@@ -382,7 +382,7 @@ def run_batch(args, world, rank, local, pkg, torch):
                    "edges": int(eoffs[-1]), "samples": samples, "arms_histogram_1_to_5": arms_hist,
                    "granularities": sorted({wl.granularity for wl in insts}),
                    "kernel_groups": [{"arms": a, "samples_per_lane": s, "broad_grid": gb, "narrow_grid": gn}
-                                     for a, s, gb, gn in groups],
+                                     for a, s, _, gb, gn in groups],
                    "launch": "one CUDA graph of the batch kernels (tuned grids)",
                    "per_instance_plain_calls_value": loop_value,
                    "l2": "flushed (256 MiB write) before every step",

@@ -193,26 +193,31 @@ mrpop_status mrpop_fk_spheres(const mrpop_robotset *robots, int arm, const float
                               int detailed, float *out, void *stream);
 
 /*
- * Batched validation of many independent planning instances (single-segment
- * edges; no counterpart in the reference, whose planner validates one edge per
- * 256-thread block).  Each item is one mrpop_validate_edges call: its scene,
- * robot set, endpoints [n_edges][7 * arms], granularity, check flags, arm
- * selection and outputs; the items may differ in all of them.  Endpoints and
- * outputs may live in device memory or in page-locked host memory, which the
- * kernels read and write in place.  Results equal the per-item calls bit for
- * bit.
+ * Batched validation of many independent planning instances (no counterpart
+ * in the reference, whose planner validates one edge per 256-thread block).
+ * Each item is one mrpop_validate_edges call (rule MRPOP_RULE_PLAIN) or one
+ * mrpop_validate_segments call without segment counts (connect, B-spline or
+ * shortcut rule with its range): its scene, robot set, endpoints
+ * [n_edges][7 * arms], granularity, check flags, arm selection, rule and
+ * outputs; the items may differ in all of them.  Endpoints and outputs may
+ * live in device memory or in page-locked host memory, which the kernels read
+ * and write in place.  Results equal the per-item calls bit for bit.
  *
  * mrpop_batch_create checks every item, allocates the device scratch and the
- * per-group parameter tables (groups = arm count x (g <= 32 or not)), and
- * keeps the item pointers: their buffers must outlive the batch.
- * mrpop_batch_run launches one persistent broad-phase and one narrow-phase
- * kernel per group on `stream`; it allocates nothing and reads the inputs as
- * they are at execution time, so a batch can be rerun on refilled buffers.
- * mrpop_batch_tune picks each launch's grid by timing (synchronous).
+ * per-group parameter tables (groups = arm count x (g <= 32 or not) x
+ * (segmented or not)), and keeps the item pointers: their buffers must outlive
+ * the batch.
+ * mrpop_batch_run launches, per group on `stream`, one persistent broad-phase
+ * and one narrow-phase kernel; a segmented group runs them in rounds (one
+ * segment of every undecided edge per round) and then one fused kernel for the
+ * edges with segments left.  It allocates nothing and reads the inputs as they
+ * are at execution time, so a batch can be rerun on refilled buffers.
+ * mrpop_batch_tune picks each group's broad and narrow grids by timing
+ * (synchronous).
  * mrpop_batch_capture records one run as a CUDA graph (each group on its own
  * branch) and mrpop_batch_launch launches that graph on `stream`.
- * mrpop_batch_info reports, per group, {arms, samples per lane, broad grid,
- * narrow grid} into grids[4 * i ..] for up to max_groups groups.
+ * mrpop_batch_info reports, per group, {arms, samples per lane, segmented,
+ * broad grid, narrow grid} into grids[5 * i ..] for up to max_groups groups.
  * A batch's staged scratch and work counters serve every run of it, so runs
  * and graph launches of one batch must be ordered (one stream, or events
  * between streams); different batches are independent.
@@ -228,6 +233,8 @@ typedef struct mrpop_batch_item {
     int32_t arm;
     uint8_t *valid;
     int32_t *first_hit;
+    int32_t rule;  /* MRPOP_RULE_*; zero-initialised items are single-segment */
+    float range;   /* segment length for the segmented rules (> 0) */
 } mrpop_batch_item;
 
 typedef struct mrpop_batch mrpop_batch;

@@ -615,25 +615,25 @@ __global__ void trig_kernel(const float *x, long long n, float *c, float *s) {
 }  // namespace
 
 namespace mrpop {
-cudaError_t batch_occupancy(int arms, bool narrow, int spl, size_t smem_bytes, int *blocks_per_sm) {
+cudaError_t batch_occupancy(int arms, int mode, bool seg, int spl, size_t smem_bytes, int *blocks_per_sm) {
     switch (arms) {
-    case 1: return batch_occupancy_arms<1>(narrow, spl, smem_bytes, blocks_per_sm);
-    case 2: return batch_occupancy_arms<2>(narrow, spl, smem_bytes, blocks_per_sm);
-    case 3: return batch_occupancy_arms<3>(narrow, spl, smem_bytes, blocks_per_sm);
-    case 4: return batch_occupancy_arms<4>(narrow, spl, smem_bytes, blocks_per_sm);
-    case 5: return batch_occupancy_arms<5>(narrow, spl, smem_bytes, blocks_per_sm);
+    case 1: return batch_occupancy_arms<1>(mode, seg, spl, smem_bytes, blocks_per_sm);
+    case 2: return batch_occupancy_arms<2>(mode, seg, spl, smem_bytes, blocks_per_sm);
+    case 3: return batch_occupancy_arms<3>(mode, seg, spl, smem_bytes, blocks_per_sm);
+    case 4: return batch_occupancy_arms<4>(mode, seg, spl, smem_bytes, blocks_per_sm);
+    case 5: return batch_occupancy_arms<5>(mode, seg, spl, smem_bytes, blocks_per_sm);
     default: return cudaErrorInvalidValue;
     }
 }
 
-cudaError_t launch_batch(int arms, bool narrow, int spl, const BatchParams &b, size_t smem_bytes, int grid,
+cudaError_t launch_batch(int arms, int mode, bool seg, int spl, const BatchParams &b, size_t smem_bytes, int grid,
                          cudaStream_t stream) {
     switch (arms) {
-    case 1: return launch_batch_arms<1>(narrow, spl, b, smem_bytes, grid, stream);
-    case 2: return launch_batch_arms<2>(narrow, spl, b, smem_bytes, grid, stream);
-    case 3: return launch_batch_arms<3>(narrow, spl, b, smem_bytes, grid, stream);
-    case 4: return launch_batch_arms<4>(narrow, spl, b, smem_bytes, grid, stream);
-    case 5: return launch_batch_arms<5>(narrow, spl, b, smem_bytes, grid, stream);
+    case 1: return launch_batch_arms<1>(mode, seg, spl, b, smem_bytes, grid, stream);
+    case 2: return launch_batch_arms<2>(mode, seg, spl, b, smem_bytes, grid, stream);
+    case 3: return launch_batch_arms<3>(mode, seg, spl, b, smem_bytes, grid, stream);
+    case 4: return launch_batch_arms<4>(mode, seg, spl, b, smem_bytes, grid, stream);
+    case 5: return launch_batch_arms<5>(mode, seg, spl, b, smem_bytes, grid, stream);
     default: return cudaErrorInvalidValue;
     }
 }

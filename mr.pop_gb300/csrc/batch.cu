@@ -1,14 +1,16 @@
-// batch.cu -- many independent single-segment validate calls (planning
-// instances of different arm counts, edge counts, granularities and scenes)
-// in one persistent launch per kernel variant, replayable as one CUDA graph.
+// batch.cu -- many independent validate calls (planning instances of
+// different arm counts, edge counts, granularities, scenes and segmentation
+// rules) in one persistent launch per kernel variant and round, replayable as
+// one CUDA graph.
 //
-// Instances are grouped by (arm count, samples per lane), the template
-// parameters of the kernels.  Each group gets a device array of parameter
-// blocks, a chunk table (up to kChunkEdges edges of one instance per chunk,
-// instances in order) and two work counters; batch_kernel<A, SPL, NARROW>
-// hands chunks to CTAs and edges to warps.  A run is every group's counter
-// reset, broad launch and narrow launch; the captured graph runs each group on
-// its own branch so small groups overlap.
+// Instances are grouped by (arm count, samples per lane, segmented), the
+// template parameters of the kernels.  Each group gets a device array of
+// parameter blocks, a chunk table (up to kChunkEdges edges of one instance per
+// chunk, instances in order) and work counters; batch_kernel<A, SPL, MODE,
+// SEG> hands chunks to CTAs and edges to warps.  A group's run is a broad and
+// a narrow launch (each after its counter reset); a segmented group runs them
+// for kSegRounds rounds and then the fused kernel.  The captured graph runs
+// each group on its own branch so small groups overlap.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -21,14 +23,15 @@
 struct mrpop_batch {
     struct Group {
         int arms = 0, spl = 1;
+        bool seg = false;  // segmented instances (connect, B-spline, shortcut)
         int64_t n_items = 0;
         mrpop::EdgeParams *d_items = nullptr;
         int4 *d_chunks = nullptr;
         int n_chunks = 0;
-        unsigned long long *d_work = nullptr;  // {broad, narrow} chunk counters
+        unsigned long long *d_work = nullptr;  // chunk counters of the broad, narrow and fused launches
         size_t smem = 0;
-        int grid[2] = {0, 0};      // CTAs of the broad / narrow launch
-        int max_grid[2] = {0, 0};  // SMs x resident CTAs
+        int grid[3] = {0, 0, 0};      // CTAs of the broad / narrow / fused launch
+        int max_grid[3] = {0, 0, 0};  // SMs x resident CTAs, at most the chunk count
     };
     int device = 0;
     std::vector<Group> groups;
@@ -57,19 +60,31 @@ void release(mrpop_batch *b) {
     delete b;
 }
 
-mrpop::BatchParams params_of(const mrpop_batch::Group &g, bool narrow) {
+// One kernel of a group (mode kBatchBroad / kBatchNarrow / kBatchFused; seg0:
+// the round, or the first segment of the fused launch): its chunk counter is
+// zeroed first (in stream order).
+cudaError_t launch_group(const mrpop_batch::Group &g, int mode, int grid, int seg0, cudaStream_t s) {
     mrpop::BatchParams p;
     p.items = g.d_items;
     p.chunks = g.d_chunks;
     p.n_chunks = g.n_chunks;
-    p.work = g.d_work + (narrow ? 1 : 0);
-    return p;
+    p.seg0 = seg0;
+    p.work = g.d_work + mode;
+    cudaError_t err = cudaMemsetAsync(p.work, 0, sizeof(unsigned long long), s);
+    if (err == cudaSuccess) err = mrpop::launch_batch(g.arms, mode, g.seg, g.spl, p, g.smem, grid, s);
+    return err;
 }
 
-// One kernel of a group: its chunk counter is zeroed first (in stream order).
-cudaError_t launch_group(const mrpop_batch::Group &g, bool narrow, int grid, cudaStream_t s) {
-    cudaError_t err = cudaMemsetAsync(g.d_work + (narrow ? 1 : 0), 0, sizeof(unsigned long long), s);
-    if (err == cudaSuccess) err = mrpop::launch_batch(g.arms, narrow, g.spl, params_of(g, narrow), g.smem, grid, s);
+// A group's whole run: broad and narrow, in segment rounds for a segmented
+// group, then the fused kernel for the edges with segments left.
+cudaError_t run_group(const mrpop_batch::Group &g, cudaStream_t s) {
+    cudaError_t err = cudaSuccess;
+    const int rounds = g.seg ? mrpop::kSegRounds : 1;
+    for (int r = 0; r < rounds && err == cudaSuccess; r++) {
+        err = launch_group(g, mrpop::kBatchBroad, g.grid[0], r, s);
+        if (err == cudaSuccess) err = launch_group(g, mrpop::kBatchNarrow, g.grid[1], r, s);
+    }
+    if (err == cudaSuccess && g.seg) err = launch_group(g, mrpop::kBatchFused, g.grid[2], mrpop::kSegRounds, s);
     return err;
 }
 
@@ -92,6 +107,7 @@ mrpop_status mrpop_batch_create(const mrpop_batch_item *items, int64_t n_items, 
     struct Entry {
         mrpop::EdgeParams p;
         int arms, spl;
+        bool seg;
         size_t smem, scratch;
     };
     std::vector<Entry> ent;
@@ -100,7 +116,7 @@ mrpop_status mrpop_batch_create(const mrpop_batch_item *items, int64_t n_items, 
         const mrpop_batch_item &it = items[i];
         Entry e;
         const mrpop_status st =
-            mrpop::make_params(it.scene, it.robots, it.q0, it.q1, it.n_edges, it.granularity, MRPOP_RULE_PLAIN, 0.0f,
+            mrpop::make_params(it.scene, it.robots, it.q0, it.q1, it.n_edges, it.granularity, it.rule, it.range,
                                it.flags, it.arm, it.valid, it.first_hit, nullptr, nullptr, e.p, e.arms, e.smem);
         if (st != MRPOP_OK) {
             release(b);
@@ -108,6 +124,7 @@ mrpop_status mrpop_batch_create(const mrpop_batch_item *items, int64_t n_items, 
         }
         if (it.n_edges == 0) continue;
         e.spl = it.granularity > 32 ? 2 : 1;
+        e.seg = it.rule != MRPOP_RULE_PLAIN;
         e.scratch = (mrpop::split_scratch_bytes(it.n_edges, it.granularity, e.arms) + 255) & ~(size_t)255;
         scratch_total += e.scratch;
         ent.push_back(e);
@@ -123,15 +140,18 @@ mrpop_status mrpop_batch_create(const mrpop_batch_item *items, int64_t n_items, 
         mrpop::set_split_scratch(e.p, (char *)b->d_scratch + off, e.p.n_edges, e.p.g, e.arms);
         off += e.scratch;
     }
-    for (int arms = 1; arms <= MRPOP_MAX_ARMS; arms++) {
-        for (int spl = 1; spl <= 2; spl++) {
+    for (int key = 0; key < 4 * MRPOP_MAX_ARMS; key++) {
+        {
+            const int arms = 1 + key / 4, spl = 1 + key % 2;
+            const bool seg = (key / 2) % 2 == 1;
             mrpop_batch::Group g;
             g.arms = arms;
             g.spl = spl;
+            g.seg = seg;
             std::vector<mrpop::EdgeParams> ps;
             std::vector<int4> chunks;
             for (const Entry &e : ent) {
-                if (e.arms != arms || e.spl != spl) continue;
+                if (e.arms != arms || e.spl != spl || e.seg != seg) continue;
                 if (e.p.n_edges > INT32_MAX) {
                     release(b);
                     return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_create: an item has 2^31 edges or more");
@@ -147,14 +167,14 @@ mrpop_status mrpop_batch_create(const mrpop_batch_item *items, int64_t n_items, 
             g.n_chunks = (int)chunks.size();
             err = cudaMalloc(&g.d_items, ps.size() * sizeof(mrpop::EdgeParams));
             if (err == cudaSuccess) err = cudaMalloc(&g.d_chunks, chunks.size() * sizeof(int4));
-            if (err == cudaSuccess) err = cudaMalloc(&g.d_work, 2 * sizeof(unsigned long long));
+            if (err == cudaSuccess) err = cudaMalloc(&g.d_work, 3 * sizeof(unsigned long long));
             if (err == cudaSuccess)
                 err = cudaMemcpy(g.d_items, ps.data(), ps.size() * sizeof(mrpop::EdgeParams), cudaMemcpyHostToDevice);
             if (err == cudaSuccess)
                 err = cudaMemcpy(g.d_chunks, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice);
-            for (int k = 0; k < 2 && err == cudaSuccess; k++) {
+            for (int k = 0; k < (seg ? 3 : 2) && err == cudaSuccess; k++) {
                 int nb = 0;
-                err = mrpop::batch_occupancy(arms, k == 1, spl, g.smem, &nb);
+                err = mrpop::batch_occupancy(arms, k, seg, spl, g.smem, &nb);
                 const long long cap = (long long)sms * std::max(nb, 1);
                 g.max_grid[k] = (int)std::max(1LL, std::min<long long>(cap, g.n_chunks));
                 g.grid[k] = g.max_grid[k];
@@ -173,18 +193,19 @@ mrpop_status mrpop_batch_create(const mrpop_batch_item *items, int64_t n_items, 
 mrpop_status mrpop_batch_run(mrpop_batch *b, void *stream) {
     if (!b) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_run: null batch");
     const cudaStream_t s = (cudaStream_t)stream;
-    for (int k = 0; k < 2; k++)
-        for (const auto &g : b->groups) {
-            const cudaError_t err = launch_group(g, k == 1, g.grid[k], s);
-            if (err != cudaSuccess) return cuda_status(err, "batch_run: launch");
-        }
+    for (const auto &g : b->groups) {
+        const cudaError_t err = run_group(g, s);
+        if (err != cudaSuccess) return cuda_status(err, "batch_run: launch");
+    }
     return MRPOP_OK;
 }
 
 // Launch-shape tuner: per group and kernel, the grid (CTAs; multiples of the
 // SM count up to the resident maximum, and the chunk count) with the shortest
 // device time over three runs.  Broad launches are tuned first (the narrow
-// kernel reads their output).  Synchronous; not for use during capture.
+// kernel reads their output); a segmented group is tuned on its first round
+// and keeps the fused kernel's largest grid.  Synchronous; not for use during
+// capture.
 mrpop_status mrpop_batch_tune(mrpop_batch *b, void *stream) {
     if (!b) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_tune: null batch");
     const cudaStream_t s = (cudaStream_t)stream;
@@ -204,11 +225,12 @@ mrpop_status mrpop_batch_tune(mrpop_batch *b, void *stream) {
             float best = 1e30f;
             int best_grid = g.grid[k];
             for (int grid : cand) {
-                if (k == 1) err = launch_group(g, false, g.grid[0], s);  // narrow reads the broad output
+                // narrow reads the broad output
+                if (k == 1) err = launch_group(g, mrpop::kBatchBroad, g.grid[0], 0, s);
                 float tot = 0.0f;
                 for (int r = 0; r < 3 && err == cudaSuccess; r++) {
                     err = cudaEventRecord(e0, s);
-                    if (err == cudaSuccess) err = launch_group(g, k == 1, grid, s);
+                    if (err == cudaSuccess) err = launch_group(g, k, grid, 0, s);
                     if (err == cudaSuccess) err = cudaEventRecord(e1, s);
                     if (err == cudaSuccess) err = cudaEventSynchronize(e1);
                     float ms = 0.0f;
@@ -231,8 +253,8 @@ mrpop_status mrpop_batch_tune(mrpop_batch *b, void *stream) {
     return MRPOP_OK;
 }
 
-// Captures one run into a CUDA graph: each group's broad and narrow launches
-// on a branch of their own, joined at the end.  Replaces an earlier capture.
+// Captures one run into a CUDA graph: each group's launches on a branch of
+// their own, joined at the end.  Replaces an earlier capture.
 mrpop_status mrpop_batch_capture(mrpop_batch *b) {
     if (!b) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_capture: null batch");
     if (b->exec) {
@@ -257,8 +279,7 @@ mrpop_status mrpop_batch_capture(mrpop_batch *b) {
         for (size_t i = 0; i < b->groups.size() && cerr == cudaSuccess; i++) {
             cudaStream_t s = b->branch[i + 1];
             cerr = cudaStreamWaitEvent(s, ev[0], 0);
-            if (cerr == cudaSuccess) cerr = launch_group(b->groups[i], false, b->groups[i].grid[0], s);
-            if (cerr == cudaSuccess) cerr = launch_group(b->groups[i], true, b->groups[i].grid[1], s);
+            if (cerr == cudaSuccess) cerr = run_group(b->groups[i], s);
             if (cerr == cudaSuccess) cerr = cudaEventRecord(ev[i + 1], s);
             if (cerr == cudaSuccess) cerr = cudaStreamWaitEvent(origin, ev[i + 1], 0);
         }
@@ -289,10 +310,11 @@ mrpop_status mrpop_batch_info(const mrpop_batch *b, int64_t *n_groups, int32_t *
     *n_groups = (int64_t)b->groups.size();
     for (int64_t i = 0; grids && i < max_groups && i < (int64_t)b->groups.size(); i++) {
         const auto &g = b->groups[i];
-        grids[4 * i + 0] = g.arms;
-        grids[4 * i + 1] = g.spl;
-        grids[4 * i + 2] = g.grid[0];
-        grids[4 * i + 3] = g.grid[1];
+        grids[5 * i + 0] = g.arms;
+        grids[5 * i + 1] = g.spl;
+        grids[5 * i + 2] = g.seg ? 1 : 0;
+        grids[5 * i + 3] = g.grid[0];
+        grids[5 * i + 4] = g.grid[1];
     }
     return MRPOP_OK;
 }

@@ -1276,46 +1276,54 @@ __device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &
 // ---------------------------------------------------------------------------
 // fused kernel: every rule, segments in order with early exit
 // ---------------------------------------------------------------------------
+// One edge through the fused kernel: segments from P.seg0 in order, both
+// phases per segment, early exit at the first colliding one.  Edges decided by
+// earlier split rounds (P.seg0 > 0) are skipped.
+template <int A, int SPL>
+__device__ __forceinline__ void fused_edge(const EdgeParams &P, WarpScratch &W, const float4 *S, const SceneLayout &L,
+                                           const float4 *det_tab, long long e, int dof, int g, int lane,
+                                           bool staged) {
+    if (!staged) {
+        if (lane == 0) {
+            P.valid[e] = 0;
+            P.first_hit[e] = -2;
+        }
+        return;
+    }
+    if (P.seg0 > 0 && (P.sdone[e] || P.snseg[e] <= P.seg0)) return; // decided by the split rounds
+    bool too_many;
+    const int nseg = edge_setup(P, W, e, dof, g, lane, too_many);
+    int first = 0;
+    double tally = 0.0;
+    const int nseg_run = too_many ? 0 : nseg;
+    if (P.rule == kRuleConnect && P.seg0 > 0) connect_advance(W, dof, P.seg0, lane);
+    for (int seg = P.seg0; seg < nseg_run && first == 0; seg++) {
+        uint64_t envw[SPL], selfw[SPL], cand_env, cand_self;
+        if (broad_decide<A, SPL>(P, W, S, L, seg, g, lane, envw, selfw, cand_env, cand_self, tally)) {
+            const int fb = narrow_segment<A, SPL>(P, W, S, L, det_tab, seg, lane, envw, selfw, cand_env, cand_self);
+            if (fb < 64) first = seg * g + fb + 1;
+        }
+        if (P.rule == kRuleConnect) {
+            __syncwarp();
+            for (int d = lane; d < dof; d += 32) W.base[d] = __fadd_rn(W.base[d], W.delta[d]);
+            __syncwarp();
+        }
+    }
+    if (lane == 0) {
+        P.valid[e] = (first == 0 && !too_many) ? 1 : 0;
+        P.first_hit[e] = too_many ? -2 : (first ? first : -1);
+        if (P.n_seg_out) P.n_seg_out[e] = nseg;
+        if (P.flops) P.flops[e] = P.seg0 > 0 ? P.flops[e] + tally : tally;
+    }
+    __syncwarp();
+}
+
 template <int A, int SPL>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
     validate_kernel(const __grid_constant__ EdgeParams P) {
     MRPOP_KERNEL_PROLOGUE()
-    for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps) {
-        if (!staged) {
-            if (lane == 0) {
-                P.valid[e] = 0;
-                P.first_hit[e] = -2;
-            }
-            continue;
-        }
-        if (P.seg0 > 0 && (P.sdone[e] || P.snseg[e] <= P.seg0)) continue; // decided by the split rounds
-        bool too_many;
-        const int nseg = edge_setup(P, W, e, dof, g, lane, too_many);
-        int first = 0;
-        double tally = 0.0;
-        const int nseg_run = too_many ? 0 : nseg;
-        if (P.rule == kRuleConnect && P.seg0 > 0) connect_advance(W, dof, P.seg0, lane);
-        for (int seg = P.seg0; seg < nseg_run && first == 0; seg++) {
-            uint64_t envw[SPL], selfw[SPL], cand_env, cand_self;
-            if (broad_decide<A, SPL>(P, W, S, L, seg, g, lane, envw, selfw, cand_env, cand_self, tally)) {
-                const int fb = narrow_segment<A, SPL>(P, W, S, L, det_tab, seg, lane, envw, selfw, cand_env,
-                                                      cand_self);
-                if (fb < 64) first = seg * g + fb + 1;
-            }
-            if (P.rule == kRuleConnect) {
-                __syncwarp();
-                for (int d = lane; d < dof; d += 32) W.base[d] = __fadd_rn(W.base[d], W.delta[d]);
-                __syncwarp();
-            }
-        }
-        if (lane == 0) {
-            P.valid[e] = (first == 0 && !too_many) ? 1 : 0;
-            P.first_hit[e] = too_many ? -2 : (first ? first : -1);
-            if (P.n_seg_out) P.n_seg_out[e] = nseg;
-            if (P.flops) P.flops[e] = P.seg0 > 0 ? P.flops[e] + tally : tally;
-        }
-        __syncwarp();
-    }
+    for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps)
+        fused_edge<A, SPL>(P, W, S, L, det_tab, e, dof, g, lane, staged);
 }
 
 // ---------------------------------------------------------------------------
@@ -1473,14 +1481,22 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
 // edges form chunks; CTAs take chunks from a counter, in instance order, and
 // copy the instance's parameters to shared memory and restage its scene with
 // the bulk-copy engine when the instance changes; the CTA's warps then take
-// the chunk's edges one at a time.
+// the chunk's edges one at a time.  MODE picks the broad, narrow or fused
+// per-edge body; SEG marks groups of segmented instances (connect, B-spline,
+// shortcut), which run the split kernels in rounds (BatchParams::seg0) and
+// the fused kernel for the edges left after them.
 // ---------------------------------------------------------------------------
 struct BatchParams {
     const EdgeParams *items;      // device array, one per instance
     const int4 *chunks;           // {instance, first edge, edge count, -}, instances in order
     int n_chunks;
+    int seg0;                     // segmented groups: the round (split kernels) or first segment (fused)
     unsigned long long *work;     // next-chunk counter, zero before each launch
 };
+
+// Batch kernel modes: the split pipeline's two kernels, and the fused kernel
+// that finishes segmented edges after the split rounds.
+constexpr int kBatchBroad = 0, kBatchNarrow = 1, kBatchFused = 2;
 
 // One bulk copy of `bytes` from global to shared memory, completed on `bar`
 // in phase `parity`; bounded wait.  Every thread of the CTA calls it after a
@@ -1515,7 +1531,7 @@ __device__ __forceinline__ bool stage_bulk(float4 *dst, const float4 *src, uint3
     return __syncthreads_and(ok);
 }
 
-template <int A, int SPL, bool NARROW>
+template <int A, int SPL, int MODE, bool SEG>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
     batch_kernel(const __grid_constant__ BatchParams B) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -1549,6 +1565,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
             uint32_t *dst = reinterpret_cast<uint32_t *>(&Ps);
             for (int i = threadIdx.x; i < (int)(sizeof(EdgeParams) / 4); i += blockDim.x) dst[i] = src[i];
             __syncthreads();
+            if (SEG) { // the round of this launch
+                if (threadIdx.x == 0) Ps.seg0 = B.seg0;
+                __syncthreads();
+            }
             const uint32_t bytes = (uint32_t)(scene_layout(Ps.sc).total * sizeof(float4));
             staged = true;
             if (bytes) {
@@ -1569,8 +1589,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
             k = __shfl_sync(kFull, k, 0);
             if ((int)k >= ch.z) break;
             const long long e = (long long)ch.y + k;
-            if (NARROW) narrow_edge<A, SPL, false>(P, W, S, L, det_tab, e, dof, P.g, lane, staged);
-            else broad_edge<A, SPL, false>(P, W, S, L, e, dof, P.g, lane, staged);
+            if (MODE == kBatchBroad) broad_edge<A, SPL, SEG>(P, W, S, L, e, dof, P.g, lane, staged);
+            else if (MODE == kBatchNarrow) narrow_edge<A, SPL, SEG>(P, W, S, L, det_tab, e, dof, P.g, lane, staged);
+            else fused_edge<A, SPL>(P, W, S, L, det_tab, e, dof, P.g, lane, staged);
         }
         __syncthreads(); // every warp is done with this chunk (and instance)
     }

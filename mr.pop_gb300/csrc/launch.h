@@ -17,16 +17,18 @@ cudaError_t launch_validate(int arms, KernelKind kind, const EdgeParams &p, size
 template <int A>
 cudaError_t launch_validate_arms(KernelKind kind, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream);
 
-// Batch kernels (BatchParams: the instances of one arm count and samples per
-// lane): resident CTAs per SM at a shared-memory size, and a launch on `grid`
-// CTAs.  The dispatchers switch on the arm count (api.cu).
-cudaError_t batch_occupancy(int arms, bool narrow, int spl, size_t smem_bytes, int *blocks_per_sm);
-cudaError_t launch_batch(int arms, bool narrow, int spl, const BatchParams &b, size_t smem_bytes, int grid,
+// Batch kernels (BatchParams: the instances of one arm count, samples per
+// lane and segmentation kind; mode = kBatchBroad / kBatchNarrow / kBatchFused,
+// seg = segmented instances): resident CTAs per SM at a shared-memory size,
+// and a launch on `grid` CTAs.  The dispatchers switch on the arm count
+// (api.cu).
+cudaError_t batch_occupancy(int arms, int mode, bool seg, int spl, size_t smem_bytes, int *blocks_per_sm);
+cudaError_t launch_batch(int arms, int mode, bool seg, int spl, const BatchParams &b, size_t smem_bytes, int grid,
                          cudaStream_t stream);
 template <int A>
-cudaError_t batch_occupancy_arms(bool narrow, int spl, size_t smem_bytes, int *blocks_per_sm);
+cudaError_t batch_occupancy_arms(int mode, bool seg, int spl, size_t smem_bytes, int *blocks_per_sm);
 template <int A>
-cudaError_t launch_batch_arms(bool narrow, int spl, const BatchParams &b, size_t smem_bytes, int grid,
+cudaError_t launch_batch_arms(int mode, bool seg, int spl, const BatchParams &b, size_t smem_bytes, int grid,
                               cudaStream_t stream);
 
 }  // namespace mrpop

@@ -74,8 +74,14 @@ const void *kernel_fn(KernelKind kind, bool seg) {
 }
 
 template <int A, int SPL>
-const void *batch_fn(bool narrow) {
-    return narrow ? (const void *)batch_kernel<A, SPL, true> : (const void *)batch_kernel<A, SPL, false>;
+const void *batch_fn(int mode, bool seg) {
+    if (!seg) return mode == kBatchNarrow ? (const void *)batch_kernel<A, SPL, kBatchNarrow, false>
+                                          : (const void *)batch_kernel<A, SPL, kBatchBroad, false>;
+    switch (mode) {
+    case kBatchBroad: return (const void *)batch_kernel<A, SPL, kBatchBroad, true>;
+    case kBatchNarrow: return (const void *)batch_kernel<A, SPL, kBatchNarrow, true>;
+    default: return (const void *)batch_kernel<A, SPL, kBatchFused, true>;
+    }
 }
 
 // Persistent grid: SMs x resident CTAs at this shared-memory size, no more
@@ -102,15 +108,15 @@ cudaError_t launch_validate_impl(KernelKind kind, const EdgeParams &p, size_t sm
 // Batch kernels: the attribute is raised when a batch is created, so launches
 // (and graph capture) do not touch it.
 template <int A>
-cudaError_t batch_occupancy_impl(bool narrow, int spl, size_t smem_bytes, int *blocks_per_sm) {
-    const void *fn = spl == 2 ? batch_fn<A, 2>(narrow) : batch_fn<A, 1>(narrow);
+cudaError_t batch_occupancy_impl(int mode, bool seg, int spl, size_t smem_bytes, int *blocks_per_sm) {
+    const void *fn = spl == 2 ? batch_fn<A, 2>(mode, seg) : batch_fn<A, 1>(mode, seg);
     return prepare_kernel(fn, smem_bytes, blocks_per_sm);
 }
 
 template <int A>
-cudaError_t launch_batch_impl(bool narrow, int spl, const BatchParams &b, size_t smem_bytes, int grid,
+cudaError_t launch_batch_impl(int mode, bool seg, int spl, const BatchParams &b, size_t smem_bytes, int grid,
                               cudaStream_t stream) {
-    const void *fn = spl == 2 ? batch_fn<A, 2>(narrow) : batch_fn<A, 1>(narrow);
+    const void *fn = spl == 2 ? batch_fn<A, 2>(mode, seg) : batch_fn<A, 1>(mode, seg);
     void *args[] = {(void *)&b};
     return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(32 * kWarpsPerBlock), args, smem_bytes, stream);
 }
@@ -126,12 +132,13 @@ cudaError_t launch_batch_impl(bool narrow, int spl, const BatchParams &b, size_t
         return launch_validate_impl<A>(kind, p, smem_bytes, stream);                                    \
     }                                                                                                   \
     template <>                                                                                         \
-    cudaError_t batch_occupancy_arms<A>(bool narrow, int spl, size_t smem_bytes, int *blocks_per_sm) {  \
-        return batch_occupancy_impl<A>(narrow, spl, smem_bytes, blocks_per_sm);                         \
+    cudaError_t batch_occupancy_arms<A>(int mode, bool seg, int spl, size_t smem_bytes,                \
+                                        int *blocks_per_sm) {                                           \
+        return batch_occupancy_impl<A>(mode, seg, spl, smem_bytes, blocks_per_sm);                      \
     }                                                                                                   \
     template <>                                                                                         \
-    cudaError_t launch_batch_arms<A>(bool narrow, int spl, const BatchParams &b, size_t smem_bytes,     \
-                                     int grid, cudaStream_t stream) {                                   \
-        return launch_batch_impl<A>(narrow, spl, b, smem_bytes, grid, stream);                          \
+    cudaError_t launch_batch_arms<A>(int mode, bool seg, int spl, const BatchParams &b,                \
+                                     size_t smem_bytes, int grid, cudaStream_t stream) {               \
+        return launch_batch_impl<A>(mode, seg, spl, b, smem_bytes, grid, stream);                       \
     }                                                                                                   \
     }

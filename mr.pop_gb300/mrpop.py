@@ -58,7 +58,7 @@ class BatchItem(C.Structure):
     _fields_ = [
         ("scene", C.c_void_p), ("robots", C.c_void_p), ("q0", C.c_void_p), ("q1", C.c_void_p),
         ("n_edges", C.c_int64), ("granularity", C.c_int32), ("flags", C.c_uint32), ("arm", C.c_int32),
-        ("valid", C.c_void_p), ("first_hit", C.c_void_p),
+        ("valid", C.c_void_p), ("first_hit", C.c_void_p), ("rule", C.c_int32), ("range", C.c_float),
     ]
 
 
@@ -313,8 +313,9 @@ def kernel_times(lib: C.CDLL | None = None) -> dict:
 class Batch:
     """Many independent validate calls in one launch per kernel variant
     (mrpop_batch_*).  items: (scene, robots, q0, q1, granularity, flags, arm)
-    with q0/q1 CUDA tensors; outputs are allocated here (self.valid[i],
-    self.first_hit[i]) unless given as items[i][7:9]."""
+    with q0/q1 CUDA (or page-locked host) tensors; outputs are allocated here
+    (self.valid[i], self.first_hit[i]) unless given as items[i][7:9] (either
+    may be None); items[i][9:11] = (rule, range) for a segmented item."""
 
     def __init__(self, items, lib: C.CDLL | None = None):
         import torch
@@ -325,13 +326,14 @@ class Batch:
         for i, it in enumerate(self.items):
             scene, robots, q0, q1, g, flags, arm = it[:7]
             n = q0.shape[0]
-            v = it[7] if len(it) > 7 else torch.empty(n, dtype=torch.uint8, device=q0.device)
-            f = it[8] if len(it) > 8 else torch.empty(n, dtype=torch.int32, device=q0.device)
+            v = it[7] if len(it) > 7 and it[7] is not None else torch.empty(n, dtype=torch.uint8, device=q0.device)
+            f = it[8] if len(it) > 8 and it[8] is not None else torch.empty(n, dtype=torch.int32, device=q0.device)
+            rule, range_ = (int(it[9]), float(it[10])) if len(it) > 10 else (RULE_PLAIN, 0.0)
             self.valid.append(v)
             self.first_hit.append(f)
             arr[i] = BatchItem(scene.handle, robots.handle, q0.data_ptr() if n else None,
                                q1.data_ptr() if n else None, n, g, flags, arm, v.data_ptr() if n else None,
-                               f.data_ptr() if n else None)
+                               f.data_ptr() if n else None, rule, range_)
         h = C.c_void_p()
         _check(self.lib, self.lib.mrpop_batch_create(arr, len(self.items), C.byref(h)))
         self.handle = h
@@ -348,11 +350,12 @@ class Batch:
     def launch(self, stream=None):
         _check(self.lib, self.lib.mrpop_batch_launch(self.handle, _stream_ptr(stream)))
 
-    def info(self) -> list[tuple[int, int, int, int]]:
+    def info(self) -> list[tuple[int, int, int, int, int]]:
+        """Per group: (arms, samples per lane, segmented, broad grid, narrow grid)."""
         n = C.c_int64()
-        grids = np.zeros(4 * 16, np.int32)
-        _check(self.lib, self.lib.mrpop_batch_info(self.handle, C.byref(n), grids.ctypes.data, 16))
-        return [tuple(int(x) for x in grids[4 * i:4 * i + 4]) for i in range(n.value)]
+        grids = np.zeros(5 * 32, np.int32)
+        _check(self.lib, self.lib.mrpop_batch_info(self.handle, C.byref(n), grids.ctypes.data, 32))
+        return [tuple(int(x) for x in grids[5 * i:5 * i + 5]) for i in range(min(n.value, 32))]
 
     def __del__(self):
         if getattr(self, "handle", None):

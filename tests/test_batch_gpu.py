@@ -50,7 +50,7 @@ def test_batch_equals_per_instance_calls(cuda, pkg):
     ref = _reference(pkg, cuda, items)
     b = pkg.Batch(items)
     groups = b.info()
-    assert len(groups) >= 5 and all(1 <= a <= 5 and s in (1, 2) for a, s, _, _ in groups)
+    assert len(groups) >= 5 and all(1 <= a <= 5 and s in (1, 2) and seg == 0 for a, s, seg, _, _ in groups)
     b.run()
     cuda.cuda.synchronize()
     _check(b, ref)
@@ -146,3 +146,49 @@ def test_batch_items_in_page_locked_host_memory(cuda, pkg):
     b.launch()
     cuda.cuda.synchronize()
     _check(b, ref)
+
+
+def test_batch_segmented_items(cuda, pkg):
+    """Connect, B-spline and shortcut items (with plain ones) in one batch:
+    segment rounds and the fused tail per group give the per-item
+    mrpop_validate_segments results bit for bit, through a plain run, after
+    tuning and through the captured graph, on a rerun of cleared outputs."""
+    W = pkg.workloads
+    rng = np.random.default_rng(21)
+    items = []
+    for k in range(12):
+        arms = 1 + k % 5
+        g = (16, 32, 64)[k % 3]
+        rule = (pkg.RULE_PLAIN, pkg.RULE_CONNECT, pkg.RULE_BSPLINE, pkg.RULE_SHORTCUT)[k % 4]
+        # long edges, so that many take more segments than the split rounds
+        n = int(rng.integers(40, 400))
+        a0, a1 = W.random_edges(rng, n, arms, 3.0)
+        sc = pkg.Scene(W.scene_config1(k) if k % 2 else W.scene_config2(k))
+        rb = pkg.RobotSet(arms, W.bases_facing_centre(arms, 0.71))
+        rng_ = 0.0 if rule == pkg.RULE_PLAIN else float((0.25, 0.5, 1.0)[k % 3])
+        items.append((sc, rb, cuda.from_numpy(a0).cuda(), cuda.from_numpy(a1).cuda(), g,
+                      pkg.CHECK_ENV | pkg.CHECK_SELF, -1, None, None, rule, rng_))
+    ref = []
+    for sc, rb, q0, q1, g, flags, arm, _, _, rule, rng_ in items:
+        out = pkg.validate(sc, rb, q0, q1, g, flags, arm, rule, rng_)
+        ref.append((out[0].cpu().numpy(), out[1].cpu().numpy()))
+    cuda.cuda.synchronize()
+    b = pkg.Batch(items)
+    assert any(seg for _, _, seg, _, _ in b.info())
+    b.run()
+    cuda.cuda.synchronize()
+    _check(b, ref)
+    for step in ("tune", "capture"):
+        for v, f in zip(b.valid, b.first_hit):
+            v.fill_(7)
+            f.fill_(-9)
+        if step == "tune":
+            b.tune()
+            b.run()
+        else:
+            b.capture()
+            b.launch()
+        cuda.cuda.synchronize()
+        _check(b, ref)
+    for it in items:
+        assert it[0].status() == 0
