@@ -1463,6 +1463,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
     (void)nwarps;
     for (long long e = next_edge(P.work, lane); e < P.n_edges; e = next_edge(P.work, lane))
         broad_edge<A, SPL, SEG>(P, W, S, L, e, dof, g, lane, staged);
+    // no edges left for this warp: the narrow kernel (launched as a
+    // programmatic dependent) may start its CTAs once every CTA got here
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 template <int A, int SPL, bool SEG>
@@ -1470,6 +1473,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
     narrow_kernel(const __grid_constant__ EdgeParams P) {
     MRPOP_KERNEL_PROLOGUE()
     (void)nwarps;
+    // the scene is staged; wait for the broad kernel (complete, its writes
+    // visible) before reading its output
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     for (long long e = next_edge(P.work + 1, lane); e < P.n_edges; e = next_edge(P.work + 1, lane))
         narrow_edge<A, SPL, SEG>(P, W, S, L, det_tab, e, dof, g, lane, staged);
 }

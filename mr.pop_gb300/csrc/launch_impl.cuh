@@ -102,7 +102,22 @@ cudaError_t launch_validate_impl(KernelKind kind, const EdgeParams &p, size_t sm
     if (need < grid) grid = need;
     if (grid < 1) grid = 1;
     void *args[] = {(void *)&p};
-    return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(32 * kWarpsPerBlock), args, smem_bytes, stream);
+    if (kind != kNarrow)
+        return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(32 * kWarpsPerBlock), args, smem_bytes, stream);
+    // the narrow kernel follows the broad one as a programmatic dependent: its
+    // CTAs start (and stage the scene) while the broad kernel's last warps
+    // finish, and wait for it in griddepcontrol.wait
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(32 * kWarpsPerBlock);
+    cfg.dynamicSmemBytes = smem_bytes;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 // Batch kernels: the attribute is raised when a batch is created, so launches
