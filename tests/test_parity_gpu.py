@@ -361,3 +361,30 @@ def test_concurrent_host_threads(cuda, pkg):
     for t in threads:
         t.join()
     assert not errors, errors
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_many_seeds_every_rule_and_mode(cuda, pkg, orc, seed):
+    """Bit-exact verdicts against the oracle fed the device's sin/cos on larger
+    seeded batches: 4 arms with every segmentation rule, 1 and 5 arms, the
+    shortcut workload; reference and exact modes."""
+    W = pkg.workloads
+    cases = [(W.config2(n_edges=2048, seed=seed), [(pkg.RULE_PLAIN, 0.0), (pkg.RULE_CONNECT, 0.3),
+                                                  (pkg.RULE_BSPLINE, 0.5), (pkg.RULE_SHORTCUT, 0.4)]),
+             (W.config1(n_edges=4096, seed=seed), [(pkg.RULE_PLAIN, 0.0)]),
+             (W.config3(n_edges=512, seed=seed), [(pkg.RULE_PLAIN, 0.0)]),
+             (W.config3_shortcuts(n_paths=32, pairs=16, seed=seed), [(pkg.RULE_SHORTCUT, 2.0)])]
+    for wl, rules in cases:
+        scene = pkg.Scene(wl.scene)
+        rb = pkg.RobotSet(len(wl.bases), wl.bases)
+        for rule, range_ in rules:
+            trig = _edge_trig(cuda, pkg, orc, wl.q0, wl.q1, wl.granularity, rule, range_)
+            for exact in (False, True):
+                flags = wl.flags | (pkg.MODE_EXACT if exact else 0)
+                got = _run(cuda, pkg, scene, rb, wl, flags=flags, rule=rule, range_=range_)
+                ref = orc.validate(wl.scene, wl.bases, wl.q0, wl.q1, wl.granularity, flags, wl.arm, rule, range_,
+                                   trig=trig)
+                assert np.array_equal(got[0], ref["valid"]) and np.array_equal(got[1], ref["first_hit"]), (rule, exact)
+                if len(got) > 2:
+                    assert np.array_equal(got[2], ref["n_seg"])
+        assert scene.status() == 0
