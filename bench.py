@@ -51,7 +51,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
-    ap.add_argument("--workload", choices=["config1", "config2", "config3", "config3s", "config4"], default="config2")
+    ap.add_argument("--workload", choices=["config1", "config2", "config3", "config3s", "config4", "config5"],
+                    default="config2")
+    ap.add_argument("--rate", type=float, default=200.0, help="config5: query arrivals per second (Poisson)")
+    ap.add_argument("--duration", type=float, default=60.0, help="config5: seconds of arrivals")
+    ap.add_argument("--isolated", type=int, default=100, help="config5: queries also solved alone, for comparison")
     ap.add_argument("--instances", type=int, default=512, help="config4: planning instances in the batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -400,6 +404,82 @@ def run_batch(args, world, rank, local, pkg, torch):
         print(json.dumps(out), flush=True)
 
 
+def run_serving(args, world, rank, local, pkg, torch):
+    """Served planning stream: Poisson arrivals at --rate for --duration
+    seconds, each query a planning run (2-5 Pandas, a fresh seeded scene from
+    the single-arm or bin-picking generator, collision-free start and goal) whose
+    validation steps go through one validation service (mrpop_server_*), so the
+    steps of concurrent queries share waves of batch launches.  The first
+    --isolated queries are also solved alone on the same service, one at a
+    time, for the latency comparison and the same-result check."""
+    P, S = pkg.planner, pkg.serving
+    flags = pkg.CHECK_ENV | pkg.CHECK_SELF
+
+    def collision_free(scene_arrays, bases, q):
+        scene = pkg.Scene(scene_arrays)
+        rb = pkg.RobotSet(len(bases), bases)
+        d = torch.from_numpy(np.ascontiguousarray(q)).cuda()
+        v, _ = pkg.validate(scene, rb, d, d, 1, flags)
+        torch.cuda.synchronize()
+        return v.cpu().numpy().astype(bool)
+
+    n = max(1, int(round(args.rate * args.duration)))
+    t0 = time.perf_counter()
+    queries = P.make_queries(n, seed=rank, collision_free=collision_free)
+    gen_s = time.perf_counter() - t0
+    settings = P.PlanSettings()
+    server = pkg.Server(budget_bytes=2 << 30, streams=4)
+    S.isolated(server, queries[:min(3, n)], settings)  # warm-up (first-use set-up of the library)
+    m = min(args.isolated, n)
+    alone = S.isolated(server, queries[:m], settings)
+    before = server.stats()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    served = S.stream(server, queries, args.rate, settings, seed=rank)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    after = server.stats()
+    wall = max_over_ranks(wall, world)
+    same = sum(S.same_result(a.result, b.result) for a, b in zip(alone, served[:m]))
+    sv, iso = S.summary(served), S.summary(alone)
+    samples = sv["edges"] * settings.granularity  # samples per segment; segmented steps check more
+    server.close()
+    if rank != 0:
+        return
+    out = {"metric": "served p99 plan latency", "value": sv["p99_ms"], "unit": "ms", "n_gpus": world,
+           "steps": n, "warmup": 3, "ms_per_step": sv["mean_ms"], "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded scenes, start/goal rejection-sampled collision-free)",
+           "config": {"workload": "config5_served_planning", "rate_qps": args.rate, "duration_s": args.duration,
+                      "queries": n, "arms": "2-5 (uniform)", "scenes": "single-arm or bin-picking generator",
+                      "planner": "batched bidirectional RRT with connect checks and shortcut passes (this "
+                                 "project's client; the reference's dRRT/AO-x is not rebuilt)",
+                      "settings": settings.__dict__, "service": "mrpop_server: 2 GiB budget, 4 streams",
+                      "query_generation_s": round(gen_s, 2)},
+           "latency": {"served_p50_ms": sv["p50_ms"], "served_p99_ms": sv["p99_ms"],
+                       "isolated_p50_ms": iso["p50_ms"], "isolated_p99_ms": iso["p99_ms"],
+                       "isolated_queries": m,
+                       "p99_ratio": sv["p99_ms"] / iso["p99_ms"] if iso["p99_ms"] else None},
+           "solve_rate": {"served": sv["solve_rate"], "isolated": iso["solve_rate"]},
+           "mean_cost": {"served": sv["mean_cost"], "isolated": iso["mean_cost"]},
+           "same_result_alone_and_mixed": f"{same}/{m}",
+           "throughput": {"queries_per_s": n / wall, "steps": sv["steps"], "edges": sv["edges"],
+                          "edge_samples_per_s_lower_bound": samples / wall,
+                          "waves": after["waves"] - before["waves"],
+                          "steps_per_wave": (after["steps"] - before["steps"]) / max(1, after["waves"] - before["waves"]),
+                          "max_wave_steps": after["max_wave_steps"],
+                          "max_waves_in_flight": after["max_waves_in_flight"],
+                          "admission_waits": after["admission_waits"]},
+           "gpu_launches": after["kernel_launches"] - before["kernel_launches"],
+           "clocks": clk,
+           "e2e": {"value": sv["p99_ms"], "unit": "ms", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                   "path": "host wall clock from each query's arrival to its plan; endpoints and verdicts in "
+                           "page-locked host buffers read and written in place by the kernels"}}
+    print(json.dumps(out), flush=True)
+
+
 def run_mine(args, world, rank, local):
     import torch
     import __graft_entry__ as ge
@@ -408,6 +488,8 @@ def run_mine(args, world, rank, local):
     if not lib.exists():
         pkg.build.build()
     pkg.library()
+    if args.workload == "config5":
+        return run_serving(args, world, rank, local, pkg, torch)
     if args.workload == "config4":
         return run_batch(args, world, rank, local, pkg, torch)
     wl = load_workload(pkg, args.workload)

@@ -247,6 +247,126 @@ mrpop_status mrpop_batch_launch(mrpop_batch *batch, void *stream);
 mrpop_status mrpop_batch_info(const mrpop_batch *batch, int64_t *n_groups, int32_t *grids, int64_t max_groups);
 mrpop_status mrpop_batch_destroy(mrpop_batch *batch);
 
+/*
+ * Serving: a continuous-batching validation service for many concurrent
+ * planning queries on one GPU.  No counterpart in the reference, which runs
+ * one query per process (dRRT::solve, Planners.hh:57-64, owning the device)
+ * and validates one edge per block (pop_planner.cu:973).
+ *
+ * mrpop_server_create reserves, once, an arena of budget_bytes of device
+ * memory on the current device, `streams` launch slots and one worker thread.
+ * A query opens a session (mrpop_session_open), which is admitted when the
+ * scratch of its largest step (arms, max_edges, max_granularity) fits in the
+ * arena's free space; otherwise the call waits, up to timeout_ms (< 0: no
+ * limit, 0: do not wait; MRPOP_ERR_OUT_OF_MEMORY when it gives up).  A session
+ * then submits one step at a time (mrpop_session_submit: an mrpop_batch_item,
+ * plain or segmented, whose buffers are device memory or page-locked host
+ * memory and must stay valid until the step is done) and waits for it
+ * (mrpop_session_wait; timeout_ms as above, MRPOP_ERR_DEVICE_TIMEOUT if the
+ * step is still running).  The worker gathers the steps pending from all
+ * sessions, in submission order, into a wave (up to max_wave_steps steps and
+ * max_wave_chunks chunks of 96 edges) and launches it as one set of persistent
+ * batch kernels on the next free slot's stream, so waves formed while others
+ * run overlap on the device.  Each step's verdicts equal the same
+ * mrpop_validate_edges / mrpop_validate_segments call made alone.
+ * mrpop_session_close waits for the session's step and returns its memory to
+ * the arena.  Sessions may be used from different host threads; one session
+ * is used by one thread at a time.  Close every session before
+ * mrpop_server_destroy, which finishes the pending steps and frees the server.
+ * A session also reserves page-locked host buffers for its steps in a host
+ * arena of host_bytes (mrpop_session_host_buffers).  Zero in a config field
+ * selects the default: 1 GiB, 4 streams, 1024 steps, 16384 chunks, 256 MiB.
+ */
+typedef struct {
+    int64_t budget_bytes;    /* device arena for the sessions' step scratch            */
+    int32_t streams;
+    int32_t max_wave_steps;
+    int64_t max_wave_chunks;
+    int64_t host_bytes;      /* page-locked host arena for the sessions' buffers       */
+} mrpop_server_config;
+
+typedef struct {
+    int64_t budget_bytes;        /* arena size                                        */
+    int64_t bytes_in_use;        /* reserved by open sessions now                     */
+    int64_t peak_bytes_in_use;   /* largest reservation seen at an admission          */
+    int64_t sessions;            /* sessions admitted                                 */
+    int64_t admission_waits;     /* sessions that had to wait for room                */
+    int64_t admission_timeouts;  /* sessions refused after waiting                    */
+    int64_t waves;               /* waves launched                                    */
+    int64_t steps;               /* steps launched                                    */
+    int64_t max_wave_steps;      /* most steps in one wave                            */
+    int64_t max_waves_in_flight; /* most waves on the device at once                  */
+    int64_t kernel_launches;     /* validator kernels launched                        */
+} mrpop_server_stats;
+
+typedef struct mrpop_server mrpop_server;
+typedef struct mrpop_session mrpop_session;
+
+mrpop_status mrpop_server_create(const mrpop_server_config *cfg, mrpop_server **out);
+mrpop_status mrpop_server_destroy(mrpop_server *server);
+mrpop_status mrpop_server_get_stats(mrpop_server *server, mrpop_server_stats *out);
+mrpop_status mrpop_session_open(mrpop_server *server, int arms, int64_t max_edges, int max_granularity,
+                                int64_t timeout_ms, mrpop_session **out);
+mrpop_status mrpop_session_submit(mrpop_session *session, const mrpop_batch_item *step);
+mrpop_status mrpop_session_wait(mrpop_session *session, int64_t timeout_ms);
+mrpop_status mrpop_session_close(mrpop_session *session);
+/* The session's page-locked host buffers for its steps, carved from the host
+ * arena the server reserved at start-up (host_bytes): q0 and q1 of
+ * [max_edges][7 * arms] floats, valid [max_edges], first_hit [max_edges].  The
+ * kernels read and write them in place, so a step may point at them. */
+mrpop_status mrpop_session_host_buffers(mrpop_session *session, float **q0, float **q1, uint8_t **valid,
+                                        int32_t **first_hit);
+
+/*
+ * A compact composite-space planner with the reference planner's step
+ * pattern: batched extends (plain edges, pop_planner.cu:551-561), connect
+ * checks of the new nodes towards the other tree (connect rule,
+ * pop_planner.cu:666-703) and shortcut passes (shortcut rule,
+ * path_simplification.cu:155-200).  It is the client that served planning
+ * measures; the reference's dRRT/AO-x planner (Planners.hh:57-64) is not
+ * rebuilt.  Deterministic given the seed and the verdicts.
+ *
+ * mrpop_plan runs it with any validator: validate(ctx, q0, q1, n, g, rule,
+ * range, valid, first_hit) checks n host edges and returns 0 (or an
+ * mrpop_status, which aborts the plan).  path_out (optional) receives up to
+ * max_waypoints waypoints [7 * arms] from start to goal.
+ * mrpop_session_plan runs it with its steps validated by the session (scene,
+ * robots and flags as for mrpop_validate_edges, composite check), in the
+ * session's host buffers; the session must allow max(batch, shortcut_pairs)
+ * edges of 7 * arms at the settings' granularity.
+ */
+typedef int (*mrpop_validate_fn)(void *ctx, const float *q0, const float *q1, int64_t n_edges, int granularity,
+                                 int rule, float range, uint8_t *valid, int32_t *first_hit);
+
+typedef struct {
+    int32_t batch;           /* extend targets per iteration (64)                      */
+    int32_t max_iters;       /* extend iterations before giving up (60)                */
+    int32_t granularity;     /* samples per edge and per segment (32)                  */
+    int32_t shortcut_passes; /* passes after the first solution (5)                    */
+    int32_t shortcut_pairs;  /* random (i<j) pairs per pass (32)                       */
+    float step;              /* extend length, composite Euclidean in rad (1.0)        */
+    float range;             /* segment length of connect and shortcut checks (1.0)    */
+    uint64_t seed;
+} mrpop_plan_settings;
+
+typedef struct {
+    int32_t solved;
+    int32_t iterations;
+    int32_t steps;           /* validate calls                                         */
+    int64_t edges;           /* edges validated                                        */
+    int64_t waypoints;
+    double cost;             /* path length, composite Euclidean                       */
+    uint64_t digest;         /* FNV-1a of every verdict received, in order             */
+} mrpop_plan_result;
+
+mrpop_status mrpop_plan(int arms, const float *start, const float *goal, const mrpop_plan_settings *settings,
+                        mrpop_validate_fn validate, void *ctx, float *path_out, int64_t max_waypoints,
+                        mrpop_plan_result *out);
+mrpop_status mrpop_session_plan(mrpop_session *session, const mrpop_scene *scene, const mrpop_robotset *robots,
+                                uint32_t flags, const float *start, const float *goal,
+                                const mrpop_plan_settings *settings, float *path_out, int64_t max_waypoints,
+                                mrpop_plan_result *out);
+
 /* Algorithmic flop count per edge (FMA = 2; the convention of the project's
  * roofline) for the same arguments as mrpop_validate_segments; writes
  * flops[e] (device, double).  Runs the validator with counting enabled. */

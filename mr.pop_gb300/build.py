@@ -16,7 +16,7 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
-SOURCES = ["api.cu", "batch.cu", "peak_probe.cu", "no_alloc.cu"] + [f"validate_a{a}.cu" for a in range(1, 6)]
+SOURCES = ["api.cu", "batch.cu", "server.cu", "planner.cu", "peak_probe.cu", "no_alloc.cu"] + [f"validate_a{a}.cu" for a in range(1, 6)]
 
 
 def _nvcc() -> str:

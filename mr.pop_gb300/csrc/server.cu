@@ -1,0 +1,597 @@
+// server.cu -- continuous-batching validation service for many concurrent
+// planning queries on one GPU.
+//
+// The reference runs one planning query per process: dRRT::solve owns the GPU,
+// allocates its state and validates one edge per block of its own kernels
+// (pop_planner.cu:220-737, 973).  Serving many queries at once needs three
+// things that it does not have, and this file provides them:
+//   - admission by device-memory footprint: a query opens a session, which
+//     reserves the scratch of its largest step inside one arena allocated when
+//     the server starts; a session that does not fit waits until others close;
+//   - co-batching: the steps that sessions submit (extend, connect, B-spline or
+//     shortcut edge sets) are gathered by one worker thread into waves, and
+//     every wave runs as one set of persistent batch launches (batch_kernel,
+//     the kernels of the mrpop_batch_* entry points) over all of its steps;
+//   - overlap: waves go to a ring of streams, so a wave is formed and launched
+//     while earlier ones are still on the GPU, and their kernels share the SMs
+//     at their tails.  A step's results are those of the same call made alone.
+// Completion comes back through a host function enqueued behind each wave;
+// it only takes the lock, marks the wave's steps done and wakes the waiters.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "launch.h"
+
+namespace {
+
+constexpr int kChunkEdges = 96;    // largest chunk (the batch entry points' chunk)
+// A wave is cut into chunks of kWarpsPerBlock..kChunkEdges edges, sized so
+// that it has about kWaveCtasPerSm chunks per SM: a planner step of a few
+// dozen edges then spreads over several CTAs instead of running through one
+// CTA's warps in turn.
+constexpr int kWaveCtasPerSm = 3;
+// Segmented groups of at most this many edges in a wave run as one fused
+// launch from segment 0 instead of the split rounds (2 launches instead of
+// 2 * kSegRounds + 1: launch latency dominates small waves).
+constexpr int64_t kFusedOnlyEdges = 4096;
+constexpr int kGroupKeys = 4 * MRPOP_MAX_ARMS;
+constexpr size_t kAlign = 256;
+
+size_t round_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
+
+}  // namespace
+
+struct mrpop_session;
+
+struct mrpop_server {
+    // One step: a validate call with its scratch in its session's arena block.
+    struct Step {
+        mrpop_session *session = nullptr;
+        mrpop::EdgeParams p{};
+        int arms = 1, spl = 1;
+        bool seg = false;
+        size_t smem = 0;
+        int n_chunks = 0;
+    };
+    // A ring slot: stream, device tables (work counters, parameter blocks and
+    // chunk lists of one wave) and their page-locked host mirror.
+    struct Slot {
+        cudaStream_t stream = nullptr;
+        char *d_tab = nullptr;
+        char *h_tab = nullptr;
+        bool busy = false;
+        std::vector<Step> steps;
+        mrpop_server *server = nullptr;
+    };
+
+    int device = 0;
+    int sms = 0;
+    mrpop_server_config cfg{};
+    char *d_arena = nullptr;
+    std::map<size_t, size_t> free_blocks;  // offset -> size, first fit
+    size_t in_use = 0;
+    char *h_arena = nullptr;               // page-locked host arena of the sessions' buffers
+    std::map<size_t, size_t> free_host;
+    size_t host_in_use = 0;
+    std::vector<Slot> slots;
+    size_t tab_params_off = 0, tab_chunks_off = 0, tab_bytes = 0;
+
+    std::mutex mu;
+    std::condition_variable cv;  // worker: steps pending or a slot freed; waiters: a step done or a block freed
+    std::deque<Step> pending;
+    bool stop = false;
+    std::thread worker;
+    mrpop_server_stats stats{};
+    std::atomic<int64_t> launches{0};  // kernels enqueued (the worker adds, stats readers load)
+};
+
+struct mrpop_session {
+    mrpop_server *server = nullptr;
+    int arms = 0;
+    int64_t max_edges = 0;
+    int max_g = 0;
+    size_t offset = 0, bytes = 0;
+    size_t host_off = 0, host_bytes = 0;
+    float *h_q0 = nullptr, *h_q1 = nullptr;
+    uint8_t *h_valid = nullptr;
+    int32_t *h_first = nullptr;
+    // guarded by server->mu
+    bool in_flight = false;
+    mrpop_status result = MRPOP_OK;
+    std::string error;
+};
+
+namespace {
+
+mrpop_status fail(mrpop_status st, const std::string &msg) { return mrpop::fail_status(st, msg.c_str()); }
+
+// First-fit allocation in an arena's free list; returns false if no block is large enough.
+bool arena_take(std::map<size_t, size_t> &free_list, size_t &in_use, size_t bytes, size_t *off) {
+    for (auto it = free_list.begin(); it != free_list.end(); ++it) {
+        if (it->second < bytes) continue;
+        *off = it->first;
+        const size_t rest = it->second - bytes;
+        const size_t at = it->first + bytes;
+        free_list.erase(it);
+        if (rest) free_list[at] = rest;
+        in_use += bytes;
+        return true;
+    }
+    return false;
+}
+
+void arena_give(std::map<size_t, size_t> &free_list, size_t &in_use, size_t off, size_t bytes) {
+    auto it = free_list.emplace(off, bytes).first;
+    auto next = std::next(it);
+    if (next != free_list.end() && it->first + it->second == next->first) {
+        it->second += next->second;
+        free_list.erase(next);
+    }
+    if (it != free_list.begin()) {
+        auto prev = std::prev(it);
+        if (prev->first + prev->second == it->first) {
+            prev->second += it->second;
+            free_list.erase(it);
+        }
+    }
+    in_use -= bytes;
+}
+
+// A session's device and host blocks, both or neither (caller holds the lock).
+bool take_blocks(mrpop_server *s, mrpop_session *ss) {
+    if (!arena_take(s->free_blocks, s->in_use, ss->bytes, &ss->offset)) return false;
+    if (!arena_take(s->free_host, s->host_in_use, ss->host_bytes, &ss->host_off)) {
+        arena_give(s->free_blocks, s->in_use, ss->offset, ss->bytes);
+        return false;
+    }
+    return true;
+}
+
+// Runs on the CUDA callback thread behind a wave: marks its steps done.
+void CUDART_CB wave_done(void *arg) {
+    auto *slot = static_cast<mrpop_server::Slot *>(arg);
+    mrpop_server *s = slot->server;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (auto &st : slot->steps) st.session->in_flight = false;
+        slot->steps.clear();
+        slot->busy = false;
+    }
+    s->cv.notify_all();
+}
+
+// One kernel of a group of the wave: its counter zeroed in stream order first.
+cudaError_t launch_one(int arms, bool seg, int spl, size_t smem, int mode, int seg0, const mrpop::EdgeParams *items,
+                       const int4 *chunks, int n_chunks, unsigned long long *work, int sms, cudaStream_t stream) {
+    mrpop::BatchParams b;
+    b.items = items;
+    b.chunks = chunks;
+    b.n_chunks = n_chunks;
+    b.seg0 = seg0;
+    b.work = work;
+    int nb = 0;
+    cudaError_t err = mrpop::batch_occupancy(arms, mode, seg, spl, smem, &nb);
+    if (err != cudaSuccess) return err;
+    const int grid = (int)std::max(1LL, std::min<long long>((long long)sms * std::max(nb, 1), n_chunks));
+    err = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream);
+    if (err == cudaSuccess) err = mrpop::launch_batch(arms, mode, seg, spl, b, smem, grid, stream);
+    return err;
+}
+
+// Builds the wave's tables in the slot, uploads them and launches every group.
+cudaError_t launch_wave(mrpop_server *s, mrpop_server::Slot &slot) {
+    auto *h_work = reinterpret_cast<unsigned long long *>(slot.h_tab);
+    auto *h_params = reinterpret_cast<mrpop::EdgeParams *>(slot.h_tab + s->tab_params_off);
+    auto *h_chunks = reinterpret_cast<int4 *>(slot.h_tab + s->tab_chunks_off);
+    auto *d_work = reinterpret_cast<unsigned long long *>(slot.d_tab);
+    auto *d_params = reinterpret_cast<mrpop::EdgeParams *>(slot.d_tab + s->tab_params_off);
+    auto *d_chunks = reinterpret_cast<int4 *>(slot.d_tab + s->tab_chunks_off);
+    (void)h_work;
+
+    struct Range {
+        int p0 = 0, np = 0, c0 = 0, nc = 0;
+        int64_t edges = 0;
+        size_t smem = 0;
+    };
+    // chunk size of this wave (a multiple of the warps per CTA)
+    int64_t total = 0;
+    for (const auto &st : slot.steps) total += st.p.n_edges;
+    const int64_t target = (int64_t)s->sms * kWaveCtasPerSm;
+    int chunk = (int)std::min<int64_t>(kChunkEdges, std::max<int64_t>(mrpop::kWarpsPerBlock, (total + target - 1) / target));
+    chunk = (chunk + mrpop::kWarpsPerBlock - 1) / mrpop::kWarpsPerBlock * mrpop::kWarpsPerBlock;
+    for (;;) {
+        int64_t n = 0;
+        for (const auto &st : slot.steps) n += (st.p.n_edges + chunk - 1) / chunk;
+        if (n <= s->cfg.max_wave_chunks || chunk >= kChunkEdges) break;
+        chunk = std::min(kChunkEdges, chunk + mrpop::kWarpsPerBlock);
+    }
+    Range ranges[kGroupKeys];
+    int np = 0, nc = 0;
+    for (int key = 0; key < kGroupKeys; key++) {
+        const int arms = 1 + key / 4, spl = 1 + key % 2;
+        const bool seg = (key / 2) % 2 == 1;
+        Range &r = ranges[key];
+        r.p0 = np;
+        r.c0 = nc;
+        for (const auto &st : slot.steps) {
+            if (st.arms != arms || st.spl != spl || st.seg != seg) continue;
+            const int item = np - r.p0;
+            h_params[np++] = st.p;
+            for (int64_t e0 = 0; e0 < st.p.n_edges; e0 += chunk)
+                h_chunks[nc++] = make_int4(item, (int)e0, (int)std::min<int64_t>(chunk, st.p.n_edges - e0), 0);
+            r.smem = std::max(r.smem, st.smem);
+            r.edges += st.p.n_edges;
+        }
+        r.np = np - r.p0;
+        r.nc = nc - r.c0;
+    }
+    cudaError_t err = cudaMemcpyAsync(d_params, h_params, (size_t)np * sizeof(mrpop::EdgeParams),
+                                      cudaMemcpyHostToDevice, slot.stream);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(d_chunks, h_chunks, (size_t)nc * sizeof(int4), cudaMemcpyHostToDevice, slot.stream);
+    for (int key = 0; key < kGroupKeys && err == cudaSuccess; key++) {
+        const Range &r = ranges[key];
+        if (!r.np) continue;
+        const int arms = 1 + key / 4, spl = 1 + key % 2;
+        const bool seg = (key / 2) % 2 == 1;
+        unsigned long long *work = d_work + 4 * key;
+        if (seg && r.edges <= kFusedOnlyEdges) {
+            s->launches += 1;
+            err = launch_one(arms, seg, spl, r.smem, mrpop::kBatchFused, 0, d_params + r.p0, d_chunks + r.c0, r.nc,
+                             work + 2, s->sms, slot.stream);
+            continue;
+        }
+        const int rounds = seg ? mrpop::kSegRounds : 1;
+        s->launches += 2 * rounds + (seg ? 1 : 0);
+        for (int rd = 0; rd < rounds && err == cudaSuccess; rd++) {
+            err = launch_one(arms, seg, spl, r.smem, mrpop::kBatchBroad, rd, d_params + r.p0, d_chunks + r.c0, r.nc,
+                             work + 0, s->sms, slot.stream);
+            if (err == cudaSuccess)
+                err = launch_one(arms, seg, spl, r.smem, mrpop::kBatchNarrow, rd, d_params + r.p0, d_chunks + r.c0,
+                                 r.nc, work + 1, s->sms, slot.stream);
+        }
+        if (err == cudaSuccess && seg)
+            err = launch_one(arms, seg, spl, r.smem, mrpop::kBatchFused, mrpop::kSegRounds, d_params + r.p0,
+                             d_chunks + r.c0, r.nc, work + 2, s->sms, slot.stream);
+    }
+    return err;
+}
+
+// The worker: forms a wave from the pending steps whenever a slot is free.
+void worker_loop(mrpop_server *s) {
+    cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        mrpop_server::Slot *slot = nullptr;
+        s->cv.wait(lk, [&] {
+            if (s->stop && s->pending.empty()) return true;
+            if (s->pending.empty()) return false;
+            for (auto &sl : s->slots)
+                if (!sl.busy) {
+                    slot = &sl;
+                    return true;
+                }
+            return false;
+        });
+        if (!slot) break;  // stopping with nothing pending
+        // FIFO: take steps while the wave's tables have room
+        int items = 0;
+        int64_t chunks = 0;
+        while (!s->pending.empty()) {
+            const auto &st = s->pending.front();
+            if (items + 1 > s->cfg.max_wave_steps || chunks + st.n_chunks > s->cfg.max_wave_chunks) break;
+            items++;
+            chunks += st.n_chunks;
+            slot->steps.push_back(st);
+            s->pending.pop_front();
+        }
+        slot->busy = true;
+        s->stats.waves++;
+        s->stats.steps += items;
+        s->stats.max_wave_steps = std::max<int64_t>(s->stats.max_wave_steps, items);
+        int in_flight = 0;
+        for (auto &sl : s->slots) in_flight += sl.busy ? 1 : 0;
+        s->stats.max_waves_in_flight = std::max<int64_t>(s->stats.max_waves_in_flight, in_flight);
+        lk.unlock();
+        cudaError_t err = launch_wave(s, *slot);
+        if (err == cudaSuccess) err = cudaLaunchHostFunc(slot->stream, wave_done, slot);
+        lk.lock();
+        if (err != cudaSuccess) {
+            // the wave's launches are not all enqueued: wait for what was, then fail its steps
+            lk.unlock();
+            cudaStreamSynchronize(slot->stream);
+            lk.lock();
+            const std::string msg = std::string("server: wave launch failed: ") + cudaGetErrorString(err);
+            for (auto &st : slot->steps) {
+                st.session->result = MRPOP_ERR_CUDA;
+                st.session->error = msg;
+                st.session->in_flight = false;
+            }
+            slot->steps.clear();
+            slot->busy = false;
+            s->cv.notify_all();
+        }
+    }
+}
+
+void destroy_server(mrpop_server *s) {
+    if (s->worker.joinable()) {
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stop = true;
+        }
+        s->cv.notify_all();
+        s->worker.join();
+    }
+    for (auto &sl : s->slots) {
+        if (sl.stream) {
+            cudaStreamSynchronize(sl.stream);
+            cudaStreamDestroy(sl.stream);
+        }
+        cudaFree(sl.d_tab);
+        cudaFreeHost(sl.h_tab);
+    }
+    cudaFree(s->d_arena);
+    cudaFreeHost(s->h_arena);
+    delete s;
+}
+
+}  // namespace
+
+extern "C" {
+
+mrpop_status mrpop_server_create(const mrpop_server_config *cfg, mrpop_server **out) {
+    if (!out) return fail(MRPOP_ERR_INVALID_ARGUMENT, "server_create: null out");
+    *out = nullptr;
+    mrpop_server_config c{};
+    if (cfg) c = *cfg;
+    if (c.budget_bytes <= 0) c.budget_bytes = (int64_t)1 << 30;
+    if (c.streams <= 0) c.streams = 4;
+    if (c.max_wave_steps <= 0) c.max_wave_steps = 1024;
+    if (c.max_wave_chunks <= 0) c.max_wave_chunks = 16384;
+    if (c.host_bytes <= 0) c.host_bytes = (int64_t)256 << 20;
+    if (c.streams > 16 || c.max_wave_steps > (1 << 20) || c.max_wave_chunks > (1 << 24))
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "server_create: streams <= 16, max_wave_steps <= 2^20, "
+                                                "max_wave_chunks <= 2^24");
+    auto *s = new (std::nothrow) mrpop_server();
+    if (!s) return fail(MRPOP_ERR_OUT_OF_MEMORY, "server_create: host allocation");
+    s->cfg = c;
+    cudaGetDevice(&s->device);
+    cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device);
+    const size_t arena = round_up((size_t)c.budget_bytes);
+    cudaError_t err = cudaMalloc(&s->d_arena, arena);
+    if (err != cudaSuccess) {
+        delete s;
+        return fail(MRPOP_ERR_OUT_OF_MEMORY, std::string("server_create: arena: ") + cudaGetErrorString(err));
+    }
+    s->free_blocks[0] = arena;
+    s->stats.budget_bytes = (int64_t)arena;
+    const size_t harena = round_up((size_t)c.host_bytes);
+    err = cudaHostAlloc(&s->h_arena, harena, cudaHostAllocDefault);
+    if (err != cudaSuccess) {
+        cudaFree(s->d_arena);
+        delete s;
+        return fail(MRPOP_ERR_OUT_OF_MEMORY, std::string("server_create: host arena: ") + cudaGetErrorString(err));
+    }
+    s->free_host[0] = harena;
+    s->tab_params_off = round_up(kGroupKeys * 4 * sizeof(unsigned long long));
+    s->tab_chunks_off = round_up(s->tab_params_off + (size_t)c.max_wave_steps * sizeof(mrpop::EdgeParams));
+    s->tab_bytes = round_up(s->tab_chunks_off + (size_t)c.max_wave_chunks * sizeof(int4));
+    s->slots.resize(c.streams);
+    for (auto &sl : s->slots) {
+        sl.server = s;
+        if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        if (err == cudaSuccess) err = cudaMalloc(&sl.d_tab, s->tab_bytes);
+        if (err == cudaSuccess) err = cudaHostAlloc(&sl.h_tab, s->tab_bytes, cudaHostAllocDefault);
+        sl.steps.reserve(c.max_wave_steps);
+    }
+    if (err != cudaSuccess) {
+        destroy_server(s);
+        return fail(MRPOP_ERR_CUDA, std::string("server_create: slots: ") + cudaGetErrorString(err));
+    }
+    s->worker = std::thread(worker_loop, s);
+    *out = s;
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_server_destroy(mrpop_server *s) {
+    if (s) destroy_server(s);
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_server_get_stats(mrpop_server *s, mrpop_server_stats *out) {
+    if (!s || !out) return fail(MRPOP_ERR_INVALID_ARGUMENT, "server_stats: null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->stats;
+    out->bytes_in_use = (int64_t)s->in_use;
+    out->kernel_launches = s->launches.load();
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_session_open(mrpop_server *s, int arms, int64_t max_edges, int max_granularity,
+                                int64_t timeout_ms, mrpop_session **out) {
+    if (!s || !out) return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_open: null argument");
+    *out = nullptr;
+    if (arms < 1 || arms > MRPOP_MAX_ARMS || max_edges < 1 || max_granularity < 1 ||
+        max_granularity > MRPOP_MAX_GRANULARITY)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_open: arms 1..5, max_edges >= 1, max_granularity 1..64");
+    const int64_t max_chunks = (max_edges + kChunkEdges - 1) / kChunkEdges;
+    if (max_chunks > s->cfg.max_wave_chunks || max_edges > INT32_MAX)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_open: max_edges exceeds one wave's chunk table");
+    const size_t bytes = round_up(mrpop::split_scratch_bytes(max_edges, max_granularity, arms));
+    const size_t qbytes = round_up((size_t)max_edges * 7 * arms * sizeof(float));
+    const size_t host_bytes = 2 * qbytes + round_up((size_t)max_edges) + round_up((size_t)max_edges * sizeof(int32_t));
+    if ((int64_t)bytes > s->stats.budget_bytes || host_bytes > round_up((size_t)s->cfg.host_bytes))
+        return fail(MRPOP_ERR_OUT_OF_MEMORY, "session_open: the session's scratch exceeds the server's budget");
+    auto *ss = new (std::nothrow) mrpop_session();
+    if (!ss) return fail(MRPOP_ERR_OUT_OF_MEMORY, "session_open: host allocation");
+    ss->server = s;
+    ss->arms = arms;
+    ss->max_edges = max_edges;
+    ss->max_g = max_granularity;
+    ss->bytes = bytes;
+    ss->host_bytes = host_bytes;
+    std::unique_lock<std::mutex> lk(s->mu);
+    bool waited = false;
+    if (!take_blocks(s, ss)) {
+        waited = true;
+        bool ok = false;
+        const auto fits = [&] { return take_blocks(s, ss); };
+        if (timeout_ms < 0) {
+            s->cv.wait(lk, fits);
+            ok = true;
+        } else if (timeout_ms > 0) {
+            ok = s->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), fits);
+        }
+        if (!ok) {
+            s->stats.admission_timeouts++;
+            lk.unlock();
+            delete ss;
+            return fail(MRPOP_ERR_OUT_OF_MEMORY, "session_open: no room in the server's budget before the timeout");
+        }
+    }
+    char *h = s->h_arena + ss->host_off;
+    ss->h_q0 = reinterpret_cast<float *>(h);
+    ss->h_q1 = reinterpret_cast<float *>(h + qbytes);
+    ss->h_valid = reinterpret_cast<uint8_t *>(h + 2 * qbytes);
+    ss->h_first = reinterpret_cast<int32_t *>(h + 2 * qbytes + round_up((size_t)max_edges));
+    s->stats.sessions++;
+    if (waited) s->stats.admission_waits++;
+    s->stats.peak_bytes_in_use = std::max<int64_t>(s->stats.peak_bytes_in_use, (int64_t)s->in_use);
+    *out = ss;
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_session_submit(mrpop_session *ss, const mrpop_batch_item *it) {
+    if (!ss || !it) return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_submit: null argument");
+    mrpop_server *s = ss->server;
+    mrpop_server::Step st;
+    st.session = ss;
+    int A = 0;
+    mrpop_status r = mrpop::make_params(it->scene, it->robots, it->q0, it->q1, it->n_edges, it->granularity,
+                                        it->rule, it->range, it->flags, it->arm, it->valid, it->first_hit, nullptr,
+                                        nullptr, st.p, A, st.smem);
+    if (r != MRPOP_OK) return r;
+    if (it->n_edges > ss->max_edges || it->granularity > ss->max_g || A > ss->arms)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_submit: step larger than the session was opened for");
+    st.arms = A;
+    st.spl = it->granularity > 32 ? 2 : 1;
+    st.seg = it->rule != MRPOP_RULE_PLAIN;
+    st.n_chunks = (int)((it->n_edges + kChunkEdges - 1) / kChunkEdges);
+    mrpop::set_split_scratch(st.p, s->d_arena + ss->offset, it->n_edges, it->granularity, A);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (ss->in_flight) return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_submit: the previous step is not done");
+        ss->result = MRPOP_OK;
+        ss->error.clear();
+        if (it->n_edges == 0) return MRPOP_OK;
+        ss->in_flight = true;
+        s->pending.push_back(st);
+    }
+    s->cv.notify_all();
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_session_wait(mrpop_session *ss, int64_t timeout_ms) {
+    if (!ss) return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_wait: null session");
+    mrpop_server *s = ss->server;
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (timeout_ms < 0) {
+        s->cv.wait(lk, [&] { return !ss->in_flight; });
+    } else if (!s->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return !ss->in_flight; })) {
+        return fail(MRPOP_ERR_DEVICE_TIMEOUT, "session_wait: the step is still running");
+    }
+    if (ss->result != MRPOP_OK) return fail(ss->result, ss->error);
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_session_close(mrpop_session *ss) {
+    if (!ss) return MRPOP_OK;
+    mrpop_server *s = ss->server;
+    {
+        std::unique_lock<std::mutex> lk(s->mu);
+        s->cv.wait(lk, [&] { return !ss->in_flight; });
+        arena_give(s->free_blocks, s->in_use, ss->offset, ss->bytes);
+        arena_give(s->free_host, s->host_in_use, ss->host_off, ss->host_bytes);
+    }
+    s->cv.notify_all();
+    delete ss;
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_session_host_buffers(mrpop_session *ss, float **q0, float **q1, uint8_t **valid,
+                                        int32_t **first_hit) {
+    if (!ss) return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_host_buffers: null session");
+    if (q0) *q0 = ss->h_q0;
+    if (q1) *q1 = ss->h_q1;
+    if (valid) *valid = ss->h_valid;
+    if (first_hit) *first_hit = ss->h_first;
+    return MRPOP_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The planner's validator for a session: the step's edges go through the
+// session's host buffers, which the kernels read and write in place.
+struct SessionValidator {
+    mrpop_session *ss;
+    const mrpop_scene *scene;
+    const mrpop_robotset *robots;
+    uint32_t flags;
+    int dof;
+};
+
+int session_validate(void *ctx, const float *q0, const float *q1, int64_t n, int g, int rule, float range,
+                     uint8_t *valid, int32_t *first_hit) {
+    auto *v = static_cast<SessionValidator *>(ctx);
+    mrpop_session *ss = v->ss;
+    if (n > ss->max_edges) return MRPOP_ERR_INVALID_ARGUMENT;
+    std::memcpy(ss->h_q0, q0, (size_t)n * v->dof * sizeof(float));
+    std::memcpy(ss->h_q1, q1, (size_t)n * v->dof * sizeof(float));
+    mrpop_batch_item it{};
+    it.scene = v->scene;
+    it.robots = v->robots;
+    it.q0 = ss->h_q0;
+    it.q1 = ss->h_q1;
+    it.n_edges = n;
+    it.granularity = g;
+    it.flags = v->flags;
+    it.arm = -1;
+    it.valid = ss->h_valid;
+    it.first_hit = ss->h_first;
+    it.rule = rule;
+    it.range = range;
+    mrpop_status st = mrpop_session_submit(ss, &it);
+    if (st == MRPOP_OK) st = mrpop_session_wait(ss, -1);
+    if (st != MRPOP_OK) return st;
+    std::memcpy(valid, ss->h_valid, (size_t)n);
+    std::memcpy(first_hit, ss->h_first, (size_t)n * sizeof(int32_t));
+    return MRPOP_OK;
+}
+
+}  // namespace
+
+extern "C" mrpop_status mrpop_session_plan(mrpop_session *ss, const mrpop_scene *scene, const mrpop_robotset *robots,
+                                           uint32_t flags, const float *start, const float *goal,
+                                           const mrpop_plan_settings *settings, float *path_out,
+                                           int64_t max_waypoints, mrpop_plan_result *out) {
+    if (!ss || !settings) return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_plan: null argument");
+    if (std::max(settings->batch, settings->shortcut_pairs) > ss->max_edges || settings->granularity > ss->max_g)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_plan: the session is smaller than the plan's steps");
+    SessionValidator v{ss, scene, robots, flags, 7 * ss->arms};
+    return mrpop_plan(ss->arms, start, goal, settings, session_validate, &v, path_out, max_waypoints, out);
+}

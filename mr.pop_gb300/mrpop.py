@@ -31,7 +31,9 @@ EXPORTED = [
     "mrpop_debug_trig", "mrpop_fp32_peak_probe", "mrpop_last_error", "mrpop_version",
     "mrpop_validate_edges_noalloc", "mrpop_broad_flops_per_sample", "mrpop_kernel_timing", "mrpop_kernel_times",
     "mrpop_debug_row5_table", "mrpop_batch_create", "mrpop_batch_run", "mrpop_batch_tune", "mrpop_batch_capture",
-    "mrpop_batch_launch", "mrpop_batch_info", "mrpop_batch_destroy",
+    "mrpop_batch_launch", "mrpop_batch_info", "mrpop_batch_destroy", "mrpop_server_create", "mrpop_server_destroy",
+    "mrpop_server_get_stats", "mrpop_session_open", "mrpop_session_submit", "mrpop_session_wait",
+    "mrpop_session_close", "mrpop_session_host_buffers", "mrpop_plan", "mrpop_session_plan",
 ]
 KERNEL_KINDS = ("fused", "broad", "narrow")
 NOALLOC_MAX_EDGES = 16384
@@ -60,6 +62,32 @@ class BatchItem(C.Structure):
         ("n_edges", C.c_int64), ("granularity", C.c_int32), ("flags", C.c_uint32), ("arm", C.c_int32),
         ("valid", C.c_void_p), ("first_hit", C.c_void_p), ("rule", C.c_int32), ("range", C.c_float),
     ]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("budget_bytes", C.c_int64), ("streams", C.c_int32), ("max_wave_steps", C.c_int32),
+                ("max_wave_chunks", C.c_int64), ("host_bytes", C.c_int64)]
+
+
+class PlanSettingsC(C.Structure):
+    _fields_ = [("batch", C.c_int32), ("max_iters", C.c_int32), ("granularity", C.c_int32),
+                ("shortcut_passes", C.c_int32), ("shortcut_pairs", C.c_int32), ("step", C.c_float),
+                ("range", C.c_float), ("seed", C.c_uint64)]
+
+
+class PlanResultC(C.Structure):
+    _fields_ = [("solved", C.c_int32), ("iterations", C.c_int32), ("steps", C.c_int32), ("edges", C.c_int64),
+                ("waypoints", C.c_int64), ("cost", C.c_double), ("digest", C.c_uint64)]
+
+
+VALIDATE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_float,
+                          C.c_void_p, C.c_void_p)
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "budget_bytes", "bytes_in_use", "peak_bytes_in_use", "sessions", "admission_waits", "admission_timeouts",
+        "waves", "steps", "max_wave_steps", "max_waves_in_flight", "kernel_launches")]
 
 
 _LIBS: dict[str, C.CDLL] = {}
@@ -102,6 +130,16 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
         "mrpop_batch_launch": [vp, vp],
         "mrpop_batch_info": [vp, C.POINTER(C.c_int64), vp, i64],
         "mrpop_batch_destroy": [vp],
+        "mrpop_server_create": [C.POINTER(ServerConfig), C.POINTER(vp)],
+        "mrpop_server_destroy": [vp],
+        "mrpop_server_get_stats": [vp, C.POINTER(ServerStats)],
+        "mrpop_session_open": [vp, i32, i64, i32, i64, C.POINTER(vp)],
+        "mrpop_session_submit": [vp, C.POINTER(BatchItem)],
+        "mrpop_session_wait": [vp, i64],
+        "mrpop_session_close": [vp],
+        "mrpop_session_host_buffers": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)],
+        "mrpop_plan": [i32, vp, vp, C.POINTER(PlanSettingsC), VALIDATE_FN, vp, vp, i64, C.POINTER(PlanResultC)],
+        "mrpop_session_plan": [vp, vp, vp, u32, vp, vp, C.POINTER(PlanSettingsC), vp, i64, C.POINTER(PlanResultC)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -390,6 +428,114 @@ class Workspace:
     def close(self):
         if getattr(self, "handle", None):
             self.lib.mrpop_workspace_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching validation service (mrpop_server_*): sessions are
+    admitted against a fixed device-memory budget and their steps co-batched."""
+
+    def __init__(self, budget_bytes: int = 1 << 30, streams: int = 4, max_wave_steps: int = 1024,
+                 max_wave_chunks: int = 16384, host_bytes: int = 256 << 20, lib: C.CDLL | None = None):
+        self.lib = lib or library()
+        cfg = ServerConfig(budget_bytes, streams, max_wave_steps, max_wave_chunks, host_bytes)
+        h = C.c_void_p()
+        _check(self.lib, self.lib.mrpop_server_create(C.byref(cfg), C.byref(h)))
+        self.handle = h
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(self.lib, self.lib.mrpop_server_get_stats(self.handle, C.byref(st)))
+        return {n: int(getattr(st, n)) for n, _ in ServerStats._fields_}
+
+    def session(self, arms: int, max_edges: int, max_granularity: int, timeout_ms: int = -1) -> "Session":
+        return Session(self, arms, max_edges, max_granularity, timeout_ms)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.mrpop_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Session:
+    """One admitted query: the session's page-locked endpoint and verdict
+    buffers of max_edges edges (from the server's host arena, read and written
+    in place by the kernels), one step at a time."""
+
+    def __init__(self, server: Server, arms: int, max_edges: int, max_granularity: int, timeout_ms: int = -1):
+        self.server, self.lib = server, server.lib
+        self.arms, self.max_edges = arms, max_edges
+        h = C.c_void_p()
+        _check(self.lib, self.lib.mrpop_session_open(server.handle, arms, max_edges, max_granularity, timeout_ms,
+                                                     C.byref(h)))
+        self.handle = h
+        p = [C.c_void_p() for _ in range(4)]
+        _check(self.lib, self.lib.mrpop_session_host_buffers(h, *[C.byref(x) for x in p]))
+        dof = 7 * arms
+        self._ptrs = [x.value for x in p]
+        self.q0 = np.ctypeslib.as_array(C.cast(p[0], C.POINTER(C.c_float)), shape=(max_edges, dof))
+        self.q1 = np.ctypeslib.as_array(C.cast(p[1], C.POINTER(C.c_float)), shape=(max_edges, dof))
+        self.valid = np.ctypeslib.as_array(C.cast(p[2], C.POINTER(C.c_uint8)), shape=(max_edges,))
+        self.first_hit = np.ctypeslib.as_array(C.cast(p[3], C.POINTER(C.c_int32)), shape=(max_edges,))
+
+    def submit(self, scene: Scene, robots: RobotSet, q0: np.ndarray, q1: np.ndarray, granularity: int,
+               flags: int = CHECK_ENV | CHECK_SELF, arm: int = -1, rule: int = RULE_PLAIN, range_: float = 0.0):
+        n = q0.shape[0]
+        self._n = n
+        if n:
+            # the step's rows [n][dof] packed at the start of the buffers (a
+            # single-arm step on a composite session has 7-float rows)
+            dof = q0.shape[1]
+            if n > self.max_edges or dof > self.q0.shape[1]:
+                raise MrpopError(1, f"session step of {n} edges x {dof} exceeds the session's "
+                                    f"{self.max_edges} x {self.q0.shape[1]}")
+            self.q0.reshape(-1)[:n * dof] = np.asarray(q0, np.float32).reshape(-1)
+            self.q1.reshape(-1)[:n * dof] = np.asarray(q1, np.float32).reshape(-1)
+        q0p, q1p, vp_, fp = self._ptrs if n else (None, None, None, None)
+        item = BatchItem(scene.handle, robots.handle, q0p, q1p, n, granularity, flags, arm, vp_, fp, rule,
+                         float(range_))
+        _check(self.lib, self.lib.mrpop_session_submit(self.handle, C.byref(item)))
+
+    def wait(self, timeout_ms: int = -1):
+        _check(self.lib, self.lib.mrpop_session_wait(self.handle, timeout_ms))
+        n = self._n
+        return self.valid[:n].copy(), self.first_hit[:n].copy()
+
+    def validate(self, scene, robots, q0, q1, granularity, flags=CHECK_ENV | CHECK_SELF, arm=-1, rule=RULE_PLAIN,
+                 range_=0.0):
+        self.submit(scene, robots, q0, q1, granularity, flags, arm, rule, range_)
+        return self.wait()
+
+    def plan(self, scene: Scene, robots: RobotSet, start: np.ndarray, goal: np.ndarray, settings: PlanSettingsC,
+             flags: int = CHECK_ENV | CHECK_SELF, max_waypoints: int = 4096):
+        """The library's planner with every step validated by this session
+        (mrpop_session_plan; one call, the GIL released throughout).
+        Returns (PlanResultC, path [waypoints, dof])."""
+        dof = 7 * self.arms
+        start = np.ascontiguousarray(start, np.float32)
+        goal = np.ascontiguousarray(goal, np.float32)
+        path = np.empty((max_waypoints, dof), np.float32)
+        res = PlanResultC()
+        _check(self.lib, self.lib.mrpop_session_plan(self.handle, scene.handle, robots.handle, flags,
+                                                     start.ctypes.data, goal.ctypes.data, C.byref(settings),
+                                                     path.ctypes.data, max_waypoints, C.byref(res)))
+        return res, path[:min(res.waypoints, max_waypoints)].copy()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.mrpop_session_close(self.handle)
             self.handle = None
 
     def __del__(self):

@@ -1,0 +1,116 @@
+"""Served planning stream: queries arrive as a Poisson process, each runs the
+library's planner (mrpop_session_plan, one call per query with the GIL
+released) on a client thread with its own session of the validation service
+(`mrpop_server_*`), and all sessions' steps are co-batched on the GPU by the
+service's worker.
+
+A query's latency runs from its arrival to its result, and includes waiting
+for admission (device-memory budget) and for a client thread, creating its
+scene and robot set on the device, and every validation step.
+"""
+from __future__ import annotations
+
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import mrpop as M
+from .planner import PlanResult, PlanSettings, Query, result_from_c
+
+
+@dataclass
+class Served:
+    result: PlanResult
+    arrival: float
+    start: float
+    finish: float
+
+    @property
+    def latency_ms(self) -> float:
+        return 1e3 * (self.finish - self.arrival)
+
+
+def run_query(server: M.Server, q: Query, settings: PlanSettings, flags: int = M.CHECK_ENV | M.CHECK_SELF,
+              timeout_ms: int = -1, keep: list | None = None) -> PlanResult:
+    """One query through a session of `server`: scene and robot set created on
+    the device for the query's lifetime, every step validated by the service.
+    keep: a list that takes the scene and robot set instead of freeing them
+    here (freeing device memory waits for the work in flight on the device, so
+    a stream frees them after its last query)."""
+    scene = M.Scene(q.scene, lib=server.lib)
+    robots = M.RobotSet(q.arms, q.bases, lib=server.lib)
+    if keep is not None:
+        keep.append((scene, robots))
+    max_edges = max(settings.batch, settings.shortcut_pairs)
+    sess = server.session(q.arms, max_edges, settings.granularity, timeout_ms)
+    try:
+        res, path = sess.plan(scene, robots, q.start, q.goal, settings.c(q.seed), flags)
+        return result_from_c(q.qid, res, path)
+    finally:
+        sess.close()
+
+
+def isolated(server: M.Server, queries: list[Query], settings: PlanSettings) -> list[Served]:
+    """Each query alone: one after another, nothing else on the service."""
+    out, keep = [], []
+    for q in queries:
+        t0 = time.perf_counter()
+        r = run_query(server, q, settings, keep=keep)
+        out.append(Served(r, t0, t0, time.perf_counter()))
+    del keep
+    return out
+
+
+def stream(server: M.Server, queries: list[Query], rate: float, settings: PlanSettings, seed: int = 0,
+           clients: int = 256) -> list[Served]:
+    """Poisson arrivals at `rate` queries/s; each query starts on a free client
+    thread (a query that finds none waits, and that wait counts as latency)."""
+    rng = np.random.default_rng(9000 + seed)
+    gaps = rng.exponential(1.0 / rate, size=len(queries))
+    out: list[Served | None] = [None] * len(queries)
+    lock = threading.Lock()
+    keep: list = []
+
+    def work(i: int, arrival: float):
+        t0 = time.perf_counter()
+        r = run_query(server, queries[i], settings, keep=keep)
+        with lock:
+            out[i] = Served(r, arrival, t0, time.perf_counter())
+
+    with ThreadPoolExecutor(max_workers=clients) as ex:
+        t_next = time.perf_counter()
+        futs = []
+        for i in range(len(queries)):
+            t_next += gaps[i]
+            delay = t_next - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            futs.append(ex.submit(work, i, t_next))
+        for f in futs:
+            f.result()
+    del keep
+    return out  # type: ignore[return-value]
+
+
+def summary(served: list[Served]) -> dict:
+    lat = np.array([s.latency_ms for s in served])
+    solved = [s for s in served if s.result.solved]
+    return {
+        "queries": len(served),
+        "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+        "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+        "mean_ms": float(lat.mean()) if len(lat) else None,
+        "solve_rate": len(solved) / max(1, len(served)),
+        "mean_cost": float(np.mean([s.result.cost for s in solved])) if solved else None,
+        "steps": int(sum(s.result.steps for s in served)),
+        "edges": int(sum(s.result.edges for s in served)),
+    }
+
+
+def same_result(a: PlanResult, b: PlanResult) -> bool:
+    """Identical plans: same verdict stream, solve flag and waypoints."""
+    return (a.solved == b.solved and a.verdict_digest == b.verdict_digest and a.steps == b.steps
+            and a.path.shape == b.path.shape and bool(np.array_equal(a.path, b.path)))

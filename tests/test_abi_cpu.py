@@ -51,3 +51,17 @@ def test_bad_flags_and_granularity_rejected(pkg, lib_path):
     assert lib.mrpop_validate_edges(fake, rb, fake, fake, 4, 32, 0x100, -1, fake, fake, None) == 1
     assert lib.mrpop_validate_edges(fake, rb, fake, fake, 4, 32, 3, 4, fake, fake, None) == 1
     lib.mrpop_robotset_destroy(rb)
+
+
+def test_server_arguments_rejected_without_gpu(pkg, lib_path):
+    lib = pkg.library(path=lib_path)
+    h = C.c_void_p()
+    bad = pkg.mrpop.ServerConfig(1 << 20, 17, 0, 0)  # more than 16 launch slots
+    assert lib.mrpop_server_create(C.byref(bad), C.byref(h)) == 1
+    assert b"streams" in lib.mrpop_last_error()
+    assert lib.mrpop_server_create(None, None) == 1
+    assert lib.mrpop_session_open(None, 4, 64, 32, 0, C.byref(h)) == 1
+    assert lib.mrpop_session_submit(None, None) == 1
+    assert lib.mrpop_session_wait(None, 0) == 1
+    assert lib.mrpop_session_close(None) == 0
+    assert lib.mrpop_server_destroy(None) == 0
