@@ -357,6 +357,9 @@ typedef struct {
     int64_t waypoints;
     double cost;             /* path length, composite Euclidean                       */
     uint64_t digest;         /* FNV-1a of every verdict received, in order             */
+    int64_t start_tree;      /* nodes of the tree grown from the start                 */
+    int64_t goal_tree;       /* nodes of the tree grown from the goal                  */
+    int64_t validate_ns;     /* host wall time spent inside validate calls             */
 } mrpop_plan_result;
 
 mrpop_status mrpop_plan(int arms, const float *start, const float *goal, const mrpop_plan_settings *settings,

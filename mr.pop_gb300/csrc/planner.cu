@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -123,7 +124,10 @@ extern "C" mrpop_status mrpop_plan(int arms, const float *start, const float *go
     std::vector<int64_t> nn(B);
 
     auto check = [&](int64_t n, int rule, float range) -> int {
+        const auto t0 = std::chrono::steady_clock::now();
         const int rc = validate(ctx, q0.data(), q1.data(), n, S.granularity, rule, range, valid.data(), first.data());
+        out->validate_ns +=
+            std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
         out->steps++;
         out->edges += n;
         digest_add(digest, valid.data(), (size_t)n);
@@ -173,6 +177,8 @@ extern "C" mrpop_status mrpop_plan(int arms, const float *start, const float *go
             }
     }
     out->digest = digest;
+    out->start_tree = T[0].size();
+    out->goal_tree = T[1].size();
     if (ja < 0) return MRPOP_OK;
 
     // path: start .. goal

@@ -77,7 +77,8 @@ class PlanSettingsC(C.Structure):
 
 class PlanResultC(C.Structure):
     _fields_ = [("solved", C.c_int32), ("iterations", C.c_int32), ("steps", C.c_int32), ("edges", C.c_int64),
-                ("waypoints", C.c_int64), ("cost", C.c_double), ("digest", C.c_uint64)]
+                ("waypoints", C.c_int64), ("cost", C.c_double), ("digest", C.c_uint64), ("start_tree", C.c_int64),
+                ("goal_tree", C.c_int64), ("validate_ns", C.c_int64)]
 
 
 VALIDATE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_float,

@@ -61,11 +61,15 @@ class PlanResult:
     steps: int
     edges: int
     verdict_digest: int
+    start_tree: int = 0
+    goal_tree: int = 0
+    validate_ns: int = 0
 
 
 def result_from_c(qid: int, r: M.PlanResultC, path: np.ndarray) -> PlanResult:
     return PlanResult(qid, bool(r.solved), path, float(r.cost) if r.solved else math.inf, int(r.iterations),
-                      int(r.steps), int(r.edges), int(r.digest))
+                      int(r.steps), int(r.edges), int(r.digest), int(r.start_tree), int(r.goal_tree),
+                      int(r.validate_ns))
 
 
 def path_cost(path: np.ndarray) -> float:

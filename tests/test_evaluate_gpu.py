@@ -1,0 +1,35 @@
+"""The reference's problem sets through the benchmark driver on the GPU: every
+query plans through a session of the validation service, the CSV holds one
+row per problem, and every waypoint of a solved path is collision-free under
+the oracle."""
+import csv
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIXTURE = Path(__file__).resolve().parent / "golden" / "problems.npz"
+
+
+@pytest.mark.parametrize("arms", [4, 5])
+def test_problem_set_to_csv(cuda, pkg, orc, tmp_path, arms):
+    E, P = pkg.evaluate, pkg.planner
+    queries = E.fixture_queries(FIXTURE, arms)[:8]
+    settings = P.PlanSettings()
+    server = pkg.Server(budget_bytes=256 << 20, streams=2)
+    out = tmp_path / f"panda_{arms}.csv"
+    rows = E.run(server, queries, settings, out)
+    server.close()
+    rec = list(csv.reader(open(out), skipinitialspace=True))
+    assert len(rec) == 1 + len(queries) and all(len(r) == 19 for r in rec)
+    assert sum(r.solved for r in rows) >= 1
+    flags = pkg.CHECK_ENV | pkg.CHECK_SELF
+    for q, r in zip(queries, rows):
+        assert r.kernel_ns <= r.wall_ns
+        if not r.solved:
+            continue
+        assert np.array_equal(r.path[0], q.start) and np.array_equal(r.path[-1], q.goal)
+        chk = orc.validate(q.scene, q.bases, r.path, r.path, 1, flags, band=1e-5)
+        assert (chk["valid"].astype(bool) | chk["ambiguous"].astype(bool)).all()
