@@ -111,3 +111,34 @@ def write_csv(rows: list[Row], settings: PlanSettings, out_csv) -> None:
         f.write(CSV_HEADER)
         for r in rows:
             f.write(csv_row(r, settings))
+
+
+def main(argv=None) -> int:
+    """evaluate <robot_name> <run_name> [problems.json]: like the reference's
+    `evaluate_mr <robot_name> <run_name>` (evaluate_mr.cu:155-186), writing
+    test_output/<robot_name>_<run_name>.csv.  Without a problems file the
+    converted fixture of the reference's problem sets is used."""
+    import argparse
+    import sys
+    ap = argparse.ArgumentParser(prog="evaluate")
+    ap.add_argument("robot_name", choices=["panda_four", "panda_five"])
+    ap.add_argument("run_name")
+    ap.add_argument("problems", nargs="?", default=None)
+    ap.add_argument("--max-iters", type=int, default=PlanSettings.max_iters)
+    a = ap.parse_args(argv)
+    arms = 4 if a.robot_name == "panda_four" else 5
+    if a.problems:
+        from .problems import load_problems
+        queries = problem_queries(load_problems(a.problems), arms)
+    else:
+        queries = fixture_queries(Path(__file__).resolve().parents[1] / "tests" / "golden" / "problems.npz", arms)
+    settings = PlanSettings(max_iters=a.max_iters)
+    Path("test_output").mkdir(exist_ok=True)
+    out = Path("test_output") / f"{a.robot_name}_{a.run_name}.csv"
+    server = M.Server(budget_bytes=256 << 20, streams=2)
+    rows = run(server, queries, settings, out)
+    server.close()
+    failed = sum(not r.solved for r in rows)
+    print(f"Total failed: {failed} / {len(rows)}", file=sys.stdout)
+    print(f"wrote {out}")
+    return 0
