@@ -481,6 +481,8 @@ mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots,
 
 // 16 bytes of work counters, then per edge: flag words, candidate masks,
 // reference-sphere bounds and segment state.
+int robotset_arms(const mrpop_robotset *robots) { return robots ? robots->n_arms : 0; }
+
 size_t split_scratch_bytes(int64_t n_edges, int g, int A) {
     const int spl = g > 32 ? 2 : 1;
     return 2 * sizeof(unsigned long long) +

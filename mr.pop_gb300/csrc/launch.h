@@ -58,6 +58,9 @@ mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots,
 size_t split_scratch_bytes(int64_t n_edges, int g, int A);
 void set_split_scratch(EdgeParams &p, void *scratch, int64_t n_edges, int g, int A);
 
+// Arm count of a robot set (0 for null).
+int robotset_arms(const mrpop_robotset *robots);
+
 // Records msg as the calling thread's last error and returns st.
 mrpop_status fail_status(mrpop_status st, const char *msg);
 

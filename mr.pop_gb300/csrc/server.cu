@@ -592,6 +592,8 @@ extern "C" mrpop_status mrpop_session_plan(mrpop_session *ss, const mrpop_scene 
     if (!ss || !settings) return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_plan: null argument");
     if (std::max(settings->batch, settings->shortcut_pairs) > ss->max_edges || settings->granularity > ss->max_g)
         return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_plan: the session is smaller than the plan's steps");
+    if (mrpop::robotset_arms(robots) != ss->arms)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_plan: the robot set's arm count differs from the session's");
     SessionValidator v{ss, scene, robots, flags, 7 * ss->arms};
     return mrpop_plan(ss->arms, start, goal, settings, session_validate, &v, path_out, max_waypoints, out);
 }

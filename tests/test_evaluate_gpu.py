@@ -1,7 +1,9 @@
 """The reference's problem sets through the benchmark driver on the GPU: every
 query plans through a session of the validation service, the CSV holds one
-row per problem, and every waypoint of a solved path is collision-free under
-the oracle."""
+row per problem, and every waypoint of a solved path passes the oracle's
+single-configuration check (the waypoints were accepted under the
+reference's verdict rules, which can leave a sample without a detailed check;
+these problems do not meet that case)."""
 import csv
 from pathlib import Path
 

@@ -52,9 +52,11 @@ def test_plan_is_deterministic_and_connects_start_to_goal(pkg, orc, oracle_queri
         solved += 1
         assert np.array_equal(a.path[0], q.start) and np.array_equal(a.path[-1], q.goal)
         assert abs(a.cost - P.path_cost(a.path)) < 1e-9
-        # every waypoint is collision-free (each is the start, the goal or the
-        # last sample of an accepted extend edge; a waypoint within 1e-5 m of
-        # contact may round either way)
+        # every waypoint passes the single-configuration check (each is the
+        # start, the goal or the last sample of an accepted extend edge; the
+        # reference's verdict rules can leave a sample of an edge without a
+        # detailed check, which these problems do not meet; a waypoint within
+        # 1e-5 m of contact may round either way)
         r = orc.validate(q.scene, q.bases, a.path, a.path, 1, flags, band=1e-5)
         assert (r["valid"].astype(bool) | r["ambiguous"].astype(bool)).all()
     assert solved >= 1
