@@ -46,6 +46,10 @@ constexpr int kWaveCtasPerSm = 3;
 // launch from segment 0 instead of the split rounds (2 launches instead of
 // 2 * kSegRounds + 1: launch latency dominates small waves).
 constexpr int64_t kFusedOnlyEdges = 4096;
+// Work counters per group and wave: one per launch (split rounds + fused
+// tail), zeroed together with the parameter upload so that no launch needs a
+// memset of its own.
+constexpr int kCountersPerGroup = 2 * mrpop::kSegRounds + 1;
 constexpr int kGroupKeys = 4 * MRPOP_MAX_ARMS;
 constexpr size_t kAlign = 256;
 
@@ -95,6 +99,7 @@ struct mrpop_server {
     std::thread worker;
     mrpop_server_stats stats{};
     std::atomic<int64_t> launches{0};  // kernels enqueued (the worker adds, stats readers load)
+    std::map<uint64_t, int> occupancy;  // resident CTAs per SM by kernel and shared-memory size (worker only)
 };
 
 struct mrpop_session {
@@ -172,22 +177,30 @@ void CUDART_CB wave_done(void *arg) {
     s->cv.notify_all();
 }
 
-// One kernel of a group of the wave: its counter zeroed in stream order first.
-cudaError_t launch_one(int arms, bool seg, int spl, size_t smem, int mode, int seg0, const mrpop::EdgeParams *items,
-                       const int4 *chunks, int n_chunks, unsigned long long *work, int sms, cudaStream_t stream) {
+// One kernel of a group of the wave (its counter was zeroed by the wave's
+// upload).  The grid is the resident maximum, at most the chunk count; the
+// resident CTAs per SM are looked up once per kernel and shared-memory size
+// (the look-up also raises the kernel's shared-memory limit).
+cudaError_t launch_one(mrpop_server *s, int arms, bool seg, int spl, size_t smem, int mode, int seg0,
+                       const mrpop::EdgeParams *items, const int4 *chunks, int n_chunks, unsigned long long *work,
+                       cudaStream_t stream) {
     mrpop::BatchParams b;
     b.items = items;
     b.chunks = chunks;
     b.n_chunks = n_chunks;
     b.seg0 = seg0;
     b.work = work;
-    int nb = 0;
-    cudaError_t err = mrpop::batch_occupancy(arms, mode, seg, spl, smem, &nb);
-    if (err != cudaSuccess) return err;
-    const int grid = (int)std::max(1LL, std::min<long long>((long long)sms * std::max(nb, 1), n_chunks));
-    err = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream);
-    if (err == cudaSuccess) err = mrpop::launch_batch(arms, mode, seg, spl, b, smem, grid, stream);
-    return err;
+    const uint64_t key = ((uint64_t)smem << 16) | (uint64_t)(arms << 8 | mode << 4 | (seg ? 2 : 0) | (spl - 1));
+    auto it = s->occupancy.find(key);
+    if (it == s->occupancy.end()) {
+        int nb = 0;
+        const cudaError_t err = mrpop::batch_occupancy(arms, mode, seg, spl, smem, &nb);
+        if (err != cudaSuccess) return err;
+        it = s->occupancy.emplace(key, std::max(nb, 1)).first;
+    }
+    const int grid = (int)std::max(1LL, std::min<long long>((long long)s->sms * it->second, n_chunks));
+    s->launches++;
+    return mrpop::launch_batch(arms, mode, seg, spl, b, smem, grid, stream);
 }
 
 // Builds the wave's tables in the slot, uploads them and launches every group.
@@ -198,7 +211,7 @@ cudaError_t launch_wave(mrpop_server *s, mrpop_server::Slot &slot) {
     auto *d_work = reinterpret_cast<unsigned long long *>(slot.d_tab);
     auto *d_params = reinterpret_cast<mrpop::EdgeParams *>(slot.d_tab + s->tab_params_off);
     auto *d_chunks = reinterpret_cast<int4 *>(slot.d_tab + s->tab_chunks_off);
-    (void)h_work;
+    std::memset(h_work, 0, s->tab_params_off);
 
     struct Range {
         int p0 = 0, np = 0, c0 = 0, nc = 0;
@@ -237,7 +250,8 @@ cudaError_t launch_wave(mrpop_server *s, mrpop_server::Slot &slot) {
         r.np = np - r.p0;
         r.nc = nc - r.c0;
     }
-    cudaError_t err = cudaMemcpyAsync(d_params, h_params, (size_t)np * sizeof(mrpop::EdgeParams),
+    // work counters (zero) and parameter blocks in one copy, chunk lists in another
+    cudaError_t err = cudaMemcpyAsync(d_work, h_work, s->tab_params_off + (size_t)np * sizeof(mrpop::EdgeParams),
                                       cudaMemcpyHostToDevice, slot.stream);
     if (err == cudaSuccess)
         err = cudaMemcpyAsync(d_chunks, h_chunks, (size_t)nc * sizeof(int4), cudaMemcpyHostToDevice, slot.stream);
@@ -246,25 +260,24 @@ cudaError_t launch_wave(mrpop_server *s, mrpop_server::Slot &slot) {
         if (!r.np) continue;
         const int arms = 1 + key / 4, spl = 1 + key % 2;
         const bool seg = (key / 2) % 2 == 1;
-        unsigned long long *work = d_work + 4 * key;
+        unsigned long long *work = d_work + (size_t)kCountersPerGroup * key;
+        const mrpop::EdgeParams *items = d_params + r.p0;
+        const int4 *chunks = d_chunks + r.c0;
         if (seg && r.edges <= kFusedOnlyEdges) {
-            s->launches += 1;
-            err = launch_one(arms, seg, spl, r.smem, mrpop::kBatchFused, 0, d_params + r.p0, d_chunks + r.c0, r.nc,
-                             work + 2, s->sms, slot.stream);
+            err = launch_one(s, arms, seg, spl, r.smem, mrpop::kBatchFused, 0, items, chunks, r.nc, work, slot.stream);
             continue;
         }
         const int rounds = seg ? mrpop::kSegRounds : 1;
-        s->launches += 2 * rounds + (seg ? 1 : 0);
         for (int rd = 0; rd < rounds && err == cudaSuccess; rd++) {
-            err = launch_one(arms, seg, spl, r.smem, mrpop::kBatchBroad, rd, d_params + r.p0, d_chunks + r.c0, r.nc,
-                             work + 0, s->sms, slot.stream);
+            err = launch_one(s, arms, seg, spl, r.smem, mrpop::kBatchBroad, rd, items, chunks, r.nc, work + 2 * rd,
+                             slot.stream);
             if (err == cudaSuccess)
-                err = launch_one(arms, seg, spl, r.smem, mrpop::kBatchNarrow, rd, d_params + r.p0, d_chunks + r.c0,
-                                 r.nc, work + 1, s->sms, slot.stream);
+                err = launch_one(s, arms, seg, spl, r.smem, mrpop::kBatchNarrow, rd, items, chunks, r.nc,
+                                 work + 2 * rd + 1, slot.stream);
         }
         if (err == cudaSuccess && seg)
-            err = launch_one(arms, seg, spl, r.smem, mrpop::kBatchFused, mrpop::kSegRounds, d_params + r.p0,
-                             d_chunks + r.c0, r.nc, work + 2, s->sms, slot.stream);
+            err = launch_one(s, arms, seg, spl, r.smem, mrpop::kBatchFused, mrpop::kSegRounds, items, chunks, r.nc,
+                             work + 2 * rounds, slot.stream);
     }
     return err;
 }
@@ -386,7 +399,7 @@ mrpop_status mrpop_server_create(const mrpop_server_config *cfg, mrpop_server **
         return fail(MRPOP_ERR_OUT_OF_MEMORY, std::string("server_create: host arena: ") + cudaGetErrorString(err));
     }
     s->free_host[0] = harena;
-    s->tab_params_off = round_up(kGroupKeys * 4 * sizeof(unsigned long long));
+    s->tab_params_off = round_up(kGroupKeys * kCountersPerGroup * sizeof(unsigned long long));
     s->tab_chunks_off = round_up(s->tab_params_off + (size_t)c.max_wave_steps * sizeof(mrpop::EdgeParams));
     s->tab_bytes = round_up(s->tab_chunks_off + (size_t)c.max_wave_chunks * sizeof(int4));
     s->slots.resize(c.streams);
