@@ -45,3 +45,23 @@ def test_csv_layout_and_oracle_plan(pkg, orc):
         back = np.array([[float(v) for v in c.split()] for c in cfgs], np.float32)
         assert back.shape == res.path.shape
         assert np.allclose(back, res.path, atol=1e-5 * (1 + np.abs(res.path)).max())
+
+
+def test_queries_from_a_problem_file(pkg):
+    """A problem dict in the reference's file format becomes a query with its
+    scene, start, first goal and arm bases."""
+    import json
+    E = pkg.evaluate
+    prob = {"name": "bins", "valid": True, "source_index": 7,
+            "start": [0.0] * 28, "goals": [[0.1] * 28, [0.2] * 28],
+            "box": [{"position": [0.5, 0.0, 0.3], "orientation_euler_xyz": [0.0, 0.0, 0.3],
+                     "half_extents": [0.1, 0.2, 0.05]}],
+            "base_positions": [[0.5, 0.5, 0.0], [-0.5, 0.5, 0.0], [-0.5, -0.5, 0.0], [0.5, -0.5, 0.0]],
+            "base_orientation_wxyz": [[1.0, 0.0, 0.0, 0.0]] * 4}
+    probs = pkg.problems.load_problems(json.dumps([prob, dict(prob, valid=False)]))
+    qs = E.problem_queries(probs, 4)
+    assert len(qs) == 1
+    q = qs[0]
+    assert q.qid == 7 and q.arms == 4 and len(q.scene.cuboids) == 1
+    assert np.allclose(q.goal, 0.1) and q.bases.shape == (4, 4, 4)
+    assert np.allclose(q.bases[1][:3, 3], [-0.5, 0.5, 0.0])

@@ -80,3 +80,39 @@ def test_validator_error_aborts_the_plan(pkg, oracle_queries):
 
     with pytest.raises(RuntimeError, match="validator down"):
         pkg.planner.plan(q, broken)
+
+
+def test_bad_settings_rejected(pkg, oracle_queries):
+    P = pkg.planner
+    q = oracle_queries[0]
+
+    def never(q0, q1, g, rule, range_):
+        raise AssertionError("no step may run")
+
+    for bad in (P.PlanSettings(batch=0), P.PlanSettings(granularity=65), P.PlanSettings(step=0.0),
+                P.PlanSettings(range=-1.0), P.PlanSettings(shortcut_pairs=0)):
+        with pytest.raises(pkg.MrpopError) as ei:
+            P.plan(q, never, bad)
+        assert ei.value.status == 1 and "settings" in str(ei.value)
+
+
+def test_zero_iterations_returns_unsolved(pkg, oracle_queries):
+    P = pkg.planner
+    q = oracle_queries[0]
+    r = P.plan(q, lambda *a: (_ for _ in ()).throw(AssertionError("no step")), P.PlanSettings(max_iters=0))
+    assert not r.solved and r.steps == 0 and r.start_tree == 1 and r.goal_tree == 1 and len(r.path) == 0
+
+
+def test_served_summary_and_comparison(pkg):
+    P, S = pkg.planner, pkg.serving
+    path = np.zeros((3, 14), np.float32)
+    a = P.PlanResult(0, True, path, 1.0, 2, 5, 100, 7)
+    b = P.PlanResult(0, True, path.copy(), 1.0, 2, 5, 100, 7)
+    c = P.PlanResult(0, True, path + 1, 1.0, 2, 5, 100, 7)
+    d = P.PlanResult(0, True, path.copy(), 1.0, 2, 5, 100, 8)
+    assert S.same_result(a, b) and not S.same_result(a, c) and not S.same_result(a, d)
+    served = [S.Served(a, 0.0, 0.0, 0.010), S.Served(P.PlanResult(1, False, path[:0], float("inf"), 60, 120, 9000, 1),
+                                                     1.0, 1.0, 1.050)]
+    s = S.summary(served)
+    assert s["queries"] == 2 and s["solve_rate"] == 0.5 and s["mean_cost"] == 1.0
+    assert abs(s["p50_ms"] - 30.0) < 1e-9 and s["steps"] == 125 and s["edges"] == 9100
