@@ -6,7 +6,7 @@ pattern of the reference's planner (whose dRRT/AO-x, Planners.hh:57-64, is not
 rebuilt).  `plan()` runs it with a Python validator (the oracle in the CPU
 tests); `Session.plan` runs it with every step validated by the service.
 
-`make_queries` draws the config-5 queries: 2-5 Pandas facing the centre of a
+`make_queries` draws the served-planning queries: 2-5 Pandas facing the centre of a
 fresh seeded scene from the single-arm or bin-picking generator, start and goal
 rejection-sampled collision-free.
 """
