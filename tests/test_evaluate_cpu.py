@@ -65,3 +65,27 @@ def test_queries_from_a_problem_file(pkg):
     assert q.qid == 7 and q.arms == 4 and len(q.scene.cuboids) == 1
     assert np.allclose(q.goal, 0.1) and q.bases.shape == (4, 4, 4)
     assert np.allclose(q.bases[1][:3, 3], [-0.5, 0.5, 0.0])
+
+
+def test_oracle_driven_plans_match_the_gb300_rows(pkg, orc):
+    """The planner with the oracle as its validator reproduces the rows that the
+    problem-set driver wrote on a GB300 (tests/golden/make_planner_golden.py):
+    every verdict along these plans agreed between the oracle and the kernels."""
+    import json
+    E, P = pkg.evaluate, pkg.planner
+    gold = json.loads((FIXTURE.parent / "planner_gb300_panda_four.json").read_text())
+    queries = E.fixture_queries(FIXTURE, gold["arms"])
+    settings = P.PlanSettings(max_iters=gold["max_iters"])
+    flags = pkg.CHECK_ENV | pkg.CHECK_SELF
+    for idx, want in gold["rows"].items():
+        q = queries[int(idx)]
+
+        def validate(q0, q1, g, rule, range_, q=q):
+            r = orc.validate(q.scene, q.bases, q0, q1, g, flags, -1, rule, range_)
+            return r["valid"], r["first_hit"]
+
+        r = P.plan(q, validate, settings)
+        row = E.Row(r.solved, r.cost, r.path, r.start_tree, r.goal_tree, r.iterations, 0, 0)
+        got = next(csv.reader(io.StringIO(E.csv_row(row, settings)), skipinitialspace=True))
+        assert got[:6] == [want[k] for k in ("solved", "cost", "path_length", "start_tree_size",
+                                             "goal_tree_size", "iters")], idx
