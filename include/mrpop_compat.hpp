@@ -19,6 +19,9 @@
 //                                     d_valid, d_first, stream));
 #pragma once
 
+#include <algorithm>
+#include <chrono>
+#include <cstddef>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -130,6 +133,64 @@ inline void validate_connect(const mrpop_scene *s, const mrpop_robotset *r, cons
                              int32_t *n_seg = nullptr, void *stream = nullptr) {
     check(mrpop_validate_segments(s, r, q0, q1, n, g, MRPOP_RULE_CONNECT, range, MRPOP_CHECK_ENV | MRPOP_CHECK_SELF,
                                   -1, valid, first_hit, n_seg, stream));
+}
+
+// Serving: RAII handles for the validation service and its sessions, and a
+// served solve that fills a PlannerResult-shaped struct (the member names of
+// the reference's PlannerResult<Robot>, Planners.hh:14-32) from the library's
+// planner.  Config is the reference's Robot::Configuration (std::array<float, D>).
+struct ServerDeleter {
+    void operator()(mrpop_server *s) const { mrpop_server_destroy(s); }
+};
+struct SessionDeleter {
+    void operator()(mrpop_session *s) const { mrpop_session_close(s); }
+};
+using ServerPtr = std::unique_ptr<mrpop_server, ServerDeleter>;
+using SessionPtr = std::unique_ptr<mrpop_session, SessionDeleter>;
+
+inline ServerPtr make_server(int64_t budget_bytes = 0, int streams = 0, int64_t host_bytes = 0) {
+    mrpop_server_config c{};
+    c.budget_bytes = budget_bytes;
+    c.streams = streams;
+    c.host_bytes = host_bytes;
+    mrpop_server *s = nullptr;
+    check(mrpop_server_create(&c, &s));
+    return ServerPtr(s);
+}
+
+inline SessionPtr open_session(mrpop_server *server, int arms, int64_t max_edges, int max_granularity,
+                               int64_t timeout_ms = -1) {
+    mrpop_session *ss = nullptr;
+    check(mrpop_session_open(server, arms, max_edges, max_granularity, timeout_ms, &ss));
+    return SessionPtr(ss);
+}
+
+template <class Result, class Config>
+inline Result solve_served(mrpop_session *ss, const mrpop_scene *s, const mrpop_robotset *r, const Config &start,
+                           const Config &goal, const mrpop_plan_settings &ps,
+                           uint32_t flags = MRPOP_CHECK_ENV | MRPOP_CHECK_SELF, int64_t max_waypoints = 4096) {
+    const size_t dof = start.size();
+    std::vector<float> path((size_t)max_waypoints * dof);
+    mrpop_plan_result pr{};
+    const auto t0 = std::chrono::steady_clock::now();
+    check(mrpop_session_plan(ss, s, r, flags, start.data(), goal.data(), &ps, path.data(), max_waypoints, &pr));
+    Result out{};
+    out.solved = pr.solved != 0;
+    for (int64_t i = 0; i < std::min(pr.waypoints, max_waypoints); i++) {
+        Config c{};
+        std::copy(path.begin() + i * dof, path.begin() + (i + 1) * dof, c.begin());
+        out.path.push_back(c);
+    }
+    out.start_tree_size = (int)pr.start_tree;
+    out.goal_tree_size = (int)pr.goal_tree;
+    out.path_length = (int)out.path.size();
+    out.iters = pr.iterations;
+    out.cost = (float)pr.cost;
+    out.wall_ns = (std::size_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
+                      std::chrono::steady_clock::now() - t0).count();
+    out.kernel_ns = (std::size_t)pr.validate_ns;  // time spent waiting on the service's validation
+    out.copy_ns = 0;                              // session buffers are read and written in place
+    return out;
 }
 
 inline void validate_roadmap(const mrpop_scene *s, const mrpop_robotset *r, int robot_id, const float *q0,

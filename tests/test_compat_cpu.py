@@ -10,8 +10,10 @@ import pytest
 ROOT = Path(__file__).resolve().parents[1]
 
 PROGRAM = textwrap.dedent(r'''
+    #include <array>
     #include <cstdio>
     #include <string>
+    #include <vector>
     #include "mrpop_compat.hpp"
     // look-alike of the reference's shape structs (name/min_distance first)
     struct Shape { std::string name; float min_distance; };
@@ -27,7 +29,23 @@ PROGRAM = textwrap.dedent(r'''
         Cuboid *cuboids; unsigned num_cuboids;
         Cuboid *z_aligned_cuboids; unsigned num_z_aligned_cuboids;
     };
-    int main() {
+    // look-alike of the reference's PlannerResult<Robot> (Planners.hh:14-32)
+    struct Result {
+        bool solved = false;
+        std::vector<std::array<float, 28>> path;
+        int start_tree_size = 0, goal_tree_size = 0, path_length = 0, iters = 0;
+        float cost = 0.0f;
+        std::size_t wall_ns = 0, kernel_ns = 0, copy_ns = 0;
+    };
+    // compiled, not called: serving needs a GPU
+    Result served(mrpop_session *ss, const mrpop_scene *s, const mrpop_robotset *r) {
+        std::array<float, 28> a{}, b{};
+        mrpop_plan_settings ps = {64, 60, 32, 5, 32, 1.0f, 1.0f, 42};
+        return mrpop::solve_served<Result>(ss, s, r, a, b, ps);
+    }
+    int main(int argc, char **) {
+        if (argc > 5) served(nullptr, nullptr, nullptr);
+        try { mrpop::make_server(1 << 20, 17); return 6; } catch (const std::runtime_error &) {}
         Sphere s[1]; s[0].x = 1; s[0].y = 2; s[0].z = 3; s[0].r = 0.5f; s[0].name = "ball";
         Capsule c[1] = {}; c[0].x1 = 0.1f; c[0].zv = 0.4f; c[0].r = 0.05f; c[0].rdv = 6.25f;
         Cuboid b[2] = {}; b[1].x = 7; b[1].axis_1_x = 1; b[1].axis_2_y = 1; b[1].axis_3_z = 1; b[1].axis_3_r = 0.25f;
