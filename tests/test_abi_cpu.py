@@ -65,3 +65,20 @@ def test_server_arguments_rejected_without_gpu(pkg, lib_path):
     assert lib.mrpop_session_wait(None, 0) == 1
     assert lib.mrpop_session_close(None) == 0
     assert lib.mrpop_server_destroy(None) == 0
+
+
+def test_session_and_plan_entry_points_reject_null_handles(pkg, lib_path):
+    """The bindings of the serving and planning entry points marshal their
+    arguments (checked on the CPU: null handles are refused before any device work)."""
+    lib = pkg.library(path=lib_path)
+    p = [C.c_void_p() for _ in range(4)]
+    assert lib.mrpop_session_host_buffers(None, *[C.byref(x) for x in p]) == 1
+    st = pkg.mrpop.PlanSettingsC(64, 60, 32, 5, 32, 1.0, 1.0, 7)
+    res = pkg.mrpop.PlanResultC()
+    start = (C.c_float * 28)()
+    assert lib.mrpop_session_plan(None, None, None, 3, start, start, C.byref(st), None, 0, C.byref(res)) == 1
+    assert lib.mrpop_plan(4, start, start, C.byref(st), pkg.mrpop.VALIDATE_FN(), None, None, 0, C.byref(res)) == 1
+    assert lib.mrpop_plan(6, start, start, C.byref(st), pkg.mrpop.VALIDATE_FN(lambda *a: 0), None, None, 0,
+                          C.byref(res)) == 1
+    stats = pkg.mrpop.ServerStats()
+    assert lib.mrpop_server_get_stats(None, C.byref(stats)) == 1
