@@ -264,10 +264,11 @@ mrpop_status mrpop_batch_destroy(mrpop_batch *batch);
  * memory and must stay valid until the step is done) and waits for it
  * (mrpop_session_wait; timeout_ms as above, MRPOP_ERR_DEVICE_TIMEOUT if the
  * step is still running).  The worker gathers the steps pending from all
- * sessions, in submission order, into a wave (up to max_wave_steps steps and
- * max_wave_chunks chunks of 96 edges) and launches it as one set of persistent
- * batch kernels on the next free slot's stream, so waves formed while others
- * run overlap on the device.  Each step's verdicts equal the same
+ * sessions, in submission order, into a wave (up to max_wave_steps steps, and
+ * up to max_wave_chunks chunks counted at 96 edges each), cuts it into chunks of
+ * 6 to 96 edges so that even a small wave spreads over the SMs, and launches it
+ * as one set of persistent batch kernels on the next free slot's stream, so
+ * waves formed while others run overlap on the device.  Each step's verdicts equal the same
  * mrpop_validate_edges / mrpop_validate_segments call made alone.
  * mrpop_session_close waits for the session's step and returns its memory to
  * the arena.  Sessions may be used from different host threads; one session
@@ -333,7 +334,8 @@ mrpop_status mrpop_session_host_buffers(mrpop_session *session, float **q0, floa
  * mrpop_session_plan runs it with its steps validated by the session (scene,
  * robots and flags as for mrpop_validate_edges, composite check), in the
  * session's host buffers; the session must allow max(batch, shortcut_pairs)
- * edges of 7 * arms at the settings' granularity.
+ * edges at the settings' granularity, and the robot set must have the
+ * session's arm count.
  */
 typedef int (*mrpop_validate_fn)(void *ctx, const float *q0, const float *q1, int64_t n_edges, int granularity,
                                  int rule, float range, uint8_t *valid, int32_t *first_hit);
