@@ -51,14 +51,17 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
-    ap.add_argument("--workload", choices=["config1", "config2", "config3", "config3s", "config4", "config5"],
+    ap.add_argument("--workload", choices=["config1", "config2", "config3", "config3s", "config4", "config5",
+                                           "planner4", "planner5"],
                     default="config2")
+    ap.add_argument("--problems", type=int, default=50, help="planner4/5: reference problems solved")
     ap.add_argument("--rate", type=float, default=200.0, help="config5: query arrivals per second (Poisson)")
     ap.add_argument("--duration", type=float, default=60.0, help="config5: seconds of arrivals")
     ap.add_argument("--isolated", type=int, default=100, help="config5: queries also solved alone, for comparison")
     ap.add_argument("--instances", type=int, default=512, help="config4: planning instances in the batch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle parity counts (CPU leg)")
     return ap.parse_args()
 
 
@@ -232,21 +235,55 @@ def roofline(kt: dict, flops: dict, peak: float, workload: str, arms: int, spl: 
     kt: {kind: (launches, total ms)} from the library's event timing over
     `steps` steps; flops: algorithmic flops per step of each kind (a kind may
     launch more than once per step: segment rounds); sm_mhz: the median SM
-    clock sampled over the timed region (for the issue-rate figure)."""
+    clock sampled over the timed region.
+
+    The kernels are bound by instruction issue (FP32 is about a third of what
+    they issue; the rest is integer, shared-memory, vote and branch work, and
+    culling skips most of the algorithmic flops), so `frac` is the dominant
+    kernel's warp-instruction rate against 4 schedulers x SMs x the sampled
+    clock.  The FP32 view -- executed FP32 flops against the measured FP32
+    FMA peak, and the algorithmic (unculled) flop rate, which can exceed that
+    peak because culling skips work -- is kept under `fp32`."""
+    import torch
     ran = {k: v for k, v in kt.items() if v[0] > 0}
     total_ms = sum(v[1] for v in ran.values())
     dom = max(ran, key=lambda k: ran[k][1])
     launches, ms = ran[dom]
     launch_s = ms / launches / 1e3
-    achieved = flops[dom] / (ms / steps / 1e3) / 1e12
+    algorithmic = flops[dom] / (ms / steps / 1e3) / 1e12
     prof = committed_profile(KERNEL_NAMES[dom], workload)
-    out = {"bound": "fp32", "kernel": f"{KERNEL_NAMES[dom]}<{arms},{spl}>", "achieved": achieved, "peak": peak,
-           "unit": "TFLOP/s", "frac": achieved / peak, "traffic": prof.get("dram_bytes_per_launch"),
-           "launch_ms": launch_s * 1e3, "launches_per_step": launches / steps, "share": ms / total_ms,
-           "peak_source": "measured: FP32 FMA loop (mrpop_fp32_peak_probe) timed in this run; "
-                          "MEASURED_PEAKS.json has no FP32 figure",
-           "achieved_basis": f"{flops[dom]:.4g} algorithmic flops per step (FMA=2, unculled per-test costs) / "
-                             f"the kernel's CUDA-event time per step on the launching stream"}
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = sm_mhz
+    if not mhz and (ROOT / "MEASURED_PEAKS.json").exists():
+        mhz = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("sm_max_mhz")
+    out = {"bound": "issue", "kernel": f"{KERNEL_NAMES[dom]}<{arms},{spl}>", "achieved": None, "peak": None,
+           "unit": "warp instructions/s", "frac": None, "traffic": prof.get("dram_bytes_per_launch"),
+           "launch_ms": launch_s * 1e3, "launches_per_step": launches / steps, "share": ms / total_ms}
+    if prof.get("warp_instructions") and mhz:
+        # every SM has four schedulers that issue at most one warp instruction per clock
+        rate = prof["warp_instructions"] / launch_s
+        cap = 4 * sms * mhz * 1e6
+        out.update({"achieved": rate, "peak": cap, "frac": rate / cap,
+                    "peak_source": f"4 schedulers x {sms} SMs x {mhz:.0f} MHz (median SM clock sampled in the "
+                                   f"timed region)",
+                    "achieved_basis": "warp instructions of one launch (ncu smsp__inst_executed.sum, committed "
+                                      f"profile profiles/{KERNEL_NAMES[dom]}_{workload}.json) / the kernel's "
+                                      "CUDA-event launch time in this run"})
+    else:
+        out["frac_note"] = f"no committed ncu instruction count for {KERNEL_NAMES[dom]} on {workload}"
+    fp32 = {"peak_tflops": peak,
+            "peak_source": "measured: FP32 FMA loop (mrpop_fp32_peak_probe) timed in this run; "
+                           "MEASURED_PEAKS.json has no FP32 figure",
+            "algorithmic_rate_tflops": algorithmic,
+            "algorithmic_basis": f"{flops[dom]:.4g} algorithmic flops per step (FMA=2, unculled per-test costs) / "
+                                 f"the kernel's CUDA-event time per step; not a fraction of anything: culling "
+                                 f"skips most of this work"}
+    if prof.get("executed_fp32_flops_per_launch"):
+        ex = prof["executed_fp32_flops_per_launch"] / launch_s / 1e12
+        fp32["executed"] = {"achieved_tflops": ex, "frac": ex / peak,
+                            "basis": "FP32 flops the kernel executed (ncu: 2*ffma + fadd + fmul thread "
+                                     "instructions, committed profile) / live launch time"}
+    out["fp32"] = fp32
     if out["traffic"]:
         hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs") \
             if (ROOT / "MEASURED_PEAKS.json").exists() else None
@@ -254,26 +291,40 @@ def roofline(kt: dict, flops: dict, peak: float, workload: str, arms: int, spl: 
         out["hbm_check"] = {"achieved_gbs": bw, "peak_gbs": hbm, "frac": bw / hbm if hbm else None,
                             "basis": "ncu DRAM bytes of one launch / live launch time, against the measured copy "
                                      "bandwidth (MEASURED_PEAKS.json): HBM is not the bound"}
-    if prof.get("executed_fp32_flops_per_launch"):
-        ex = prof["executed_fp32_flops_per_launch"] / launch_s / 1e12
-        out["executed"] = {"achieved": ex, "frac": ex / peak,
-                           "basis": "FP32 flops the kernel executed (ncu: 2*ffma + fadd + fmul thread "
-                                    "instructions) / live launch time; culling skips algorithmic work"}
-    if prof.get("warp_instructions") and sm_mhz:
-        # every SM has four schedulers that issue at most one warp instruction per clock
-        import torch
-        sms = torch.cuda.get_device_properties(0).multi_processor_count
-        rate = prof["warp_instructions"] / launch_s
-        cap = 4 * sms * sm_mhz * 1e6
-        out["issue"] = {"achieved": rate, "peak": cap, "unit": "warp instructions/s", "frac": rate / cap,
-                        "basis": "warp instructions of one launch (ncu smsp__inst_executed.sum, committed profile) / "
-                                 "live launch time, against 4 schedulers x SMs x the median SM clock sampled "
-                                 "in the timed region: the kernel is bound by instruction issue and latency, "
-                                 "not by FP32 throughput or HBM"}
     out["kernels"] = {KERNEL_NAMES[k]: {"launches": v[0], "avg_ms": v[1] / v[0], "share": v[1] / total_ms,
                                         "algorithmic_tflops": flops[k] / (v[1] / steps / 1e3) / 1e12}
                       for k, v in ran.items()}
     return out
+
+
+def parity_counts(orc, pkg, torch, wl, valid: np.ndarray, first: np.ndarray, band: float = 1e-5) -> dict:
+    """Verdicts of the timed run against the oracle over the whole workload,
+    with the near-contact samples counted: a sample is ambiguous when a
+    deciding minimum signed distance (FP64) lies within `band` of zero, and a
+    verdict may differ only on an edge holding such a sample.  Edges that
+    differ from the host-trig oracle without being ambiguous are checked again
+    with the device's __sinf/__cosf values replayed into the oracle."""
+    t = time.perf_counter()
+    o = orc.validate(wl.scene, wl.bases, wl.q0, wl.q1, wl.granularity, wl.flags, wl.arm, wl.rule, wl.range_,
+                     band=band, threads=orc.max_threads(), count_ambiguous=True)
+    amb = o["ambiguous"].astype(bool)
+    diff = (valid != o["valid"]) | (first != o["first_hit"])
+    idx = np.nonzero(diff & ~amb)[0]
+    replay = 0
+    if len(idx):
+        def dev_trig(x):
+            c, s = pkg.debug_trig(torch.from_numpy(x).cuda())
+            torch.cuda.synchronize()
+            return c.cpu().numpy(), s.cpu().numpy()
+        r = orc.validate_with_trig(wl.scene, wl.bases, wl.q0[idx], wl.q1[idx], wl.granularity, wl.flags, wl.arm,
+                                   wl.rule, wl.range_, dev_trig)
+        replay = int(((valid[idx] != r["valid"]) | (first[idx] != r["first_hit"])).sum())
+    return {"against": "oracle/edge_oracle.c: FP32 restatement of the reference's edge check (host sinf/cosf; "
+                       "the device uses __sinf/__cosf), FP64 distances for the ambiguity band",
+            "edges": int(len(valid)), "edges_differ": int(diff.sum()),
+            "edges_differ_unambiguous": int(len(idx)), "edges_differ_after_device_trig_replay": replay,
+            "ambiguous_edges": int(amb.sum()), "ambiguous_samples": int(o["amb_samples"].sum()), "band_m": band,
+            "invalid_edges": int((valid == 0).sum()), "oracle_s": round(time.perf_counter() - t, 1)}
 
 
 def run_batch(args, world, rank, local, pkg, torch):
@@ -480,6 +531,93 @@ def run_serving(args, world, rank, local, pkg, torch):
     print(json.dumps(out), flush=True)
 
 
+def planner_summary(rows: list[dict]) -> dict:
+    """Solve rate, costs and latencies of a list of per-problem results."""
+    solved = [r for r in rows if r["solved"]]
+    k = np.array([r["kernel_ns"] for r in rows if "kernel_ns" in r], np.float64) / 1e6
+    w = np.array([r["wall_ns"] for r in rows if "wall_ns" in r], np.float64) / 1e6
+    c = np.array([r["cost"] for r in solved], np.float64)
+    return {"problems": len(rows), "solved": len(solved), "solve_rate": len(solved) / max(1, len(rows)),
+            "cost_median": float(np.median(c)) if len(c) else None,
+            "cost_mean": float(c.mean()) if len(c) else None,
+            "kernel_ms_p50": float(np.percentile(k, 50)) if len(k) else None,
+            "kernel_ms_p99": float(np.percentile(k, 99)) if len(k) else None,
+            "wall_ms_p50": float(np.percentile(w, 50)) if len(w) else None,
+            "wall_ms_p99": float(np.percentile(w, 99)) if len(w) else None}
+
+
+def planner_line(args, impl: str, rows: list[dict], extra: dict) -> dict:
+    sm = planner_summary(rows)
+    arms = 4 if args.workload == "planner4" else 5
+    out = {"metric": "dRRT/AO-x solve latency p50 (kernel_ns, the reference's timer)", "value": sm["kernel_ms_p50"],
+           "unit": "ms", "n_gpus": 1, "steps": len(rows), "warmup": 1, "ms_per_step": sm["kernel_ms_p50"],
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "the reference's benchmark problems (scripts/panda_{four,five}_problems.json, converted fixture)",
+           "config": {"workload": f"planner_{arms}panda_{len(rows)}_problems",
+                      "settings": "evaluate_mr: 300 attempts per iteration, g=64, range 2.0, 3 AO-x passes, "
+                                  "8 roadmap blocks per arm"},
+           "planner": sm, "e2e": {"value": sm["wall_ms_p50"], "unit": "ms", "h2d_bytes_per_step": None,
+                                  "d2h_bytes_per_step": None,
+                                  "path": "host wall clock of one whole solve call per problem"}}
+    if impl == "reference":
+        out["impl"] = "reference"
+    out["config"].update(extra)
+    return out
+
+
+def run_planner(args, pkg, torch):
+    """The reference's planner rebuilt on the batched validator (dRRT::solve,
+    mrpop_drrt_solve) over the reference's benchmark problems."""
+    arms = 4 if args.workload == "planner4" else 5
+    z = np.load(ROOT / "tests" / "golden" / "problems.npz")
+    n = min(args.problems, int(z[f"n{arms}"]))
+    st = pkg.drrt.evaluate_settings()
+    rb = pkg.RobotSet(arms)  # the reference's compiled-in bases, as its driver places the arms
+    # warm-up: first-use set-up of the library and the device
+    pkg.drrt.solve(pkg.Scene(pkg.SceneArrays(cuboids=z[f"a{arms}_p0_boxes"])), rb, z[f"a{arms}_p0_start"],
+                   z[f"a{arms}_p0_goal"], pkg.drrt.evaluate_settings(rrtc_iter=1))
+    clocks = ClockSampler(0)
+    clocks.start()
+    rows = []
+    for p in range(n):
+        scene = pkg.Scene(pkg.SceneArrays(cuboids=z[f"a{arms}_p{p}_boxes"]))
+        t0 = time.perf_counter_ns()
+        r = pkg.drrt.solve(scene, rb, z[f"a{arms}_p{p}_start"], z[f"a{arms}_p{p}_goal"], st)
+        wall = time.perf_counter_ns() - t0
+        rows.append({"problem": p, "solved": r.solved, "cost": r.cost, "kernel_ns": r.stats["kernel_ns"],
+                     "wall_ns": wall, "iterations": r.stats["iterations"], "edges": r.stats["edges_validated"],
+                     "validate_ns": r.stats["validate_ns"], "nn_ns": r.stats["nn_ns"]})
+    clk = clocks.stop()
+    edges = sum(r["edges"] for r in rows)
+    out = planner_line(args, "mine", rows, {"validated_edges": edges,
+                                            "validate_share_of_kernel_ns": sum(r["validate_ns"] for r in rows) /
+                                            max(1, sum(r["kernel_ns"] for r in rows)),
+                                            "nn_share_of_kernel_ns": sum(r["nn_ns"] for r in rows) /
+                                            max(1, sum(r["kernel_ns"] for r in rows))})
+    out["clocks"] = clk
+    out["gpu_launches"] = None
+    out["per_problem"] = [{k: r[k] for k in ("problem", "solved", "cost", "kernel_ns")} for r in rows]
+    print(json.dumps(out), flush=True)
+
+
+def run_reference_planner(args, torch):
+    """The reference's own planner kernels (oracle/ref_planner.py) on the same problems."""
+    import subprocess as sp
+    import tempfile
+    arms = 4 if args.workload == "planner4" else 5
+    with tempfile.TemporaryDirectory() as d:
+        out_path = Path(d) / "ref.jsonl"
+        sp.run([sys.executable, "-m", "oracle.ref_planner_eval", str(arms), str(out_path), "--first",
+                str(args.problems)], cwd=str(ROOT), check=False, stdout=sp.DEVNULL)
+        rows = [json.loads(l) for l in open(out_path)] if out_path.exists() else []
+    line = planner_line(args, "reference", rows, {
+        "harness": "the reference's pop_planner.cu / path_processing.cu / path_simplification.cu compiled "
+                   "unmodified for sm_103a; its host loop restated with bounds (oracle/ref_planner.py)"})
+    line["per_problem"] = [{k: r.get(k) for k in ("problem", "solved", "cost", "kernel_ns", "stopped")} for r in rows]
+    line["gpu_launches"] = None
+    print(json.dumps(line), flush=True)
+
+
 def run_mine(args, world, rank, local):
     import torch
     import __graft_entry__ as ge
@@ -492,6 +630,8 @@ def run_mine(args, world, rank, local):
         return run_serving(args, world, rank, local, pkg, torch)
     if args.workload == "config4":
         return run_batch(args, world, rank, local, pkg, torch)
+    if args.workload in ("planner4", "planner5"):
+        return run_planner(args, pkg, torch) if rank == 0 else None
     wl = load_workload(pkg, args.workload)
     scene = pkg.Scene(wl.scene)
     robots = pkg.RobotSet(len(wl.bases), wl.bases)
@@ -593,6 +733,9 @@ def run_mine(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as orc
         out["cpu_baseline"] = cpu_baseline(orc, wl, min(n, 65536))
+        if not args.no_parity:
+            # outside the timed region: the last timed step's verdicts against the oracle
+            out["parity"] = parity_counts(orc, pkg, torch, wl, valid.cpu().numpy(), first.cpu().numpy())
     if rank == 0:
         print(json.dumps(out), flush=True)
 
@@ -644,6 +787,14 @@ def run_reference(args, world, rank, local):
     pkg = ge.load_package()
     from oracle import oracle as orc
     from oracle import ref_runner
+    if args.workload in ("planner4", "planner5"):
+        from oracle import ref_planner
+        if not ref_planner.available():
+            print(json.dumps({"impl": "reference", "metric": "dRRT/AO-x solve latency p50", "unit": "ms",
+                              "higher_is_better": False,
+                              "unavailable": "reference planner cubin not built (oracle/_ref)"}), flush=True)
+            return
+        return run_reference_planner(args, torch)
     if args.workload == "config5":
         print(json.dumps({"impl": "reference", "metric": "served p99 plan latency", "unit": "ms",
                           "higher_is_better": False,

@@ -625,8 +625,9 @@ static int or_sample_ambiguous(const or_ctx *cx, const or_sample *sm) {
 
 /* One fkcc_single_buffer* call: g samples already interpolated in sm[0..g-1]
  * (sample k+1 in sm[k]).  Returns the 1-based sample that fired first, or 0.
- * `amb` is set when any sample is ambiguous (only computed when band > 0). */
-static int or_check_segment(const or_ctx *cx, or_sample *sm, int g, double *flops, int *amb) {
+ * `amb` counts the ambiguous samples (only computed when band > 0; with
+ * count_all = 0 it stops at the first). */
+static int or_check_segment(const or_ctx *cx, or_sample *sm, int g, double *flops, int *amb, int count_all) {
     int envc[OR_MAX_G], selfc[OR_MAX_G], envd[OR_MAX_G], selfd[OR_MAX_G];
     int any_env = 0, any_self = 0;
     for (int k = 0; k < g; k++) {
@@ -638,7 +639,7 @@ static int or_check_segment(const or_ctx *cx, or_sample *sm, int g, double *flop
     }
     *flops += g * or_broad_flops(cx);
     if (cx->band > 0.0)
-        for (int k = 0; k < g && !*amb; k++) *amb |= or_sample_ambiguous(cx, &sm[k]);
+        for (int k = 0; k < g && (count_all || !*amb); k++) *amb += or_sample_ambiguous(cx, &sm[k]);
     if (!any_env && !any_self) return 0;
     int exact = (cx->flags & OR_EXACT) != 0;
     if (!exact) {
@@ -689,7 +690,7 @@ int oracle_validate(const orc_scene *sc, const orc_robots *rb, const float *q0, 
                     int64_t n_edges, int g, int flags, int arm, int rule, float range,
                     int pair_order, double band, const orc_trig *trig, int n_threads,
                     uint8_t *valid, int32_t *first_hit, uint8_t *ambiguous, double *flops_out,
-                    int32_t *n_seg_out) {
+                    int32_t *n_seg_out, int32_t *amb_samples) {
     or_init_tables();
     if (g < 1 || g > OR_MAX_G || rb->n_arms < 1 || rb->n_arms > OR_MAX_ARMS) return 1;
     if (arm >= rb->n_arms) return 1;
@@ -726,7 +727,7 @@ int oracle_validate(const orc_scene *sc, const orc_robots *rb, const float *q0, 
                     else v = acc[k][d];
                     sm[k].q[d] = v;
                 }
-            int f = or_check_segment(&cx, sm, g, &fl, &amb);
+            int f = or_check_segment(&cx, sm, g, &fl, &amb, amb_samples != NULL);
             if (f) first = s * g + f;
             if (rule == OR_RULE_CONNECT)
                 for (int d = 0; d < dim; d++) base[d] = base[d] + step[d];
@@ -736,7 +737,8 @@ int oracle_validate(const orc_scene *sc, const orc_robots *rb, const float *q0, 
         }
         valid[e] = first == 0;
         first_hit[e] = first ? first : -1;
-        if (ambiguous) ambiguous[e] = (uint8_t)amb;
+        if (ambiguous) ambiguous[e] = (uint8_t)(amb > 0);
+        if (amb_samples) amb_samples[e] = amb;
         if (n_seg_out) n_seg_out[e] = nseg;
         total_flops += fl;
     }
@@ -811,9 +813,11 @@ int oracle_det_spheres(float *out) {
     return 0;
 }
 
+/* Host threads available (processors, not the current OpenMP setting, which a
+ * one-thread call leaves at 1). */
 int oracle_max_threads(void) {
 #ifdef _OPENMP
-    return omp_get_max_threads();
+    return omp_get_num_procs();
 #else
     return 1;
 #endif

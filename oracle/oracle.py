@@ -41,7 +41,7 @@ def lib() -> C.CDLL:
         vp = C.c_void_p
         L.oracle_validate.argtypes = [C.POINTER(_Scene), C.POINTER(_Robots), vp, vp, C.c_int64, C.c_int, C.c_int,
                                       C.c_int, C.c_int, C.c_float, C.c_int, C.c_double, C.POINTER(_Trig), C.c_int,
-                                      vp, vp, vp, C.POINTER(C.c_double), vp]
+                                      vp, vp, vp, C.POINTER(C.c_double), vp, vp]
         L.oracle_validate.restype = C.c_int
         L.oracle_fk_spheres.argtypes = [vp, vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.POINTER(_Trig), vp]
         L.oracle_fk_spheres.restype = C.c_int
@@ -100,8 +100,13 @@ def _robots_struct(bases: np.ndarray):
 
 
 def validate(scene, bases, q0, q1, g, flags, arm=-1, rule=RULE_PLAIN, range_=0.0, pair_order=0, band=0.0,
-             trig: TrigTable | None = None, threads=0):
-    """Oracle verdicts: dict(valid u8, first_hit i32, ambiguous u8, flops float, n_seg i32)."""
+             trig: TrigTable | None = None, threads=0, count_ambiguous=False):
+    """Oracle verdicts: dict(valid u8, first_hit i32, ambiguous u8, flops float, n_seg i32).
+
+    With band > 0 an edge is ambiguous when one of its checked samples has a
+    deciding minimum signed distance (FP64) within band metres of zero;
+    count_ambiguous=True also returns amb_samples i32, the number of such
+    samples per edge (every checked sample is then examined)."""
     L = lib()
     q0 = np.ascontiguousarray(q0, np.float32)
     q1 = np.ascontiguousarray(q1, np.float32)
@@ -113,14 +118,29 @@ def validate(scene, bases, q0, q1, g, flags, arm=-1, rule=RULE_PLAIN, range_=0.0
     amb = np.zeros(n, np.uint8)
     nseg = np.zeros(n, np.int32)
     fl = C.c_double(0.0)
+    ams = np.zeros(n, np.int32) if count_ambiguous else None
     rc = L.oracle_validate(C.byref(sc), C.byref(rb), q0.ctypes.data, q1.ctypes.data, n, g, flags, arm, rule,
                            float(range_), pair_order, float(band), C.byref(trig._c) if trig else None, threads,
-                           valid.ctypes.data, first.ctypes.data, amb.ctypes.data, C.byref(fl), nseg.ctypes.data)
+                           valid.ctypes.data, first.ctypes.data, amb.ctypes.data, C.byref(fl), nseg.ctypes.data,
+                           ams.ctypes.data if ams is not None else None)
     if rc == 1:
         raise ValueError("oracle_validate: bad arguments")
     if rc == 2:
         raise KeyError("oracle_validate: a sine/cosine input was missing from the trig table")
-    return {"valid": valid, "first_hit": first, "ambiguous": amb, "flops": fl.value, "n_seg": nseg}
+    out = {"valid": valid, "first_hit": first, "ambiguous": amb, "flops": fl.value, "n_seg": nseg}
+    if ams is not None:
+        out["amb_samples"] = ams
+    return out
+
+
+def validate_with_trig(scene, bases, q0, q1, g, flags, arm, rule, range_, trig_fn, threads=0):
+    """validate() with the sine/cosine values of every sample taken from
+    trig_fn(x) -> (cos, sin) (e.g. the device's __cosf/__sinf), which makes the
+    restatement bit-exact against device code."""
+    samples = edge_samples(q0, q1, g, rule, range_)
+    x = np.ascontiguousarray(samples, np.float32).ravel()
+    c, s = trig_fn(x)
+    return validate(scene, bases, q0, q1, g, flags, arm, rule, range_, trig=TrigTable(x, c, s), threads=threads)
 
 
 def fk_spheres(base, q, detailed, fp64=False, pair_order=0, trig: TrigTable | None = None) -> np.ndarray:
