@@ -483,13 +483,6 @@ mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots,
 // reference-sphere bounds and segment state.
 int robotset_arms(const mrpop_robotset *robots) { return robots ? robots->n_arms : 0; }
 
-size_t split_scratch_bytes(int64_t n_edges, int g, int A) {
-    const int spl = g > 32 ? 2 : 1;
-    return 2 * sizeof(unsigned long long) +
-           (size_t)n_edges * (32 * spl * 2 * sizeof(uint64_t) + 2 * sizeof(uint64_t) + A * kRefSpheres * sizeof(float4) +
-                              2 * sizeof(int32_t));
-}
-
 void set_split_scratch(EdgeParams &p, void *scratch, int64_t n_edges, int g, int A) {
     const int spl = g > 32 ? 2 : 1;
     const size_t flag_bytes = (size_t)n_edges * 32 * spl * 2 * sizeof(uint64_t);

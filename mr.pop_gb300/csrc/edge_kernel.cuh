@@ -1,21 +1,31 @@
 // edge_kernel.cuh -- the batched edge validator (sm_103a).
 //
-// One warp owns one edge at a time (persistent grid, warp-strided over the
-// batch).  Lane L evaluates samples k = L+1 (+32) of the edge:
+// One warp owns one edge at a time; warps take edges from a per-launch work
+// counter (persistent grid).  Lane L evaluates samples k = L+1 (+32) of the
+// edge.  Single-segment edges run as two kernels (broad, then narrow, the
+// narrow kernel a programmatic dependent of the broad one); segmented rules
+// run those two per segment round and a fused kernel for the tail.
 //   broad phase  per lane: FK of every arm (FP32 FMA, __sinf/__cosf as the
 //                reference), the 11 broad-phase spheres per arm against the
-//                scene staged in shared memory (one bulk-async copy per CTA),
-//                the intra-arm pairs and the arm-vs-arm pairs; the result is a
-//                per-(arm, joint) flag word and per-sample sphere counts.
+//                scene staged in shared memory (one bulk-async copy per CTA,
+//                bounded mbarrier wait), the intra-arm pairs and the arm-vs-arm
+//                pairs, each screened one pair per lane against swept bounds of
+//                the warp's samples first; the result is a per-(arm, joint)
+//                flag word and per-sample sphere counts, staged in HBM with the
+//                swept bounds for the narrow kernel.
 //   decision     per warp: shuffle reductions give the edge totals; the
 //                reference's proportional 4g-thread split (utils.cuh:476-517)
 //                is evaluated exactly to pick the samples that get a detailed
-//                check (or every flagged sample in EXACT mode).
-//   narrow phase per warp, one sample at a time in increasing k: lanes rebuild
-//                the joint frames of that sample, place the 59 detailed
-//                spheres per arm in shared memory, then split the flagged env
-//                tests and self rows (compacted into dense work lists) over the
-//                lanes; a warp vote ends the edge at the first colliding sample.
+//                check (or every flagged sample in EXACT mode); ballots form
+//                the candidate masks.
+//   narrow phase lane per candidate sample: all lanes walk the arms' joint
+//                chains in step (lanes without a candidate keep the others
+//                company), test the detailed spheres of flagged joints against
+//                obstacles that survive a warp-wide screen per sphere group,
+//                the flagged intra-arm rows (the forearm-hand rows skipped
+//                where a (q6, q7) table certifies them apart) and the
+//                arm-vs-arm group pairs that survive a warp-wide screen; the
+//                first hit is the lowest set bit of a warp ballot.
 // Culling: every obstacle carries a bounding sphere (1 mm margin) and every
 // arm / joint group a bounding sphere computed from its own sphere set; an
 // exact test is skipped only where the bounds prove it cannot fire, so the
@@ -215,6 +225,15 @@ __device__ __forceinline__ bool stage_scene(float4 *dst, const float4 *src, uint
     if (!done) {
         atomicOr(status, 1u);
         ok = false;
+        // the bulk copy may still be writing this CTA's shared memory: give it
+        // a second bounded wait before the CTA reports its edges and leaves
+        for (int it = 0; it < (1 << 22) && !done; it++) {
+            asm volatile(
+                "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+                : "=r"(done)
+                : "r"(smem_u32(bar))
+                : "memory");
+        }
     }
     return __syncthreads_and(ok);
 }
@@ -1533,6 +1552,15 @@ __device__ __forceinline__ bool stage_bulk(float4 *dst, const float4 *src, uint3
     if (!done) {
         atomicOr(status, 1u);
         ok = false;
+        // the bulk copy may still be writing this CTA's shared memory: give it
+        // a second bounded wait before the CTA reports its edges and leaves
+        for (int it = 0; it < (1 << 22) && !done; it++) {
+            asm volatile(
+                "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                : "=r"(done)
+                : "r"(smem_u32(bar)), "r"(parity)
+                : "memory");
+        }
     }
     return __syncthreads_and(ok);
 }

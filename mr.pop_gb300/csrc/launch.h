@@ -54,8 +54,14 @@ mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots,
                          size_t &smem);
 
 // Scratch of the single-segment pipeline (staged flags, candidate masks and
-// reference-sphere bounds): its size, and its slices in p.
-size_t split_scratch_bytes(int64_t n_edges, int g, int A);
+// reference-sphere bounds): its size, and its slices in p.  Two work counters,
+// then per edge: 32 * spl samples x {env, self} flag words, {env, self}
+// candidate masks, A arms' reference-sphere bounds and the segment state.
+constexpr size_t split_scratch_bytes(int64_t n_edges, int g, int A) {
+    return 2 * sizeof(unsigned long long) +
+           (size_t)n_edges * (32 * (g > 32 ? 2 : 1) * 2 * sizeof(uint64_t) + 2 * sizeof(uint64_t) +
+                              (size_t)A * kRefSpheres * sizeof(float4) + 2 * sizeof(int32_t));
+}
 void set_split_scratch(EdgeParams &p, void *scratch, int64_t n_edges, int g, int A);
 
 // Arm count of a robot set (0 for null).

@@ -24,11 +24,11 @@
 
 namespace {
 
-// per edge: 64 samples x {env, self} flag words + {env, self} candidate masks
-// + the swept bounds of 5 arms' reference spheres + segment state
-constexpr size_t kNoAllocBytesPerEdge =
-    (64 * 2 + 2) * sizeof(uint64_t) + mrpop::kMaxArms * mrpop::kRefSpheres * sizeof(float4) + 2 * sizeof(int32_t);
-constexpr size_t kNoAllocBytes = 2 * sizeof(unsigned long long) + (size_t)MRPOP_NOALLOC_MAX_EDGES * kNoAllocBytesPerEdge;
+// The scratch of the largest call allowed: MRPOP_NOALLOC_MAX_EDGES edges at
+// granularity 64 with 5 arms (the same size function the pool path uses).
+constexpr size_t kNoAllocBytes = mrpop::split_scratch_bytes(MRPOP_NOALLOC_MAX_EDGES, 64, mrpop::kMaxArms);
+static_assert(kNoAllocBytes >= mrpop::split_scratch_bytes(MRPOP_NOALLOC_MAX_EDGES, 32, mrpop::kMaxArms),
+              "the array must hold the largest call at every granularity");
 
 // Host code must not use this name as a device address (on the host it is only
 // a stand-in); the device address comes from cudaGetSymbolAddress below.
@@ -39,7 +39,10 @@ std::mutex g_mu;
 void *g_scratch_addr[kMaxDevices] = {};
 
 // Device address of the array on the current device, looked up once per
-// device (with that device current) on the first call there.
+// device (with that device current) on the first call there.  The cached
+// address belongs to that device's primary context: after cudaDeviceReset
+// (which also invalidates every scene and robot-set handle) it is stale, so
+// the library is not to be used across a reset.
 mrpop_status scratch_address(void **out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
