@@ -13,6 +13,9 @@ same for this library:
   half extents, after any cylinder-boxes;
 - problems whose "valid" is false are skipped, like the reference's loop
   (evaluate_mr.cu:125-127).
+The values are cast to float32 first and the obstacles built in float32 the
+way the reference's Eigen factories evaluate them (workloads.box_f32 /
+capsule_f32); precision="f64" builds them in float64 and rounds once.
 
 Each Problem also carries the start and goal configurations and, when the
 file gives them, the arm bases (base_positions, base_orientation_wxyz) as
@@ -27,7 +30,7 @@ from pathlib import Path
 import numpy as np
 
 from .mrpop import SceneArrays
-from .workloads import box, capsule
+from .workloads import box, box_f32, capsule, capsule_f32
 
 
 @dataclass
@@ -53,19 +56,25 @@ def quat_base(position, wxyz) -> np.ndarray:
     return t.astype(np.float32)
 
 
-def problem_scene(problem: dict) -> SceneArrays:
+def problem_scene(problem: dict, precision: str = "f32") -> SceneArrays:
     """The obstacles of one problem dict (evaluate_mr.cu:14-79)."""
+    if precision == "f32":
+        box_fn, capsule_fn = box_f32, capsule_f32
+    elif precision == "f64":
+        box_fn, capsule_fn = box, capsule
+    else:
+        raise ValueError(precision)
     name = problem.get("name", "")
     spheres = [np.array([*o["position"], o["radius"]], np.float32) for o in problem.get("sphere", [])]
     caps, cubs = [], []
     for o in problem.get("cylinder", []):
         r = float(o["radius"])
         if name == "box":
-            cubs.append(box(o["position"], o["orientation_euler_xyz"], (r, r, np.float32(r) / np.float32(2.0))))
+            cubs.append(box_fn(o["position"], o["orientation_euler_xyz"], (r, r, np.float32(r) / np.float32(2.0))))
         else:
-            caps.append(capsule(o["position"], o["orientation_euler_xyz"], r, float(o["length"])))
+            caps.append(capsule_fn(o["position"], o["orientation_euler_xyz"], r, float(o["length"])))
     for o in problem.get("box", []):
-        cubs.append(box(o["position"], o["orientation_euler_xyz"], o["half_extents"]))
+        cubs.append(box_fn(o["position"], o["orientation_euler_xyz"], o["half_extents"]))
     kw = {}
     if spheres:
         kw["spheres"] = np.stack(spheres)

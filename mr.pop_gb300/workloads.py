@@ -61,6 +61,88 @@ def capsule(center, euler_xyz, radius, length) -> np.ndarray:
     return np.array([*p1, *v, radius, np.float32(1.0 / float(dot))], np.float32)
 
 
+# ---------------------------------------------------------------------------
+# The reference's factories in float32, as its host code evaluates them:
+# Eigen::AngleAxisf(phi, Z) * AngleAxisf(theta, Y) * AngleAxisf(rho, X) is a
+# product of unit quaternions (factory.hh:29-31, 103-105), applied to the unit
+# axes (box) or turned into a rotation matrix of an affine transform (capsule).
+# Restated from Eigen 3.4's scalar (non-vectorised) code paths -- AngleAxis to
+# Quaternion (w = cos(a/2), v = sin(a/2) * axis), the generic quaternion product,
+# QuaternionBase::_transformVector (uv = 2 * v x p; p + w * uv + v x uv) and
+# toRotationMatrix -- every operation rounded to float32 without fused
+# multiply-adds.  The reference's build enables SSE/AVX2/FMA (CMakeLists.txt:30),
+# under which Eigen may take vectorised paths that round differently, so these
+# are pinned against the float64 construction (box, capsule above) to 1e-6.
+# ---------------------------------------------------------------------------
+_F = np.float32
+
+
+def _quat_axis(angle, axis: int):
+    ha = _F(0.5) * _F(angle)
+    s = _F(math.sin(ha))  # std::sin on float
+    q = [_F(math.cos(ha)), _F(0), _F(0), _F(0)]
+    q[1 + axis] = _F(s * _F(1))
+    return q
+
+
+def _quat_mul(a, b):
+    aw, ax, ay, az = a
+    bw, bx, by, bz = b
+    return [_F(_F(_F(aw * bw) - _F(ax * bx)) - _F(ay * by)) - _F(az * bz),
+            _F(_F(_F(aw * bx) + _F(ax * bw)) + _F(ay * bz)) - _F(az * by),
+            _F(_F(_F(aw * by) + _F(ay * bw)) + _F(az * bx)) - _F(ax * bz),
+            _F(_F(_F(aw * bz) + _F(az * bw)) + _F(ax * by)) - _F(ay * bx)]
+
+
+def _cross(a, b):
+    return [_F(_F(a[1] * b[2]) - _F(a[2] * b[1])), _F(_F(a[2] * b[0]) - _F(a[0] * b[2])),
+            _F(_F(a[0] * b[1]) - _F(a[1] * b[0]))]
+
+
+def _quat_rotate(q, p):
+    v = q[1:]
+    uv = _cross(v, p)
+    uv = [_F(u + u) for u in uv]
+    vuv = _cross(v, uv)
+    return [_F(_F(p[i] + _F(q[0] * uv[i])) + vuv[i]) for i in range(3)]
+
+
+def euler_quat_f32(euler_xyz):
+    rho, theta, phi = (_F(e) for e in euler_xyz)
+    return _quat_mul(_quat_mul(_quat_axis(phi, 2), _quat_axis(theta, 1)), _quat_axis(rho, 0))
+
+
+def quat_matrix_f32(q):
+    w, x, y, z = q
+    tx, ty, tz = _F(2) * x, _F(2) * y, _F(2) * z
+    twx, twy, twz = tx * w, ty * w, tz * w
+    txx, txy, txz = tx * x, ty * x, tz * x
+    tyy, tyz, tzz = ty * y, tz * y, tz * z
+    return np.array([[_F(1) - (tyy + tzz), txy - twz, txz + twy],
+                     [txy + twz, _F(1) - (txx + tzz), tyz - twx],
+                     [txz - twy, tyz + twx, _F(1) - (txx + tyy)]], np.float32)
+
+
+def box_f32(center, euler_xyz, half) -> np.ndarray:
+    """factory::cuboid::flat (factory.hh:26-41) in float32."""
+    q = euler_quat_f32(euler_xyz)
+    axes = [_quat_rotate(q, [_F(1) if i == k else _F(0) for i in range(3)]) for k in range(3)]
+    return np.array([*(_F(c) for c in center), *axes[0], *axes[1], *axes[2], *(_F(h) for h in half)], np.float32)
+
+
+def capsule_f32(center, euler_xyz, radius, length) -> np.ndarray:
+    """factory::cylinder::center::flat (factory.hh:100-114, endpoints at
+    +-length/2 on the local z axis, rdv = 1/|v|^2 in double, :70-80) in float32."""
+    r = quat_matrix_f32(euler_quat_f32(euler_xyz))
+    c = np.asarray(center, np.float32)
+    hl = _F(_F(length) / _F(2))
+    p1 = np.array([_F(_F(r[i, 2] * hl) + c[i]) for i in range(3)], np.float32)
+    p2 = np.array([_F(_F(r[i, 2] * -hl) + c[i]) for i in range(3)], np.float32)
+    v = (p2 - p1).astype(np.float32)
+    dot = np.float32(np.float32(np.float32(v[0] * v[0]) + np.float32(v[1] * v[1])) + np.float32(v[2] * v[2]))
+    return np.array([*p1, *v, _F(radius), np.float32(1.0 / float(dot))], np.float32)
+
+
 def yaw_base(x: float, y: float, z: float, yaw: float) -> np.ndarray:
     c, s = math.cos(yaw), math.sin(yaw)
     return np.array([[c, -s, 0, x], [s, c, 0, y], [0, 0, 1, z], [0, 0, 0, 1]], np.float32)

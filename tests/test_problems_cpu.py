@@ -26,8 +26,11 @@ def test_loader_maps_every_shape(pkg):
     t, b = probs
     assert t.index == 7 and t.start.shape == (28,) and t.goals.shape == (2, 28)
     assert np.allclose(t.scene.spheres, [[0.1, 0.2, 0.3, 0.05]])
-    assert np.array_equal(t.scene.capsules[0], W.capsule([0.4, 0.0, 0.2], [0.1, 0.2, 0.3], 0.04, 0.3))
-    assert np.array_equal(t.scene.cuboids[0], W.box([0.0, 0.5, 0.1], [0.0, 0.0, 0.7], [0.1, 0.2, 0.05]))
+    assert np.array_equal(t.scene.capsules[0], W.capsule_f32([0.4, 0.0, 0.2], [0.1, 0.2, 0.3], 0.04, 0.3))
+    assert np.array_equal(t.scene.cuboids[0], W.box_f32([0.0, 0.5, 0.1], [0.0, 0.0, 0.7], [0.1, 0.2, 0.05]))
+    # the float64 construction agrees to 1e-6
+    t64 = P.load_problems(json.dumps([_problem("table")]))[0]
+    assert np.abs(P.problem_scene(_problem("table"), "f64").cuboids - t64.scene.cuboids).max() < 1e-6
     # problems named "box" turn cylinders into boxes of half extents (r, r, r/2), ahead of the boxes
     assert len(b.scene.capsules) == 0 and len(b.scene.cuboids) == 2
     assert np.allclose(b.scene.cuboids[0][12:], [0.04, 0.04, 0.02])
@@ -48,3 +51,38 @@ def test_fixture_bases_are_rigid(pkg):
         b = d[f"a{arms}_bases"].astype(np.float64)
         for t in b:
             assert np.allclose(t[:3, :3] @ t[:3, :3].T, np.eye(3), atol=1e-6)
+
+
+def test_float32_factory_matches_float64_on_every_fixture_problem(pkg):
+    """The boxes of the reference's 100 benchmark problems, built in float32 as
+    its Eigen factory does (AngleAxisf products, factory.hh:26-41), agree with
+    the float64 construction to 1e-6, and the fixture holds the float32 ones."""
+    from pathlib import Path
+    W = pkg.workloads
+    d = np.load(Path(__file__).parent / "golden" / "problems.npz")
+    worst = 0.0
+    for arms in (4, 5):
+        for i in range(int(d[f"n{arms}"])):
+            params = d[f"a{arms}_p{i}_box_params"]
+            boxes = d[f"a{arms}_p{i}_boxes"]
+            assert len(params) == len(boxes)
+            for prm, rec in zip(params, boxes):
+                f32 = W.box_f32(prm[0:3], prm[3:6], prm[6:9])
+                f64 = W.box(prm[0:3], prm[3:6], prm[6:9])
+                assert np.array_equal(f32, rec)
+                worst = max(worst, float(np.abs(f32.astype(np.float64) - f64).max()))
+    assert worst < 1e-6
+
+
+def test_float32_factory_on_general_rotations(pkg):
+    """Arbitrary Euler angles (the fixture's are mostly plain yaws): boxes and
+    capsules from the float32 path stay within 1e-6 of the float64 path."""
+    W = pkg.workloads
+    rng = np.random.default_rng(3)
+    for _ in range(500):
+        c, e = rng.uniform(-1, 1, 3), rng.uniform(-3.2, 3.2, 3)
+        h = rng.uniform(0.01, 0.3, 3)
+        assert np.abs(W.box_f32(c, e, h).astype(np.float64) - W.box(c, e, h)).max() < 1e-6
+        a, b = W.capsule_f32(c, e, 0.05, 0.4), W.capsule(c, e, 0.05, 0.4)
+        assert np.abs(a[:7].astype(np.float64) - b[:7]).max() < 1e-6
+        assert abs(a[7] / b[7] - 1) < 1e-5
