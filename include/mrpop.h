@@ -155,7 +155,14 @@ mrpop_status mrpop_validate_segments(const mrpop_scene *scene, const mrpop_robot
  *   - n_edges above MRPOP_NOALLOC_MAX_EDGES is rejected (MRPOP_ERR_INVALID_ARGUMENT).
  *   - The first call on a device looks up the array's device address (a one-time
  *     set-up per device, done with that device current); make that first call
- *     before any stream capture.
+ *     before any stream capture.  With CUDA's default lazy module loading the
+ *     driver places the array, and loads each kernel variant, on first use: the
+ *     first call per device -- and the first per arm count and granularity class
+ *     (g <= 32 or not) -- is a warm-up in which the driver may take device
+ *     memory.  A caller with a fixed budget makes those calls at start-up (or
+ *     sets CUDA_MODULE_LOADING=EAGER); later calls take none.
+ *   - The cached address, like every handle of this library, does not survive
+ *     cudaDeviceReset.
  *   - Every call shares the array: calls that overlap on the GPU (different
  *     streams, other host threads) race on it and must be ordered by the caller.
  *     The array keeps the last call's contents; no call depends on them.
@@ -213,7 +220,11 @@ mrpop_status mrpop_fk_spheres(const mrpop_robotset *robots, int arm, const float
  * edges with segments left.  It allocates nothing and reads the inputs as they
  * are at execution time, so a batch can be rerun on refilled buffers.
  * mrpop_batch_tune picks each group's broad and narrow grids by timing
- * (synchronous).
+ * (synchronous).  It times launches on the items' own buffers, so it writes
+ * their outputs: afterwards single-segment items hold their verdicts, but
+ * segmented items hold only the first segment round's partial state (their
+ * later rounds are not run) -- run the batch or launch its graph before
+ * reading them.
  * mrpop_batch_capture records one run as a CUDA graph (each group on its own
  * branch) and mrpop_batch_launch launches that graph on `stream`.
  * mrpop_batch_info reports, per group, {arms, samples per lane, segmented,
@@ -371,6 +382,123 @@ mrpop_status mrpop_session_plan(mrpop_session *session, const mrpop_scene *scene
                                 uint32_t flags, const float *start, const float *goal,
                                 const mrpop_plan_settings *settings, float *path_out, int64_t max_waypoints,
                                 mrpop_plan_result *out);
+
+/*
+ * The reference's planner, dRRT with per-arm roadmaps under the AO-x
+ * meta-algorithm (dRRT::solve, Planners.hh:57-64, pop_planner.cu:173-1030,
+ * roadmap_interior.cuh:36-341, utils.cuh:688-759, path_simplification.cu:17-242),
+ * rebuilt on this library's batched validator.  The reference runs it as
+ * persistent kernels that check one edge per 256-thread block; here the host
+ * steps all `num_new_configs` extension attempts of an iteration together and
+ * validates their edges in one call per form:
+ *   roadmap nodes and edges  single-arm form (fkcc_single_buffer_mr), one call
+ *                            per arm and round (roadmap_interior.cuh:167-263)
+ *   extend                   self only (fkcc_single_buffer_drrt, pop_planner.cu:551-564)
+ *   connect                  env + self, connect segmentation (pop_planner.cu:624-703)
+ *   B-spline smoothing       env + self, B-spline segmentation (path_simplification.cu:55-141)
+ *   shortcut DP              env + self, shortcut segmentation (path_simplification.cu:143-233)
+ * Tree nearest-neighbour searches (pop_planner.cu:472-507, 630-663) run as a
+ * kernel over the trees, which live in page-locked host memory that the GPU
+ * reads in place.  The algorithm follows the reference step for step
+ * (sampling, balance strategy, direction oracle, cost bounds, PHS sampling in
+ * the optimising passes, B-spline and shortcut passes); its races between
+ * blocks are replaced by a fixed order (attempts in block order within an
+ * iteration), and its random numbers come from seeded per-block streams of
+ * this library, so a solve is deterministic given the seed and the verdicts.
+ *
+ * Settings: the fields of the reference's pop_settings (pop_settings.hh:3-32)
+ * in order, bools as int32, then this library's additions.
+ * mrpop_drrt_settings_default fills the reference's defaults (and
+ * block_per_robot 8, max_launches 20, seed 1234).  dd_radius, dd_min_radius,
+ * resample_iter, cost_bound_resample and the perturb fields are carried but
+ * read nowhere, as in the reference; dynamic_domain is honoured as the
+ * reference computes it (its radii never leave FLT_MAX, so it never prunes).
+ *
+ * mrpop_drrt_solve validates with this library's kernels on the current
+ * device.  start: [7 * arms]; goals: [num_goals][7 * arms] (host).  The
+ * robot set gives the arms and their bases (arm count 1-5).  path_out
+ * (optional) receives up to max_waypoints waypoints of the best solution, in
+ * the reference's order: from the goal to the start (record_connected_path,
+ * path_processing.cu:11-70), simplified when path_simplify is set.
+ * on_solution (optional) is called for every improving solution, as the
+ * reference's copy_path_to_result (path_processing.cu:73-122) appends to
+ * PlannerResult::seed_paths: the pass, its cost, the path as path_out has it,
+ * and the unsimplified path of that pass.  The pointers are valid during the
+ * call only.  The first pass repeats (one roadmap round, then up to max_iters
+ * iterations) until it finds a solution, as the reference's does, but at most
+ * max_launches times (the reference repeats without limit); trees are capped
+ * at max_samples nodes.
+ * mrpop_drrt_solve_with takes any validator (validate(ctx, q0, q1, n, g,
+ * rule, range, flags, arm, valid, first_hit) checks n host edges, returns 0 or
+ * an mrpop_status) and searches nearest neighbours on the host with the same
+ * arithmetic, so the same settings, seed and verdicts give the same solve:
+ * the CPU tests drive it with the oracle.
+ */
+typedef int (*mrpop_check_fn)(void *ctx, const float *q0, const float *q1, int64_t n_edges, int granularity,
+                              int rule, float range, uint32_t flags, int arm, uint8_t *valid, int32_t *first_hit);
+typedef void (*mrpop_drrt_solution_fn)(void *ctx, int32_t pass, float cost, const float *path, int64_t n_waypoints,
+                                       const float *raw_path, int64_t n_raw);
+
+typedef struct {
+    int32_t max_samples;      /* tree capacity (1000000)                                  */
+    int32_t max_iters;        /* iterations per launch (1000)                             */
+    int32_t optimize_iters;   /* iteration cap of the optimising passes (400000)          */
+    int32_t num_new_configs;  /* extension attempts per iteration (256)                   */
+    int32_t granularity;      /* samples per edge and segment (16)                        */
+    float range;              /* roadmap radius, connect and shortcut segment length (0.5) */
+    int32_t balance;          /* 2: swap trees unless the other is twice as large (2)     */
+    float tree_ratio;         /* (1.0)                                                    */
+    int32_t dynamic_domain;   /* (0)                                                      */
+    float dd_alpha;           /* (0.0001)                                                 */
+    float dd_radius;          /* (4.0, unused)                                            */
+    float dd_min_radius;      /* (1.0, unused)                                            */
+    int32_t roadmap_reassign; /* connected arms' roadmap blocks help the others (0)       */
+    int32_t rrtc_iter;        /* AO-x passes: the first finds a path, the rest optimise (1) */
+    int32_t resample_iter;    /* (5, unused)                                              */
+    int32_t cost_bound_resample; /* (0, unused)                                           */
+    int32_t path_simplify;    /* B-spline and shortcut passes after every pass (1)        */
+    int32_t phs;              /* informed (prolate hyperspheroid) sampling when optimising (1) */
+    int32_t simplify_round;   /* (1)                                                      */
+    int32_t bspline_step;     /* (3)                                                      */
+    float bspline_min_change; /* (0.01)                                                   */
+    int32_t perturb_step;     /* (3, unused)                                              */
+    int32_t perturb_empty_step; /* (2, unused)                                            */
+    /* this library's additions */
+    int32_t block_per_robot;  /* roadmap blocks per arm, 230 samples each per round (8)   */
+    int32_t max_launches;     /* bound on the first pass's roadmap + rrtc repeats (20)    */
+    uint64_t seed;            /* random streams (1234, the reference's curand seed)       */
+} mrpop_drrt_settings;
+
+typedef struct {
+    int32_t solved;
+    int32_t iters;            /* iteration of the attempt that found the reported solution */
+    float cost;               /* the reported solution's cost after simplification        */
+    int32_t passes;           /* passes run                                               */
+    int32_t solutions;        /* improving solutions reported (on_solution calls)         */
+    int32_t launches;         /* first-pass repeats                                       */
+    int64_t start_tree_size;  /* tree sizes when the reported solution was found          */
+    int64_t goal_tree_size;
+    int64_t path_length;      /* waypoints of the reported path                           */
+    int64_t roadmap_nodes[MRPOP_MAX_ARMS];
+    int64_t roadmap_edges[MRPOP_MAX_ARMS];
+    int64_t validate_calls;
+    int64_t edges_validated;
+    int64_t iterations;       /* rrtc iterations over all passes                          */
+    int64_t wall_ns;          /* whole call                                               */
+    int64_t kernel_ns;        /* from the first pass's start to the end (reference's kernel_ns) */
+    int64_t validate_ns;      /* inside validate calls                                    */
+    int64_t nn_ns;            /* inside nearest-neighbour searches                        */
+} mrpop_drrt_result;
+
+mrpop_status mrpop_drrt_settings_default(mrpop_drrt_settings *out);
+mrpop_status mrpop_drrt_solve(const mrpop_scene *scene, const mrpop_robotset *robots, const float *start,
+                              const float *goals, int num_goals, const mrpop_drrt_settings *settings,
+                              float *path_out, int64_t max_waypoints, mrpop_drrt_solution_fn on_solution,
+                              void *solution_ctx, mrpop_drrt_result *out);
+mrpop_status mrpop_drrt_solve_with(int arms, mrpop_check_fn validate, void *ctx, const float *start,
+                                   const float *goals, int num_goals, const mrpop_drrt_settings *settings,
+                                   float *path_out, int64_t max_waypoints, mrpop_drrt_solution_fn on_solution,
+                                   void *solution_ctx, mrpop_drrt_result *out);
 
 /* Algorithmic flop count per edge (FMA = 2; the convention of the project's
  * roofline) for the same arguments as mrpop_validate_segments; writes

@@ -16,7 +16,11 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
-SOURCES = ["api.cu", "batch.cu", "server.cu", "planner.cu", "peak_probe.cu", "no_alloc.cu"] + [f"validate_a{a}.cu" for a in range(1, 6)]
+SOURCES = ["api.cu", "batch.cu", "server.cu", "planner.cu", "drrt.cu", "peak_probe.cu", "no_alloc.cu"] + \
+    [f"validate_a{a}.cu" for a in range(1, 6)]
+# the planners' host arithmetic is written with explicit fmaf where the
+# reference's compiler fuses; no other contraction, so x86 and Arm hosts agree
+SOURCE_FLAGS = {"drrt.cu": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def _nvcc() -> str:
@@ -47,7 +51,8 @@ def build(variant: str = "", defines: tuple[str, ...] = (), verbose: bool = Fals
         s = CSRC / src
         if obj.exists() and obj.stat().st_mtime > max(s.stat().st_mtime, dep_mtime):
             return obj
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *dflags, f"-I{INCLUDE}", "-c", str(s), "-o", str(obj)]
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *SOURCE_FLAGS.get(src, []), *dflags, f"-I{INCLUDE}", "-c", str(s), "-o",
+               str(obj)]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,0 +1,1146 @@
+// drrt.cu -- the reference's dRRT / AO-x planner on the batched validator.
+//
+// The reference (dRRT::solve, src/planning/pop_planner.cu:739-1030) runs its
+// planner as persistent kernels: a cooperative roadmap kernel
+// (build_roadmap, pop_planner.cu:173-218 -> roadmap_interior.cuh:36-341) and
+// rrtc<Robot> with 300 blocks of 4g threads (pop_planner.cu:220-737), each
+// block validating one edge at a time.  Here the host steps every block's
+// attempt of an iteration together, and each kind of edge check of the
+// iteration is one batched call into the validator:
+//   roadmap round   per arm: every block's 230 samples node-checked in one
+//                   call (single-arm form, g = 1: the reference checks the
+//                   node as g identical samples, all of which reach the
+//                   detailed phase, so the verdict is the same), then every
+//                   (old node, new node) pair within `range` in one call
+//   rrtc iteration  every block's extend edge (self only) in one call, then
+//                   every new node's connect edge (connect segmentation) in one
+//   simplification  all B-spline candidate edges of a step in one call, and
+//                   all shortcut pairs (i, i+2 .. i+16) in one call before the
+//                   shortcut dynamic programme runs on the host
+// Nearest-neighbour searches over the trees (pop_planner.cu:472-507, 630-663)
+// run as one kernel launch per tree and query chunk, over device copies of
+// the trees that grow as nodes are added.
+//
+// Where the reference's blocks race (atomicAdd node indices, the
+// atomicCAS(solved) winner), attempts are taken in block order within an
+// iteration; the rest follows the reference step for step, including its
+// quirks: a new node's cost is its parent's cost plus the distance to the
+// random sample (pop_planner.cu:531), a connect node's cost adds only
+// 1/n_ext of the connect distance (:717), the first-pass relaunch loop
+// (:958-984), the PHS transform (:290-341, 398-442), and the path from the
+// goal to the start (path_processing.cu:11-70).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <unordered_map>
+#include <vector>
+
+#include "launch.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+int64_t ns_since(Clock::time_point t0) {
+    return std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t0).count();
+}
+
+// Panda joint limits as q = u * s_m + s_a (Robots.hh:13-23).
+constexpr float kSm[7] = {5.9342f, 3.6652f, 5.9342f, 3.2289f, 5.9342f, 3.9095999999999997f, 5.9342f};
+constexpr float kSa[7] = {-2.9671f, -1.8326f, -2.9671f, -3.1416f, -2.9671f, -0.0873f, -2.9671f};
+constexpr int kRoadmapIters = 230;        // ROADMAP_BUILD_ITER (roadmap_interior.cuh:20)
+constexpr int kMaxRoadmap = 100000;       // MAX_ROADMAP_SIZE (roadmap_interior.cuh:21)
+constexpr float kExistSq = 1e-5f;         // a node "already exists" within this squared distance (:526)
+constexpr int kShortcutSpan = 16;         // the simplify kernel's 16 blocks (pop_planner.cu:911)
+constexpr int kNNChunk = 128;             // queries per nearest-neighbour launch
+
+// splitmix64 (Steele, Lea, Flood 2014) streams; uniform() is in (0, 1).
+struct Rng {
+    uint64_t s = 0;
+    uint64_t next() {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    float uniform() { return ((float)(next() >> 40) + 0.5f) * 0x1.0p-24f; }
+};
+
+Rng rng_stream(uint64_t seed, uint64_t kind, uint64_t index) {
+    Rng r{seed ^ (kind * 0xD1B54A32D192ED03ull) ^ ((index + 1) * 0xA0761D6478BD642Full)};
+    r.next();
+    return r;
+}
+
+// The reference's distance arithmetic (utils.cuh:123-144): ans += d * d, which
+// its compiler fuses; written as fmaf so host and device round alike.
+inline float sq_l2(const float *a, const float *b, int dim) {
+    float s = 0.0f;
+    for (int i = 0; i < dim; i++) {
+        const float d = a[i] - b[i];
+        s = fmaf(d, d, s);
+    }
+    return s;
+}
+inline float l2(const float *a, const float *b, int dim) { return sqrtf(sq_l2(a, b, dim)); }
+
+// compute_angle (utils.cuh:63-95): the angle at c1 between c2 - c1 and c3 - c1.
+float angle_at(const float *c1, const float *c2, const float *c3, int dim) {
+    float v[7], w[7];
+    for (int t = 0; t < dim; t++) {
+        v[t] = c2[t] - c1[t];
+        w[t] = c3[t] - c1[t];
+    }
+    float dot = 0.0f, vn = 0.0f, wn = 0.0f;
+    for (int t = 0; t < dim; t++) dot = fmaf(v[t], w[t], dot);
+    for (int t = 0; t < dim; t++) {
+        vn = fmaf(v[t], v[t], vn);
+        wn = fmaf(w[t], w[t], wn);
+    }
+    vn = sqrtf(vn);
+    wn = sqrtf(wn);
+    if (vn < 1e-8f || wn < 1e-8f) return 0.0f;
+    float c = dot / (vn * wn);
+    c = fminf(1.0f, fmaxf(-1.0f, c));
+    return acosf(c);
+}
+
+// ---------------------------------------------------------------------------
+// Per-arm roadmap: nodes, sorted adjacency lists, union-find components.
+// ---------------------------------------------------------------------------
+struct Roadmap {
+    std::vector<float> q;  // [n][7]
+    std::vector<std::vector<int>> adj;
+    std::vector<int> uf;
+    int64_t edges = 0;
+    int size() const { return (int)adj.size(); }
+    const float *node(int i) const { return &q[(size_t)i * 7]; }
+    int add(const float *x) {
+        q.insert(q.end(), x, x + 7);
+        adj.emplace_back();
+        uf.push_back(size() - 1);
+        return size() - 1;
+    }
+    int find(int x) {
+        while (uf[x] != x) {
+            uf[x] = uf[uf[x]];
+            x = uf[x];
+        }
+        return x;
+    }
+    void link(int a, int b) {  // a < b: b is the newer node
+        adj[a].push_back(b);
+        adj[b].push_back(a);
+        edges++;
+        const int ra = find(a), rb = find(b);
+        if (ra != rb) uf[std::max(ra, rb)] = std::min(ra, rb);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Trees: host master copy plus a device copy for the nearest-neighbour kernel.
+// ---------------------------------------------------------------------------
+struct Tree {
+    int dim = 0, arms = 0;
+    std::vector<float> q, cost;
+    std::vector<int> parent, rid;  // rid [n][arms]: roadmap vertex of each arm, -1 for connect nodes
+    std::unordered_map<uint64_t, std::vector<int>> by_ids;
+    std::vector<int> connect_nodes;
+    // device copy
+    float *d_q = nullptr, *d_cost = nullptr;
+    int64_t d_cap = 0, uploaded = 0;
+    bool cost_dirty = false;
+
+    int64_t size() const { return (int64_t)parent.size(); }
+    const float *node(int64_t i) const { return &q[(size_t)i * dim]; }
+    static uint64_t key(const int *ids, int arms) {
+        uint64_t h = 0xCBF29CE484222325ull;
+        for (int a = 0; a < arms; a++) {
+            h ^= (uint64_t)(uint32_t)ids[a];
+            h *= 0x100000001B3ull;
+        }
+        return h;
+    }
+    void clear() {
+        q.clear();
+        cost.clear();
+        parent.clear();
+        rid.clear();
+        by_ids.clear();
+        connect_nodes.clear();
+        uploaded = 0;
+        cost_dirty = false;
+    }
+    int add(const float *x, int par, float c, const int *ids) {
+        const int i = (int)size();
+        q.insert(q.end(), x, x + dim);
+        cost.push_back(c);
+        parent.push_back(par < 0 ? i : par);
+        if (ids) {
+            rid.insert(rid.end(), ids, ids + arms);
+            by_ids[key(ids, arms)].push_back(i);
+        } else {
+            rid.insert(rid.end(), (size_t)arms, -1);
+            connect_nodes.push_back(i);
+        }
+        return i;
+    }
+    // An existing node within the reference's 1e-5 squared distance of x
+    // (pop_planner.cu:522-528), looked up by roadmap-vertex tuple and among
+    // the connect nodes; -1 if none.
+    int existing(const float *x, const int *ids) const {
+        auto it = by_ids.find(key(ids, arms));
+        if (it != by_ids.end())
+            for (int i : it->second)
+                if (sq_l2(node(i), x, dim) <= kExistSq) return i;
+        for (int i : connect_nodes)
+            if (sq_l2(node(i), x, dim) <= kExistSq) return i;
+        return -1;
+    }
+    void free_device() {
+        if (d_q) cudaFree(d_q);
+        if (d_cost) cudaFree(d_cost);
+        d_q = d_cost = nullptr;
+        d_cap = uploaded = 0;
+    }
+    cudaError_t sync_device(cudaStream_t s) {
+        const int64_t n = size();
+        if (n > d_cap) {
+            int64_t cap = std::max<int64_t>(d_cap * 2, 65536);
+            while (cap < n) cap *= 2;
+            float *nq = nullptr, *nc = nullptr;
+            cudaError_t e = cudaMalloc(&nq, (size_t)cap * dim * sizeof(float));
+            if (e == cudaSuccess) e = cudaMalloc(&nc, (size_t)cap * sizeof(float));
+            if (e != cudaSuccess) {
+                cudaFree(nq);
+                return e;
+            }
+            cudaFree(d_q);
+            cudaFree(d_cost);
+            d_q = nq;
+            d_cost = nc;
+            d_cap = cap;
+            uploaded = 0;
+            cost_dirty = false;
+        }
+        cudaError_t e = cudaSuccess;
+        if (n > uploaded)
+            e = cudaMemcpyAsync(d_q + uploaded * dim, node(uploaded), (size_t)(n - uploaded) * dim * sizeof(float),
+                                cudaMemcpyHostToDevice, s);
+        const int64_t c0 = cost_dirty ? 0 : uploaded;
+        if (e == cudaSuccess && n > c0)
+            e = cudaMemcpyAsync(d_cost + c0, &cost[c0], (size_t)(n - c0) * sizeof(float), cudaMemcpyHostToDevice, s);
+        uploaded = n;
+        cost_dirty = false;
+        return e;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Nearest-neighbour kernel: for each query, the lowest (squared distance,
+// index) among the nodes that pass the query's filter.
+//   mode 0 (extend search): node cost < bound      (pop_planner.cu:479)
+//   mode 1 (connect search): sqrt(distance) < bound (pop_planner.cu:642)
+// One thread per node (held in registers); queries in shared memory.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void __launch_bounds__(256) tree_nn_kernel(const float *__restrict__ nodes, const float *__restrict__ cost,
+                                                      long long n, const float *__restrict__ qx,
+                                                      const float *__restrict__ qb, int nq, int mode,
+                                                      unsigned long long *__restrict__ best) {
+    __shared__ float sx[kNNChunk * DIM];
+    __shared__ float sb[kNNChunk];
+    __shared__ unsigned long long red[8][kNNChunk];
+    for (int i = threadIdx.x; i < nq * DIM; i += blockDim.x) sx[i] = qx[i];
+    for (int i = threadIdx.x; i < nq; i += blockDim.x) sb[i] = qb[i];
+    __syncthreads();
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool have = i < n;
+    float x[DIM];
+    float c = 0.0f;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) x[d] = have ? nodes[i * DIM + d] : 0.0f;
+    if (have && mode == 0) c = cost[i];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int q = 0; q < nq; q++) {
+        unsigned long long key = ~0ull;
+        if (have) {
+            float s = 0.0f;
+#pragma unroll
+            for (int d = 0; d < DIM; d++) {
+                const float t = x[d] - sx[q * DIM + d];
+                s = __fmaf_rn(t, t, s);
+            }
+            const bool ok = (mode == 0 ? c < sb[q] : sqrtf(s) < sb[q]) && s < FLT_MAX;
+            if (ok) key = ((unsigned long long)__float_as_uint(s) << 32) | (unsigned long long)(unsigned)i;
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            const unsigned long long other = __shfl_xor_sync(0xffffffffu, key, o);
+            key = other < key ? other : key;
+        }
+        if (lane == 0) red[warp][q] = key;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        unsigned long long k = red[0][q];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) k = red[w][q] < k ? red[w][q] : k;
+        if (k != ~0ull) atomicMin(&best[q], k);
+    }
+}
+
+cudaError_t launch_tree_nn(int dim, const Tree &t, const float *d_qx, const float *d_qb, int nq, int mode,
+                           unsigned long long *d_best, cudaStream_t s) {
+    const long long n = t.size();
+    const unsigned grid = (unsigned)std::max<long long>(1, (n + 255) / 256);
+    switch (dim) {
+        case 7: tree_nn_kernel<7><<<grid, 256, 0, s>>>(t.d_q, t.d_cost, n, d_qx, d_qb, nq, mode, d_best); break;
+        case 14: tree_nn_kernel<14><<<grid, 256, 0, s>>>(t.d_q, t.d_cost, n, d_qx, d_qb, nq, mode, d_best); break;
+        case 21: tree_nn_kernel<21><<<grid, 256, 0, s>>>(t.d_q, t.d_cost, n, d_qx, d_qb, nq, mode, d_best); break;
+        case 28: tree_nn_kernel<28><<<grid, 256, 0, s>>>(t.d_q, t.d_cost, n, d_qx, d_qb, nq, mode, d_best); break;
+        case 35: tree_nn_kernel<35><<<grid, 256, 0, s>>>(t.d_q, t.d_cost, n, d_qx, d_qb, nq, mode, d_best); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Validation on this library's kernels: page-locked staging buffers that the
+// kernels read and write in place (mrpop_validate_edges_host).
+// ---------------------------------------------------------------------------
+struct GpuChecker {
+    const mrpop_scene *scene = nullptr;
+    const mrpop_robotset *robots = nullptr;
+    mrpop_workspace *ws = nullptr;
+    float *q0 = nullptr, *q1 = nullptr;
+    uint8_t *valid = nullptr;
+    int32_t *first = nullptr;
+    size_t cap_f = 0, cap_e = 0;
+
+    ~GpuChecker() {
+        if (q0) cudaFreeHost(q0);
+        if (q1) cudaFreeHost(q1);
+        if (valid) cudaFreeHost(valid);
+        if (first) cudaFreeHost(first);
+        if (ws) mrpop_workspace_destroy(ws);
+    }
+    static int call(void *ctx, const float *a, const float *b, int64_t n, int g, int rule, float range,
+                    uint32_t flags, int arm, uint8_t *valid_out, int32_t *first_out) {
+        GpuChecker &c = *static_cast<GpuChecker *>(ctx);
+        const int dof = 7 * (arm >= 0 ? 1 : mrpop::robotset_arms(c.robots));
+        const size_t nf = (size_t)n * dof;
+        if (nf > c.cap_f) {
+            cudaFreeHost(c.q0);
+            cudaFreeHost(c.q1);
+            c.q0 = c.q1 = nullptr;
+            c.cap_f = 0;
+            const size_t cap = std::max(nf, (size_t)1 << 16) * 2;
+            if (cudaHostAlloc(&c.q0, cap * sizeof(float), cudaHostAllocDefault) != cudaSuccess ||
+                cudaHostAlloc(&c.q1, cap * sizeof(float), cudaHostAllocDefault) != cudaSuccess)
+                return mrpop::fail_status(MRPOP_ERR_OUT_OF_MEMORY, "drrt: page-locked staging buffers");
+            c.cap_f = cap;
+        }
+        if ((size_t)n > c.cap_e) {
+            cudaFreeHost(c.valid);
+            cudaFreeHost(c.first);
+            c.valid = nullptr;
+            c.first = nullptr;
+            c.cap_e = 0;
+            const size_t cap = std::max((size_t)n, (size_t)1 << 12) * 2;
+            if (cudaHostAlloc(&c.valid, cap, cudaHostAllocDefault) != cudaSuccess ||
+                cudaHostAlloc(&c.first, cap * sizeof(int32_t), cudaHostAllocDefault) != cudaSuccess)
+                return mrpop::fail_status(MRPOP_ERR_OUT_OF_MEMORY, "drrt: page-locked staging buffers");
+            c.cap_e = cap;
+        }
+        std::memcpy(c.q0, a, nf * sizeof(float));
+        std::memcpy(c.q1, b, nf * sizeof(float));
+        const mrpop_status st = mrpop_validate_edges_host(c.ws, c.scene, c.robots, c.q0, c.q1, n, g, flags, arm, rule,
+                                                          range, c.valid, c.first);
+        if (st != MRPOP_OK) return st;
+        std::memcpy(valid_out, c.valid, (size_t)n);
+        std::memcpy(first_out, c.first, (size_t)n * sizeof(int32_t));
+        return 0;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// The planner.
+// ---------------------------------------------------------------------------
+struct Solver {
+    mrpop_drrt_settings S;
+    int arms = 0, dim = 0, g = 0, num_goals = 0;
+    mrpop_check_fn validate = nullptr;
+    void *vctx = nullptr;
+    bool device_nn = false;
+    cudaStream_t stream = nullptr;
+    float *d_qx = nullptr, *d_qb = nullptr;
+    unsigned long long *d_best = nullptr, *h_best = nullptr;
+    mrpop_drrt_result *R = nullptr;
+    mrpop_drrt_solution_fn on_solution = nullptr;
+    void *sctx = nullptr;
+
+    std::vector<float> start, goals;
+    std::vector<Roadmap> rm;
+    std::vector<Rng> rm_rng;  // [arm][block]
+    std::vector<Rng> blk_rng;  // per rrtc block
+    Tree T[2];
+    int roadmap_launches = 0;
+    float best_cost = FLT_MAX;
+    // the reference's result state (pop_planner.cu:34-50, path_simplification.cu:14-15)
+    std::vector<float> path_out, raw_path;
+    int path_total = 0;
+    float cost_sym = 0.0f;
+    int solved_iters = 0;
+    int64_t sol_tree[2] = {0, 0};
+    bool init_sol = false;
+    float res_cost = 0.0f;
+    std::vector<float> res_path;
+    // scratch
+    std::vector<float> a0, a1;
+    std::vector<uint8_t> ok;
+    std::vector<int32_t> fh;
+
+    ~Solver() {
+        T[0].free_device();
+        T[1].free_device();
+        if (d_qx) cudaFree(d_qx);
+        if (d_qb) cudaFree(d_qb);
+        if (d_best) cudaFree(d_best);
+        if (h_best) cudaFreeHost(h_best);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    int check(int64_t n, int rule, float range, uint32_t flags, int arm, int gran) {
+        if (n == 0) return 0;
+        ok.resize((size_t)n);
+        fh.resize((size_t)n);
+        const auto t0 = Clock::now();
+        const int rc = validate(vctx, a0.data(), a1.data(), n, gran, rule, range, flags, arm, ok.data(), fh.data());
+        R->validate_ns += ns_since(t0);
+        R->validate_calls++;
+        R->edges_validated += n;
+        return rc;
+    }
+
+    // ---- nearest neighbours ------------------------------------------------
+    // idx[q] = nearest node of tree t to x[q] passing the filter, or -1;
+    // sqd[q] = its squared distance.
+    int nearest(Tree &t, const std::vector<float> &x, const std::vector<float> &bound, int mode,
+                std::vector<int> &idx, std::vector<float> &sqd) {
+        const int nq = (int)bound.size();
+        idx.assign(nq, -1);
+        sqd.assign(nq, FLT_MAX);
+        if (nq == 0) return 0;
+        const auto t0 = Clock::now();
+        if (!device_nn) {
+            for (int q = 0; q < nq; q++) {
+                const float *xq = &x[(size_t)q * dim];
+                uint64_t bestk = ~0ull;
+                for (int64_t i = 0; i < t.size(); i++) {
+                    const float s = sq_l2(t.node(i), xq, dim);
+                    const bool pass = (mode == 0 ? t.cost[i] < bound[q] : sqrtf(s) < bound[q]) && s < FLT_MAX;
+                    if (!pass) continue;
+                    uint32_t sb;
+                    std::memcpy(&sb, &s, 4);
+                    const uint64_t k = ((uint64_t)sb << 32) | (uint64_t)(uint32_t)i;
+                    bestk = std::min(bestk, k);
+                }
+                if (bestk != ~0ull) {
+                    idx[q] = (int)(uint32_t)bestk;
+                    const uint32_t sb = (uint32_t)(bestk >> 32);
+                    std::memcpy(&sqd[q], &sb, 4);
+                }
+            }
+            R->nn_ns += ns_since(t0);
+            return 0;
+        }
+        cudaError_t e = t.sync_device(stream);
+        for (int c0 = 0; c0 < nq && e == cudaSuccess; c0 += kNNChunk) {
+            const int m = std::min(kNNChunk, nq - c0);
+            e = cudaMemcpyAsync(d_qx, &x[(size_t)c0 * dim], (size_t)m * dim * sizeof(float), cudaMemcpyHostToDevice,
+                                stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(d_qb, &bound[c0], (size_t)m * sizeof(float), cudaMemcpyHostToDevice, stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(d_best, 0xFF, (size_t)m * sizeof(unsigned long long), stream);
+            if (e == cudaSuccess) e = launch_tree_nn(dim, t, d_qx, d_qb, m, mode, d_best, stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(h_best, d_best, (size_t)m * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                    stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+            for (int q = 0; q < m && e == cudaSuccess; q++) {
+                const unsigned long long k = h_best[q];
+                if (k == ~0ull) continue;
+                idx[c0 + q] = (int)(uint32_t)k;
+                const uint32_t sb = (uint32_t)(k >> 32);
+                std::memcpy(&sqd[c0 + q], &sb, 4);
+            }
+        }
+        R->nn_ns += ns_since(t0);
+        if (e != cudaSuccess) return mrpop::fail_status(MRPOP_ERR_CUDA, "drrt: nearest-neighbour search");
+        return 0;
+    }
+
+    // ---- roadmaps (roadmap_interior.cuh:36-341) ------------------------------
+    void init_roadmaps() {
+        rm.assign(arms, Roadmap{});
+        for (int a = 0; a < arms; a++) {
+            rm[a].add(&start[7 * a]);
+            for (int k = 0; k < num_goals; k++) rm[a].add(&goals[(size_t)k * dim + 7 * a]);
+        }
+    }
+    bool connected(int a) {
+        const int r0 = rm[a].find(0);
+        for (int k = 0; k < num_goals; k++)
+            if (rm[a].find(1 + k) == r0) return true;
+        return false;
+    }
+
+    // One round: `blocks[a]` blocks of 230 samples grow arm a's roadmap.
+    int roadmap_round(const std::vector<int> &blocks) {
+        for (int a = 0; a < arms; a++) {
+            const int nb = blocks[a];
+            if (nb <= 0) continue;
+            Roadmap &M = rm[a];
+            // samples in time order: iteration-major, block-minor
+            const int64_t K = (int64_t)nb * kRoadmapIters;
+            a0.resize((size_t)K * 7);
+            for (int xx = 0; xx < kRoadmapIters; xx++)
+                for (int b = 0; b < nb; b++) {
+                    Rng &r = rm_rng[(size_t)a * S.block_per_robot + (b % S.block_per_robot)];
+                    float *x = &a0[((size_t)xx * nb + b) * 7];
+                    for (int j = 0; j < 7; j++) x[j] = fmaf(r.uniform(), kSm[j], kSa[j]);
+                }
+            a1 = a0;
+            int rc = check(K, MRPOP_RULE_PLAIN, 0.0f, MRPOP_CHECK_ENV | MRPOP_CHECK_SELF, a, 1);
+            if (rc) return rc;
+            std::vector<float> nodes;
+            for (int64_t k = 0; k < K; k++)
+                if (ok[k]) nodes.insert(nodes.end(), &a0[(size_t)k * 7], &a0[(size_t)k * 7] + 7);
+            // edges: every existing node within `range` of each new node, the
+            // new node being the edge's end (roadmap_interior.cuh:183-240)
+            const int n_old = M.size();
+            const int n_new = std::min<int>((int)(nodes.size() / 7), kMaxRoadmap - n_old);
+            std::vector<int> ea, eb;
+            for (int j = 0; j < n_new; j++) {
+                const float *x = &nodes[(size_t)j * 7];
+                const int id = n_old + j;
+                for (int i = 0; i < id; i++) {
+                    const float *y = i < n_old ? M.node(i) : &nodes[(size_t)(i - n_old) * 7];
+                    if (l2(y, x, 7) < S.range) {
+                        ea.push_back(i);
+                        eb.push_back(id);
+                    }
+                }
+            }
+            for (int j = 0; j < n_new; j++) M.add(&nodes[(size_t)j * 7]);
+            const int64_t ne = (int64_t)ea.size();
+            a0.resize((size_t)ne * 7);
+            a1.resize((size_t)ne * 7);
+            for (int64_t e = 0; e < ne; e++) {
+                std::memcpy(&a0[(size_t)e * 7], M.node(ea[e]), 7 * sizeof(float));
+                std::memcpy(&a1[(size_t)e * 7], M.node(eb[e]), 7 * sizeof(float));
+            }
+            rc = check(ne, MRPOP_RULE_PLAIN, 0.0f, MRPOP_CHECK_ENV | MRPOP_CHECK_SELF, a, g);
+            if (rc) return rc;
+            std::vector<std::pair<int, int>> good;
+            for (int64_t e = 0; e < ne; e++)
+                if (ok[e]) good.emplace_back(ea[e], eb[e]);
+            std::sort(good.begin(), good.end(), [](auto &x, auto &y) { return x.second != y.second ? x.second < y.second : x.first < y.first; });
+            for (auto &p : good) M.link(p.first, p.second);
+        }
+        return 0;
+    }
+
+    // One build_roadmap launch: the first one loops rounds until every arm's
+    // start and goal are connected (or a roadmap is full); later ones run one
+    // round on every arm (roadmap_interior.cuh:88-339).  The first launch's
+    // rounds are bounded by max_launches (the reference loops until its
+    // roadmaps overflow).
+    int build_roadmaps() {
+        const bool first = roadmap_launches == 0;
+        roadmap_launches++;
+        if (!first) return roadmap_round(std::vector<int>(arms, S.block_per_robot));
+        for (int round = 0; round < S.max_launches; round++) {
+            std::vector<int> blocks(arms, 0);
+            int first_open = -1, closed = 0;
+            for (int a = 0; a < arms; a++) {
+                if (connected(a)) {
+                    closed++;
+                } else {
+                    blocks[a] = S.block_per_robot;
+                    if (first_open < 0) first_open = a;
+                }
+            }
+            if (first_open < 0) return 0;
+            if (S.roadmap_reassign) blocks[first_open] += closed * S.block_per_robot;
+            for (int a = 0; a < arms; a++)
+                if (rm[a].size() >= kMaxRoadmap) return 0;
+            const int rc = roadmap_round(blocks);
+            if (rc) return rc;
+        }
+        return 0;
+    }
+
+    // ---- informed sampling set-up (pop_planner.cu:290-341) ----------------
+    std::vector<float> tf, center;
+    void phs_setup() {
+        tf.assign((size_t)dim * dim, 0.0f);
+        center.assign(dim, 0.0f);
+        const float *f1 = T[0].node(0), *f2 = T[1].node(0);
+        const float dmin = l2(f1, f2, dim);
+        const float dtr = best_cost;
+        std::vector<float> rot((size_t)dim * dim, 0.0f), axis(dim);
+        for (int t = 0; t < dim; t++) center[t] = (f1[t] + f2[t]) / 2.0f;
+        if (dmin < 1e-6f) {
+            for (int t = 0; t < dim; t++) rot[(size_t)t * dim + t] = 1.0f;
+        } else {
+            for (int d = 0; d < dim; d++) axis[d] = (f2[d] - f1[d]) / dmin;
+            const float v0 = 1.0f - axis[0];
+            float vtv = v0 * v0;
+            for (int i = 1; i < dim; i++) vtv = fmaf(-axis[i], -axis[i], vtv);
+            const float beta = 2.0f / vtv;
+            for (int c = 0; c < dim; c++) {
+                const float vc = c == 0 ? 1.0f - axis[0] : -axis[c];
+                for (int r = 0; r < dim; r++) {
+                    const float vr = r == 0 ? 1.0f - axis[0] : -axis[r];
+                    float val = -beta * vr * vc;
+                    if (r == c) val += 1.0f;
+                    rot[(size_t)r * dim + c] = val;
+                }
+            }
+        }
+        const float conj = sqrtf(fmaf(dtr, dtr, -(dmin * dmin)));
+        std::vector<float> diag(dim, conj / 2);
+        diag[0] = dtr / 2;
+        for (int r = 0; r < dim; r++)
+            for (int c = 0; c < dim; c++) tf[(size_t)r * dim + c] = rot[(size_t)r * dim + c] * diag[c];
+    }
+    // One informed sample (pop_planner.cu:398-445), then clamped to the limits.
+    void phs_sample(Rng &r, float *x) {
+        const float k = sqrtf((float)(M_PI / 8.0f));
+        for (int d = 0; d < dim; d++) {
+            const float u = r.uniform();
+            x[d] = logf(u * (1.0f / (1.0f - u))) * k;
+        }
+        float n = 0.0f;
+        for (int d = 0; d < dim; d++) n = fmaf(x[d], x[d], n);
+        n = sqrtf(n);
+        for (int d = 0; d < dim; d++) x[d] = x[d] / n;
+        const float rad = powf(r.uniform(), 1.0f / (float)dim);
+        for (int d = 0; d < dim; d++) x[d] = x[d] * rad;
+        std::vector<float> y(dim);
+        for (int t = 0; t < dim; t++) {
+            float v = 0.0f;
+            for (int c = 0; c < dim; c++) v = fmaf(tf[(size_t)t * dim + c], x[c], v);
+            y[t] = v + center[t];
+        }
+        for (int t = 0; t < dim; t++) {
+            const int j = t % 7;
+            float u = (y[t] - kSa[j]) / kSm[j];
+            u = fmaxf(fminf(1.0f, u), 0.0f);
+            x[t] = fmaf(u, kSm[j], kSa[j]);
+        }
+    }
+
+    // ---- direction oracle (nn_angle_mr, utils.cuh:688-759) ------------------
+    bool nn_angle(const float *sample, int near, float bound, bool optimize, float *out, int *ids) {
+        const Tree &t = T[tree_now];
+        const float *vn = t.node(near);
+        for (int a = 0; a < arms; a++) {
+            const int r0 = t.rid[(size_t)near * arms + a];
+            if (r0 < 0) return false;
+            const Roadmap &M = rm[a];
+            int best = -1;
+            float best_angle = 1e3f;
+            for (int v : M.adj[r0]) {
+                if (v == r0) continue;
+                const float ed = l2(vn + 7 * a, M.node(v), 7);
+                if ((optimize && ed > bound) || ed > S.range) continue;
+                const float ang = angle_at(vn + 7 * a, sample + 7 * a, M.node(v), 7);
+                if (ang < best_angle) {
+                    best_angle = ang;
+                    best = v;
+                }
+            }
+            ids[a] = best;
+            if (best < 0) return false;
+            std::memcpy(out + 7 * a, M.node(best), 7 * sizeof(float));
+            bound -= l2(M.node(best), vn + 7 * a, 7);
+        }
+        return true;
+    }
+    int tree_now = 0;
+
+    // ---- a solution (record_connected_path, path_processing.cu:11-70) -------
+    void record_path(int t, int ti, int oi, int iter) {
+        const int o = 1 - t;
+        float c = 0.0f;
+        std::vector<int> pt, po;
+        for (int cur = ti; T[t].parent[cur] != cur; cur = T[t].parent[cur]) {
+            c += l2(T[t].node(cur), T[t].node(T[t].parent[cur]), dim);
+            pt.push_back(cur);
+        }
+        pt.push_back(0);
+        for (int cur = oi; T[o].parent[cur] != cur; cur = T[o].parent[cur]) {
+            c += l2(T[o].node(cur), T[o].node(T[o].parent[cur]), dim);
+            po.push_back(cur);
+        }
+        po.push_back(0);
+        const std::vector<int> &p1 = t == 1 ? pt : po, &p0 = t == 0 ? pt : po;
+        path_out.clear();
+        for (auto it = p1.rbegin(); it != p1.rend(); ++it) path_out.insert(path_out.end(), T[1].node(*it), T[1].node(*it) + dim);
+        for (int i : p0) path_out.insert(path_out.end(), T[0].node(i), T[0].node(i) + dim);
+        path_total = (int)(path_out.size() / dim);
+        raw_path = path_out;
+        cost_sym = c;
+        solved_iters = iter;
+        best_cost = std::min(best_cost, c);
+        sol_tree[0] = T[0].size();
+        sol_tree[1] = T[1].size();
+    }
+
+    // ---- one rrtc launch (pop_planner.cu:220-737) -------------------------
+    // Returns the status; *solved = 1 when a connection was made.
+    int rrtc(bool optimize, int *solved) {
+        *solved = 0;
+        const int N = S.num_new_configs;
+        if (optimize && S.phs) phs_setup();
+        std::vector<int> tsel(N, 0);
+        std::vector<float> x((size_t)N * dim), crand(N, FLT_MAX);
+        std::vector<char> live(N);
+        std::vector<int> idx, cidx;
+        std::vector<float> sqd, csqd;
+        for (int iter = 1;; iter++) {
+            if (iter > S.max_iters || (optimize && iter > S.optimize_iters)) return 0;
+            if (T[0].size() >= S.max_samples || T[1].size() >= S.max_samples) return 0;
+            R->iterations++;
+            const int64_t sz[2] = {T[0].size(), T[1].size()};
+            // tree choice, sample, cost bound
+            for (int b = 0; b < N; b++) {
+                Rng &r = blk_rng[b];
+                if (iter == 1) {
+                    tsel[b] = b < N / 2 ? 0 : 1;
+                } else if (S.balance == 2) {
+                    const int t = tsel[b];
+                    const float ratio = (float)std::llabs(sz[t] - sz[1 - t]) / (float)sz[t];
+                    if (ratio < S.tree_ratio) tsel[b] = 1 - t;
+                }
+                float *xb = &x[(size_t)b * dim];
+                if (!S.phs || !optimize) {
+                    for (int d = 0; d < dim; d++) xb[d] = fmaf(r.uniform(), kSm[d % 7], kSa[d % 7]);
+                } else {
+                    phs_sample(r, xb);
+                }
+                live[b] = !(l2(T[0].node(0), xb, dim) + l2(T[1].node(0), xb, dim) >= best_cost);
+                if (live[b] && optimize) {
+                    const int t = tsel[b];
+                    const float gh = l2(T[t].node(0), xb, dim);
+                    const float hh = l2(T[1 - t].node(0), xb, dim);
+                    const float range = std::max(best_cost - (gh + hh), 0.0f);
+                    crand[b] = fmaf(r.uniform(), range, gh);
+                }
+            }
+            // nearest node of each live attempt in its tree (one search per tree)
+            std::vector<int> near(N, -1);
+            std::vector<float> nd(N, FLT_MAX);
+            for (int t = 0; t < 2; t++) {
+                std::vector<float> qx, qb;
+                std::vector<int> who;
+                for (int b = 0; b < N; b++)
+                    if (live[b] && tsel[b] == t) {
+                        qx.insert(qx.end(), &x[(size_t)b * dim], &x[(size_t)b * dim] + dim);
+                        qb.push_back(optimize ? crand[b] : FLT_MAX);
+                        who.push_back(b);
+                    }
+                const int rc = nearest(T[t], qx, qb, 0, idx, sqd);
+                if (rc) return rc;
+                for (size_t k = 0; k < who.size(); k++) {
+                    near[who[k]] = idx[k] < 0 ? 0 : idx[k];
+                    nd[who[k]] = sqrtf(idx[k] < 0 ? FLT_MAX : sqd[k]);
+                }
+            }
+            // direction oracle, existing-node test, cost prunes; extend edges
+            struct Ext {
+                int b, t, near, exist;
+                float cost;
+                std::vector<float> cfg;
+                std::vector<int> ids;
+            };
+            std::vector<Ext> ext;
+            std::vector<float> cfg(dim);
+            std::vector<int> ids(arms);
+            for (int b = 0; b < N; b++) {
+                if (!live[b]) continue;
+                const int t = tsel[b];
+                tree_now = t;
+                const int nr = near[b];
+                const float bound = optimize ? crand[b] - T[t].cost[nr] : FLT_MAX;
+                if (!nn_angle(&x[(size_t)b * dim], nr, bound, optimize, cfg.data(), ids.data())) continue;
+                const int ex = T[t].existing(cfg.data(), ids.data());
+                const float nc = T[t].cost[nr] + nd[b];
+                if (ex >= 0 && (!optimize || nc >= T[t].cost[ex])) continue;
+                if (optimize && nc >= best_cost) continue;
+                ext.push_back(Ext{b, t, nr, ex, nc, cfg, ids});
+            }
+            const int64_t ne = (int64_t)ext.size();
+            a0.resize((size_t)ne * dim);
+            a1.resize((size_t)ne * dim);
+            for (int64_t k = 0; k < ne; k++) {
+                std::memcpy(&a0[(size_t)k * dim], T[ext[k].t].node(ext[k].near), dim * sizeof(float));
+                std::memcpy(&a1[(size_t)k * dim], ext[k].cfg.data(), dim * sizeof(float));
+            }
+            int rc = check(ne, MRPOP_RULE_PLAIN, 0.0f, MRPOP_CHECK_SELF, -1, g);
+            if (rc) return rc;
+            // grow the trees in block order; remember the new nodes to connect
+            struct Con {
+                int b, t, node;
+            };
+            std::vector<Con> con;
+            for (int64_t k = 0; k < ne; k++) {
+                if (!ok[k]) continue;
+                Ext &e = ext[k];
+                Tree &tt = T[e.t];
+                if (e.exist >= 0) {  // rewire (pop_planner.cu:571-577)
+                    tt.parent[e.exist] = e.near;
+                    tt.cost[e.exist] = e.cost;
+                    tt.cost_dirty = true;
+                    continue;
+                }
+                const int ni = tt.add(e.cfg.data(), e.near, e.cost, e.ids.data());
+                con.push_back(Con{e.b, e.t, ni});
+            }
+            // connect: nearest node of the other tree, one search per tree
+            std::vector<int> onear(con.size(), -1);
+            std::vector<float> od(con.size(), 0.0f);
+            for (int o = 0; o < 2; o++) {
+                std::vector<float> qx, qb;
+                std::vector<int> who;
+                for (size_t k = 0; k < con.size(); k++)
+                    if (1 - con[k].t == o) {
+                        const Tree &tt = T[con[k].t];
+                        qx.insert(qx.end(), tt.node(con[k].node), tt.node(con[k].node) + dim);
+                        qb.push_back(optimize ? best_cost - tt.cost[con[k].node] : FLT_MAX);
+                        who.push_back((int)k);
+                    }
+                rc = nearest(T[o], qx, qb, 1, cidx, csqd);
+                if (rc) return rc;
+                for (size_t k = 0; k < who.size(); k++)
+                    if (cidx[k] >= 0) {
+                        onear[who[k]] = cidx[k];
+                        od[who[k]] = sqrtf(csqd[k]);
+                    }
+            }
+            std::vector<int> ck;
+            for (size_t k = 0; k < con.size(); k++)
+                if (onear[k] >= 0) ck.push_back((int)k);
+            const int64_t nc = (int64_t)ck.size();
+            a0.resize((size_t)nc * dim);
+            a1.resize((size_t)nc * dim);
+            for (int64_t j = 0; j < nc; j++) {
+                const Con &c = con[ck[j]];
+                std::memcpy(&a0[(size_t)j * dim], T[c.t].node(c.node), dim * sizeof(float));
+                std::memcpy(&a1[(size_t)j * dim], T[1 - c.t].node(onear[ck[j]]), dim * sizeof(float));
+            }
+            rc = check(nc, MRPOP_RULE_CONNECT, S.range, MRPOP_CHECK_ENV | MRPOP_CHECK_SELF, -1, g);
+            if (rc) return rc;
+            for (int64_t j = 0; j < nc; j++) {
+                if (!ok[j]) continue;
+                const Con &c = con[ck[j]];
+                Tree &tt = T[c.t];
+                const float d = od[ck[j]];
+                const int next = (int)(d / S.range) + 1;
+                // the accumulated end of the connect loop (pop_planner.cu:684-716)
+                std::vector<float> cur(tt.node(c.node), tt.node(c.node) + dim), vec(dim);
+                const float *target = T[1 - c.t].node(onear[ck[j]]);
+                for (int dd = 0; dd < dim; dd++) vec[dd] = (target[dd] - cur[dd]) / (float)next;
+                for (int s = 0; s < next; s++)
+                    for (int dd = 0; dd < dim; dd++) cur[dd] += vec[dd];
+                const float ncost = tt.cost[c.node] + d / (float)next;
+                const int ni = tt.add(cur.data(), c.node, ncost, nullptr);
+                if (!*solved) {
+                    *solved = 1;
+                    record_path(c.t, ni, onear[ck[j]], iter);
+                }
+            }
+            if (*solved) return 0;
+        }
+    }
+
+    // ---- simplification (multiBlock_simplify, path_simplification.cu:17-242)
+    int simplify() {
+        const int n = path_total;
+        if (n < 1) return 0;
+        std::vector<float> &P = path_out;
+        for (int round = 0; round < S.simplify_round; round++) {
+            std::vector<float> pc(n, FLT_MAX);
+            std::vector<int> par(n, -1);
+            pc[0] = 0.0f;
+            // B-spline midpoint smoothing of the odd waypoints, bspline_step steps
+            const int R = (int)ceilf((float)(n - 3) / (2.0f * kShortcutSpan));
+            for (int step = 0; step < S.bspline_step && R > 0; step++) {
+                std::vector<int> cand;
+                std::vector<float> mids;
+                // the odd waypoints the 16 blocks reach in R strides (the last one
+                // can be left out, as in the reference)
+                for (int i = 1; i < n - 1 && i <= 2 * kShortcutSpan * R - 1; i += 2) {
+                    const float *c1 = &P[(size_t)(i - 1) * dim], *c2 = &P[(size_t)i * dim],
+                                *c3 = &P[(size_t)(i + 1) * dim];
+                    std::vector<float> mid(dim);
+                    for (int d = 0; d < dim; d++) {
+                        const float b1 = (c1[d] + c2[d]) / 2.0f, b2 = (c2[d] + c3[d]) / 2.0f;
+                        mid[d] = (b1 + b2) / 2.0f;
+                    }
+                    if (l2(c2, mid.data(), dim) < S.bspline_min_change) continue;
+                    cand.push_back(i);
+                    mids.insert(mids.end(), mid.begin(), mid.end());
+                }
+                const int64_t m = (int64_t)cand.size();
+                a0.resize((size_t)2 * m * dim);
+                a1.resize((size_t)2 * m * dim);
+                for (int64_t k = 0; k < m; k++) {
+                    const int i = cand[k];
+                    std::memcpy(&a0[(size_t)(2 * k) * dim], &P[(size_t)(i - 1) * dim], dim * sizeof(float));
+                    std::memcpy(&a0[(size_t)(2 * k + 1) * dim], &P[(size_t)(i + 1) * dim], dim * sizeof(float));
+                    std::memcpy(&a1[(size_t)(2 * k) * dim], &mids[(size_t)k * dim], dim * sizeof(float));
+                    std::memcpy(&a1[(size_t)(2 * k + 1) * dim], &mids[(size_t)k * dim], dim * sizeof(float));
+                }
+                const int rc = check(2 * m, MRPOP_RULE_BSPLINE, S.range, MRPOP_CHECK_ENV | MRPOP_CHECK_SELF, -1, g);
+                if (rc) return rc;
+                for (int64_t k = 0; k < m; k++)
+                    if (ok[2 * k] && ok[2 * k + 1])
+                        std::memcpy(&P[(size_t)cand[k] * dim], &mids[(size_t)k * dim], dim * sizeof(float));
+            }
+            // shortcut dynamic programme: edge i -> i+b+1 for b in 1..15 checked,
+            // i -> i+1 taken as valid (path_simplification.cu:143-217)
+            std::vector<int> ei, ej;
+            for (int i = 0; i < n - 1; i++)
+                for (int b = 1; b < kShortcutSpan; b++)
+                    if (i + b + 1 < n) {
+                        ei.push_back(i);
+                        ej.push_back(i + b + 1);
+                    }
+            const int64_t m = (int64_t)ei.size();
+            a0.resize((size_t)m * dim);
+            a1.resize((size_t)m * dim);
+            for (int64_t k = 0; k < m; k++) {
+                std::memcpy(&a0[(size_t)k * dim], &P[(size_t)ei[k] * dim], dim * sizeof(float));
+                std::memcpy(&a1[(size_t)k * dim], &P[(size_t)ej[k] * dim], dim * sizeof(float));
+            }
+            const int rc = check(m, MRPOP_RULE_SHORTCUT, S.range, MRPOP_CHECK_ENV | MRPOP_CHECK_SELF, -1, g);
+            if (rc) return rc;
+            std::vector<uint8_t> good(ok.begin(), ok.begin() + m);
+            int64_t k = 0;
+            for (int i = 0; i < n - 1; i++) {
+                for (int b = 0; b < kShortcutSpan; b++) {
+                    const int j = i + b + 1;
+                    if (j >= n) continue;
+                    bool eg = true;
+                    if (b > 0) eg = good[k++];
+                    if (!eg) continue;
+                    const float d = l2(&P[(size_t)i * dim], &P[(size_t)j * dim], dim);
+                    if (pc[j] > d + pc[i]) {
+                        pc[j] = d + pc[i];
+                        par[j] = i;
+                    }
+                }
+            }
+            // reconstruct: waypoints skipped by a shortcut become copies of its start
+            if (pc[n - 1] < best_cost) {
+                int child = n - 1, p = par[child];
+                while (p < n && p != -1) {
+                    for (int b = 0; b < kShortcutSpan; b++) {
+                        const int w = b + p + 1;
+                        if (w < child) std::memcpy(&P[(size_t)w * dim], &P[(size_t)p * dim], dim * sizeof(float));
+                    }
+                    child = p;
+                    p = par[child];
+                }
+            }
+            cost_sym = pc[n - 1];
+            best_cost = std::min(best_cost, cost_sym);
+        }
+        return 0;
+    }
+
+    void report(int pass, int solved_flag) {
+        // copy_path_to_result (path_processing.cu:73-122), called when the pass
+        // solved and its cost improves on the reported one (pop_planner.cu:1007)
+        if (!(solved_flag > 0 && (!init_sol || res_cost > cost_sym))) return;
+        init_sol = true;
+        res_cost = cost_sym;
+        res_path.assign(path_out.begin(), path_out.begin() + (size_t)path_total * dim);
+        R->solved = 1;
+        R->cost = cost_sym;
+        R->iters = solved_iters;
+        R->path_length = path_total;
+        R->start_tree_size = sol_tree[0];
+        R->goal_tree_size = sol_tree[1];
+        R->solutions++;
+        if (on_solution)
+            on_solution(sctx, pass, cost_sym, res_path.data(), path_total, raw_path.data(),
+                        (int64_t)(raw_path.size() / dim));
+    }
+
+    void reset_trees() {
+        for (int t = 0; t < 2; t++) {
+            T[t].clear();
+            T[t].dim = dim;
+            T[t].arms = arms;
+        }
+        std::vector<int> ids(arms, 0);
+        T[0].add(start.data(), -1, 0.0f, ids.data());
+        for (int k = 0; k < num_goals; k++) {
+            std::fill(ids.begin(), ids.end(), 1 + k);
+            T[1].add(&goals[(size_t)k * dim], -1, 0.0f, ids.data());
+        }
+    }
+
+    int run() {
+        const auto t_start = Clock::now();
+        init_roadmaps();
+        rm_rng.clear();
+        for (int a = 0; a < arms; a++)
+            for (int b = 0; b < S.block_per_robot; b++) rm_rng.push_back(rng_stream(S.seed, 1, (uint64_t)a * 4096 + b));
+        blk_rng.clear();
+        for (int b = 0; b < S.num_new_configs; b++) blk_rng.push_back(rng_stream(S.seed, 2, b));
+        const auto t_kernel = Clock::now();
+        for (int pass = 0; pass < S.rrtc_iter; pass++) {
+            R->passes++;
+            reset_trees();
+            const bool optimize = pass != 0;
+            int solved = 0;
+            do {
+                int rc = build_roadmaps();
+                if (rc) return rc;
+                rc = rrtc(optimize, &solved);
+                if (rc) return rc;
+                if (!optimize) R->launches++;
+            } while (!solved && !optimize && R->launches < S.max_launches);
+            if (S.path_simplify && path_total > 0) {
+                const int rc = simplify();
+                if (rc) return rc;
+            }
+            report(pass, solved);
+        }
+        for (int a = 0; a < arms && a < MRPOP_MAX_ARMS; a++) {
+            R->roadmap_nodes[a] = rm[a].size();
+            R->roadmap_edges[a] = rm[a].edges;
+        }
+        R->kernel_ns = ns_since(t_kernel);
+        R->wall_ns = ns_since(t_start);
+        return 0;
+    }
+};
+
+mrpop_status check_settings(const mrpop_drrt_settings &S) {
+    if (S.granularity < 1 || S.granularity > MRPOP_MAX_GRANULARITY || !(S.range > 0.0f) || S.num_new_configs < 1 ||
+        S.max_iters < 0 || S.max_samples < 2 || S.block_per_robot < 1 || S.rrtc_iter < 0 || S.max_launches < 1 ||
+        S.simplify_round < 0 || S.bspline_step < 0)
+        return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "drrt: bad settings");
+    return MRPOP_OK;
+}
+
+mrpop_status solve(Solver &sv, int arms, const float *start, const float *goals, int num_goals,
+                   const mrpop_drrt_settings *settings, float *path_out, int64_t max_waypoints,
+                   mrpop_drrt_solution_fn on_solution, void *sctx, mrpop_drrt_result *out) {
+    sv.S = *settings;
+    sv.arms = arms;
+    sv.dim = 7 * arms;
+    sv.g = settings->granularity;
+    sv.num_goals = num_goals;
+    sv.start.assign(start, start + sv.dim);
+    sv.goals.assign(goals, goals + (size_t)num_goals * sv.dim);
+    sv.R = out;
+    sv.on_solution = on_solution;
+    sv.sctx = sctx;
+    const int rc = sv.run();
+    if (rc) return (mrpop_status)rc;
+    if (path_out && max_waypoints > 0 && !sv.res_path.empty())
+        std::memcpy(path_out, sv.res_path.data(),
+                    (size_t)std::min<int64_t>(out->path_length, max_waypoints) * sv.dim * sizeof(float));
+    return MRPOP_OK;
+}
+
+}  // namespace
+
+extern "C" mrpop_status mrpop_drrt_settings_default(mrpop_drrt_settings *o) {
+    if (!o) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "drrt_settings_default: null");
+    *o = mrpop_drrt_settings{};
+    // pop_settings.hh:3-32
+    o->max_samples = 1000000;
+    o->max_iters = 1000;
+    o->optimize_iters = 400000;
+    o->num_new_configs = 256;
+    o->granularity = 16;
+    o->range = 0.5f;
+    o->balance = 2;
+    o->tree_ratio = 1.0f;
+    o->dynamic_domain = 0;
+    o->dd_alpha = 0.0001f;
+    o->dd_radius = 4.0f;
+    o->dd_min_radius = 1.0f;
+    o->roadmap_reassign = 0;
+    o->rrtc_iter = 1;
+    o->resample_iter = 5;
+    o->cost_bound_resample = 0;
+    o->path_simplify = 1;
+    o->phs = 1;
+    o->simplify_round = 1;
+    o->bspline_step = 3;
+    o->bspline_min_change = 0.01f;
+    o->perturb_step = 3;
+    o->perturb_empty_step = 2;
+    // this library's additions
+    o->block_per_robot = 8;
+    o->max_launches = 20;
+    o->seed = 1234;
+    return MRPOP_OK;
+}
+
+extern "C" mrpop_status mrpop_drrt_solve_with(int arms, mrpop_check_fn validate, void *ctx, const float *start,
+                                              const float *goals, int num_goals, const mrpop_drrt_settings *settings,
+                                              float *path_out, int64_t max_waypoints,
+                                              mrpop_drrt_solution_fn on_solution, void *solution_ctx,
+                                              mrpop_drrt_result *out) {
+    if (arms < 1 || arms > MRPOP_MAX_ARMS || !validate || !start || !goals || num_goals < 1 || !settings || !out)
+        return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "drrt_solve_with: bad argument");
+    const mrpop_status st = check_settings(*settings);
+    if (st != MRPOP_OK) return st;
+    *out = mrpop_drrt_result{};
+    Solver sv;
+    sv.validate = validate;
+    sv.vctx = ctx;
+    sv.device_nn = false;
+    return solve(sv, arms, start, goals, num_goals, settings, path_out, max_waypoints, on_solution, solution_ctx, out);
+}
+
+extern "C" mrpop_status mrpop_drrt_solve(const mrpop_scene *scene, const mrpop_robotset *robots, const float *start,
+                                         const float *goals, int num_goals, const mrpop_drrt_settings *settings,
+                                         float *path_out, int64_t max_waypoints, mrpop_drrt_solution_fn on_solution,
+                                         void *solution_ctx, mrpop_drrt_result *out) {
+    const int arms = mrpop::robotset_arms(robots);
+    if (!scene || arms < 1 || !start || !goals || num_goals < 1 || !settings || !out)
+        return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "drrt_solve: bad argument");
+    const mrpop_status st = check_settings(*settings);
+    if (st != MRPOP_OK) return st;
+    *out = mrpop_drrt_result{};
+    GpuChecker chk;
+    chk.scene = scene;
+    chk.robots = robots;
+    if (mrpop_workspace_create(&chk.ws) != MRPOP_OK) return MRPOP_ERR_CUDA;
+    Solver sv;
+    sv.validate = &GpuChecker::call;
+    sv.vctx = &chk;
+    sv.device_nn = true;
+    cudaError_t e = cudaStreamCreateWithFlags(&sv.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&sv.d_qx, (size_t)kNNChunk * 7 * MRPOP_MAX_ARMS * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&sv.d_qb, (size_t)kNNChunk * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&sv.d_best, (size_t)kNNChunk * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaHostAlloc(&sv.h_best, (size_t)kNNChunk * sizeof(unsigned long long), cudaHostAllocDefault);
+    if (e != cudaSuccess) return mrpop::fail_status(MRPOP_ERR_CUDA, "drrt_solve: set-up");
+    return solve(sv, arms, start, goals, num_goals, settings, path_out, max_waypoints, on_solution, solution_ctx, out);
+}

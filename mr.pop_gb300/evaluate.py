@@ -3,18 +3,26 @@ format of the reference's `evaluate_mr` (scripts/evaluate_mr.cu:81-109).
 
 For every valid problem (scripts/<robot>_problems.json through
 `problems.load_problems`, or the converted fixture tests/golden/problems.npz)
-the library's planner runs through a session of the validation service, and
-one CSV row is written with the reference's columns:
+one planner runs and one CSV row is written with the reference's columns:
+  - `--planner drrt` (default): the reference's planner, dRRT / AO-x
+    (mrpop_drrt_solve, `drrt.py`) with the driver's settings
+    (scripts/evaluate_mr.cu:162-166: 300 attempts per iteration, granularity
+    64, range 2.0, three passes) and the arms on the reference's compiled-in
+    bases (solve(..., 4, 8) / solve(..., 5, 8), :133-136);
+  - `--planner compact`: this library's compact planner through a session of
+    the validation service.
+Columns:
 
   solved,cost,path_length,start_tree_size,goal_tree_size,iters,wall_ns,
   kernel_ns,copy_ns,num_new_configs,granularity,range,balance,tree_ratio,
   dynamic_domain,dd_alpha,dd_radius,dd_min_radius,configs_str
 
-Columns of the reference's pop_settings (pop_settings.hh:3-32) that this
-planner has no use for (balance, tree_ratio, dynamic_domain, dd_*) carry that
-struct's defaults.  kernel_ns is the time the planner waited for the service
-(all of its validation steps); copy_ns is 0, since the kernels read and write
-the session's page-locked buffers in place.  configs_str lists the path's
+For the dRRT planner the settings columns are its settings and kernel_ns is
+the reference's (from the first pass's start to the end).  For the compact
+planner the columns of pop_settings (pop_settings.hh:3-32) it has no use for
+(balance, tree_ratio, dynamic_domain, dd_*) carry that struct's defaults and
+kernel_ns is the time it waited for the service.  copy_ns is 0: nothing is
+staged (page-locked buffers are read and written in place).  configs_str lists the path's
 configurations, each value followed by a space and each configuration by a
 literal backslash-n, as print_cfg_to_ss does (Planners.hh:43-48).
 """
@@ -55,13 +63,23 @@ class Row:
     kernel_ns: int
 
 
-def csv_row(r: Row, settings: PlanSettings) -> str:
+def settings_columns(settings) -> dict:
+    """The settings columns of a row: a PlanSettings (compact planner) or an
+    mrpop_drrt_settings (dRRT)."""
+    if isinstance(settings, PlanSettings):
+        return dict(POP_DEFAULTS, num_new_configs=settings.batch, granularity=settings.granularity,
+                    range=settings.range)
+    return {k: getattr(settings, k) for k in ("num_new_configs", "granularity", "range", "balance", "tree_ratio",
+                                               "dynamic_domain", "dd_alpha", "dd_radius", "dd_min_radius")}
+
+
+def csv_row(r: Row, settings) -> str:
+    c = settings_columns(settings)
     cfgs = "".join("".join(_g(v) + " " for v in q) + "\\n" for q in r.path)
     f = [str(int(r.solved)), _g(r.cost if r.solved else 0.0), str(len(r.path)), str(r.start_tree),
-         str(r.goal_tree), str(r.iters), str(r.wall_ns), str(r.kernel_ns), "0", str(settings.batch),
-         str(settings.granularity), _g(settings.range), str(POP_DEFAULTS["balance"]),
-         _g(POP_DEFAULTS["tree_ratio"]), str(POP_DEFAULTS["dynamic_domain"]), _g(POP_DEFAULTS["dd_alpha"]),
-         _g(POP_DEFAULTS["dd_radius"]), _g(POP_DEFAULTS["dd_min_radius"])]
+         str(r.goal_tree), str(r.iters), str(r.wall_ns), str(r.kernel_ns), "0", str(c["num_new_configs"]),
+         str(c["granularity"]), _g(c["range"]), str(int(c["balance"])), _g(c["tree_ratio"]),
+         str(int(c["dynamic_domain"])), _g(c["dd_alpha"]), _g(c["dd_radius"]), _g(c["dd_min_radius"])]
     return ", ".join(f) + ", \"" + cfgs + "\"\n"
 
 
@@ -106,7 +124,25 @@ def run(server: M.Server, queries: list[Query], settings: PlanSettings, out_csv:
     return rows
 
 
-def write_csv(rows: list[Row], settings: PlanSettings, out_csv) -> None:
+def run_drrt(queries: list[Query], st, out_csv: str | Path | None = None, native_bases: bool = True) -> list[Row]:
+    """dRRT / AO-x on every query in turn (one mrpop_drrt_solve each); write the CSV.
+    native_bases: the arms on the reference's compiled-in layout (as its
+    driver's solve(..., arms, 8) call places them), else the problem's bases."""
+    from . import drrt
+    rows = []
+    for q in queries:
+        t0 = time.perf_counter_ns()
+        scene = M.Scene(q.scene)
+        robots = M.RobotSet(q.arms, None if native_bases else q.bases)
+        r = drrt.solve(scene, robots, q.start, q.goal, st)
+        rows.append(Row(r.solved, r.cost, r.path, r.stats["start_tree_size"], r.stats["goal_tree_size"], r.iters,
+                        time.perf_counter_ns() - t0, r.stats["kernel_ns"]))
+    if out_csv is not None:
+        write_csv(rows, st, out_csv)
+    return rows
+
+
+def write_csv(rows: list[Row], settings, out_csv) -> None:
     with open(out_csv, "w") as f:
         f.write(CSV_HEADER)
         for r in rows:
@@ -124,7 +160,8 @@ def main(argv=None) -> int:
     ap.add_argument("robot_name", choices=["panda_four", "panda_five"])
     ap.add_argument("run_name")
     ap.add_argument("problems", nargs="?", default=None)
-    ap.add_argument("--max-iters", type=int, default=PlanSettings.max_iters)
+    ap.add_argument("--planner", choices=["drrt", "compact"], default="drrt")
+    ap.add_argument("--max-iters", type=int, default=None, help="iterations per launch (pass)")
     a = ap.parse_args(argv)
     arms = 4 if a.robot_name == "panda_four" else 5
     if a.problems:
@@ -132,12 +169,17 @@ def main(argv=None) -> int:
         queries = problem_queries(load_problems(a.problems), arms)
     else:
         queries = fixture_queries(Path(__file__).resolve().parents[1] / "tests" / "golden" / "problems.npz", arms)
-    settings = PlanSettings(max_iters=a.max_iters)
     Path("test_output").mkdir(exist_ok=True)
     out = Path("test_output") / f"{a.robot_name}_{a.run_name}.csv"
-    server = M.Server(budget_bytes=256 << 20, streams=2)
-    rows = run(server, queries, settings, out)
-    server.close()
+    if a.planner == "drrt":
+        from . import drrt
+        st = drrt.evaluate_settings(**({"max_iters": a.max_iters} if a.max_iters else {}))
+        rows = run_drrt(queries, st, out)
+    else:
+        settings = PlanSettings(max_iters=a.max_iters or PlanSettings.max_iters)
+        server = M.Server(budget_bytes=256 << 20, streams=2)
+        rows = run(server, queries, settings, out)
+        server.close()
     failed = sum(not r.solved for r in rows)
     print(f"Total failed: {failed} / {len(rows)}", file=sys.stdout)
     print(f"wrote {out}")

@@ -34,6 +34,7 @@ EXPORTED = [
     "mrpop_batch_launch", "mrpop_batch_info", "mrpop_batch_destroy", "mrpop_server_create", "mrpop_server_destroy",
     "mrpop_server_get_stats", "mrpop_session_open", "mrpop_session_submit", "mrpop_session_wait",
     "mrpop_session_close", "mrpop_session_host_buffers", "mrpop_plan", "mrpop_session_plan",
+    "mrpop_drrt_settings_default", "mrpop_drrt_solve", "mrpop_drrt_solve_with",
 ]
 KERNEL_KINDS = ("fused", "broad", "narrow")
 NOALLOC_MAX_EDGES = 16384
@@ -83,6 +84,33 @@ class PlanResultC(C.Structure):
 
 VALIDATE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_float,
                           C.c_void_p, C.c_void_p)
+
+
+class DrrtSettingsC(C.Structure):
+    """mrpop_drrt_settings: the reference's pop_settings fields in order, then this library's additions."""
+    _fields_ = [("max_samples", C.c_int32), ("max_iters", C.c_int32), ("optimize_iters", C.c_int32),
+                ("num_new_configs", C.c_int32), ("granularity", C.c_int32), ("range", C.c_float),
+                ("balance", C.c_int32), ("tree_ratio", C.c_float), ("dynamic_domain", C.c_int32),
+                ("dd_alpha", C.c_float), ("dd_radius", C.c_float), ("dd_min_radius", C.c_float),
+                ("roadmap_reassign", C.c_int32), ("rrtc_iter", C.c_int32), ("resample_iter", C.c_int32),
+                ("cost_bound_resample", C.c_int32), ("path_simplify", C.c_int32), ("phs", C.c_int32),
+                ("simplify_round", C.c_int32), ("bspline_step", C.c_int32), ("bspline_min_change", C.c_float),
+                ("perturb_step", C.c_int32), ("perturb_empty_step", C.c_int32), ("block_per_robot", C.c_int32),
+                ("max_launches", C.c_int32), ("seed", C.c_uint64)]
+
+
+class DrrtResultC(C.Structure):
+    _fields_ = [("solved", C.c_int32), ("iters", C.c_int32), ("cost", C.c_float), ("passes", C.c_int32),
+                ("solutions", C.c_int32), ("launches", C.c_int32), ("start_tree_size", C.c_int64),
+                ("goal_tree_size", C.c_int64), ("path_length", C.c_int64), ("roadmap_nodes", C.c_int64 * 5),
+                ("roadmap_edges", C.c_int64 * 5), ("validate_calls", C.c_int64), ("edges_validated", C.c_int64),
+                ("iterations", C.c_int64), ("wall_ns", C.c_int64), ("kernel_ns", C.c_int64),
+                ("validate_ns", C.c_int64), ("nn_ns", C.c_int64)]
+
+
+CHECK_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_float,
+                       C.c_uint32, C.c_int, C.c_void_p, C.c_void_p)
+SOLUTION_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int32, C.c_float, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64)
 
 
 class ServerStats(C.Structure):
@@ -141,6 +169,11 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
         "mrpop_session_host_buffers": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)],
         "mrpop_plan": [i32, vp, vp, C.POINTER(PlanSettingsC), VALIDATE_FN, vp, vp, i64, C.POINTER(PlanResultC)],
         "mrpop_session_plan": [vp, vp, vp, u32, vp, vp, C.POINTER(PlanSettingsC), vp, i64, C.POINTER(PlanResultC)],
+        "mrpop_drrt_settings_default": [C.POINTER(DrrtSettingsC)],
+        "mrpop_drrt_solve": [vp, vp, vp, vp, i32, C.POINTER(DrrtSettingsC), vp, i64, SOLUTION_FN, vp,
+                             C.POINTER(DrrtResultC)],
+        "mrpop_drrt_solve_with": [i32, CHECK_FN, vp, vp, vp, i32, C.POINTER(DrrtSettingsC), vp, i64, SOLUTION_FN, vp,
+                                  C.POINTER(DrrtResultC)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
