@@ -55,6 +55,8 @@ def parse():
                                            "planner4", "planner5"],
                     default="config2")
     ap.add_argument("--problems", type=int, default=50, help="planner4/5: reference problems solved")
+    ap.add_argument("--planner", choices=["drrt", "compact"], default="drrt",
+                    help="config5: the client planner of the served stream")
     ap.add_argument("--rate", type=float, default=200.0, help="config5: query arrivals per second (Poisson)")
     ap.add_argument("--duration", type=float, default=60.0, help="config5: seconds of arrivals")
     ap.add_argument("--isolated", type=int, default=100, help="config5: queries also solved alone, for comparison")
@@ -478,7 +480,15 @@ def run_serving(args, world, rank, local, pkg, torch):
     t0 = time.perf_counter()
     queries = P.make_queries(n, seed=rank, collision_free=collision_free)
     gen_s = time.perf_counter() - t0
-    settings = P.PlanSettings()
+    if args.planner == "drrt":
+        settings = S.served_drrt_settings()
+        planner_desc = ("the reference's dRRT / AO-x (mrpop_session_drrt): per-arm roadmaps, direction oracle, "
+                        "PHS sampling, first pass + 5 optimising passes, B-spline and shortcut simplification")
+        settings_desc = pkg.drrt.settings_dict(settings)
+    else:
+        settings = P.PlanSettings()
+        planner_desc = "batched bidirectional RRT with connect checks and shortcut passes (this library's compact planner)"
+        settings_desc = settings.__dict__
     server = pkg.Server(budget_bytes=2 << 30, streams=4)
     S.isolated(server, queries[:min(3, n)], settings)  # warm-up (first-use set-up of the library)
     m = min(args.isolated, n)
@@ -495,7 +505,7 @@ def run_serving(args, world, rank, local, pkg, torch):
     wall = max_over_ranks(wall, world)
     same = sum(S.same_result(a.result, b.result) for a, b in zip(alone, served[:m]))
     sv, iso = S.summary(served), S.summary(alone)
-    samples = sv["edges"] * settings.granularity  # samples per segment; segmented steps check more
+    samples = sv["edges"] * int(settings.granularity)  # samples per segment; segmented steps check more
     server.close()
     if rank != 0:
         return
@@ -505,9 +515,8 @@ def run_serving(args, world, rank, local, pkg, torch):
            "data": "synthetic (seeded scenes, start/goal rejection-sampled collision-free)",
            "config": {"workload": "config5_served_planning", "rate_qps": args.rate, "duration_s": args.duration,
                       "queries": n, "arms": "2-5 (uniform)", "scenes": "single-arm or bin-picking generator",
-                      "planner": "batched bidirectional RRT with connect checks and shortcut passes (this "
-                                 "project's client; the reference's dRRT/AO-x is not rebuilt)",
-                      "settings": settings.__dict__, "service": "mrpop_server: 2 GiB budget, 4 streams",
+                      "planner": planner_desc,
+                      "settings": settings_desc, "service": "mrpop_server: 2 GiB budget, 4 streams",
                       "query_generation_s": round(gen_s, 2)},
            "latency": {"served_p50_ms": sv["p50_ms"], "served_p99_ms": sv["p99_ms"],
                        "isolated_p50_ms": iso["p50_ms"], "isolated_p99_ms": iso["p99_ms"],

@@ -488,6 +488,8 @@ typedef struct {
     int64_t kernel_ns;        /* from the first pass's start to the end (reference's kernel_ns) */
     int64_t validate_ns;      /* inside validate calls                                    */
     int64_t nn_ns;            /* inside nearest-neighbour searches                        */
+    int64_t oracle_ns;        /* direction oracle and prunes of the attempts (host)       */
+    int64_t roadmap_ns;       /* roadmap neighbour searches (host)                        */
 } mrpop_drrt_result;
 
 mrpop_status mrpop_drrt_settings_default(mrpop_drrt_settings *out);
@@ -499,6 +501,15 @@ mrpop_status mrpop_drrt_solve_with(int arms, mrpop_check_fn validate, void *ctx,
                                    const float *goals, int num_goals, const mrpop_drrt_settings *settings,
                                    float *path_out, int64_t max_waypoints, mrpop_drrt_solution_fn on_solution,
                                    void *solution_ctx, mrpop_drrt_result *out);
+/* The same planner with its checks served by a session of the validation
+ * service (below): every check becomes steps of at most the session's edge
+ * count, co-batched with the steps of the other sessions; the tree searches
+ * run on the device on a stream of the call's own.  The session needs the
+ * robot set's arm count and a granularity of at least settings->granularity. */
+mrpop_status mrpop_session_drrt(mrpop_session *session, const mrpop_scene *scene, const mrpop_robotset *robots,
+                                const float *start, const float *goals, int num_goals,
+                                const mrpop_drrt_settings *settings, float *path_out, int64_t max_waypoints,
+                                mrpop_drrt_solution_fn on_solution, void *solution_ctx, mrpop_drrt_result *out);
 
 /* Algorithmic flop count per edge (FMA = 2; the convention of the project's
  * roofline) for the same arguments as mrpop_validate_segments; writes

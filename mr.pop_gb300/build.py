@@ -19,8 +19,10 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 SOURCES = ["api.cu", "batch.cu", "server.cu", "planner.cu", "drrt.cu", "peak_probe.cu", "no_alloc.cu"] + \
     [f"validate_a{a}.cu" for a in range(1, 6)]
 # the planners' host arithmetic is written with explicit fmaf where the
-# reference's compiler fuses; no other contraction, so x86 and Arm hosts agree
-SOURCE_FLAGS = {"drrt.cu": ["-Xcompiler", "-ffp-contract=off"]}
+# reference's compiler fuses; no other contraction, so x86 and Arm hosts agree;
+# their per-attempt host work runs on OpenMP threads
+SOURCE_FLAGS = {"drrt.cu": ["-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fopenmp"]}
+LINK_FLAGS = ["-Xcompiler", "-fopenmp"]
 
 
 def _nvcc() -> str:
@@ -65,7 +67,7 @@ def build(variant: str = "", defines: tuple[str, ...] = (), verbose: bool = Fals
         objs = list(ex.map(compile_one, SOURCES))
     lib = lib_path(variant)
     if not lib.exists() or lib.stat().st_mtime < max(o.stat().st_mtime for o in objs):
-        cmd = [nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart"]
+        cmd = [nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart", *LINK_FLAGS]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -377,7 +377,7 @@ struct Solver {
     void *vctx = nullptr;
     bool device_nn = false;
     cudaStream_t stream = nullptr;
-    float *d_qx = nullptr, *d_qb = nullptr;
+    float *d_qx = nullptr, *d_qb = nullptr, *h_q = nullptr;
     unsigned long long *d_best = nullptr, *h_best = nullptr;
     mrpop_drrt_result *R = nullptr;
     mrpop_drrt_solution_fn on_solution = nullptr;
@@ -407,10 +407,10 @@ struct Solver {
     ~Solver() {
         T[0].free_device();
         T[1].free_device();
-        if (d_qx) cudaFree(d_qx);
-        if (d_qb) cudaFree(d_qb);
+        if (d_qx) cudaFree(d_qx);  // d_qb lies inside it
         if (d_best) cudaFree(d_best);
         if (h_best) cudaFreeHost(h_best);
+        if (h_q) cudaFreeHost(h_q);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -427,57 +427,118 @@ struct Solver {
     }
 
     // ---- nearest neighbours ------------------------------------------------
-    // idx[q] = nearest node of tree t to x[q] passing the filter, or -1;
-    // sqd[q] = its squared distance.
-    int nearest(Tree &t, const std::vector<float> &x, const std::vector<float> &bound, int mode,
-                std::vector<int> &idx, std::vector<float> &sqd) {
-        const int nq = (int)bound.size();
-        idx.assign(nq, -1);
-        sqd.assign(nq, FLT_MAX);
-        if (nq == 0) return 0;
+    // For both trees at once: idx[t][q] = the node of tree t nearest to
+    // x[t][q] that passes the filter (lowest squared distance, then lowest
+    // index), or -1; sqd[t][q] = its squared distance.  One upload, one launch
+    // per tree and chunk of 128 queries, one read-back.
+    struct NNJob {
+        std::vector<float> x, bound;
+        std::vector<int> who, idx;
+        std::vector<float> sqd;
+        void clear() {
+            x.clear();
+            bound.clear();
+            who.clear();
+        }
+    };
+    size_t d_cap_q = 0;
+
+    int nearest(NNJob *jobs, int mode) {
         const auto t0 = Clock::now();
+        int nq_total = 0;
+        for (int t = 0; t < 2; t++) {
+            const int nq = (int)jobs[t].bound.size();
+            jobs[t].idx.assign(nq, -1);
+            jobs[t].sqd.assign(nq, FLT_MAX);
+            nq_total += nq;
+        }
+        if (nq_total == 0) return 0;
         if (!device_nn) {
-            for (int q = 0; q < nq; q++) {
-                const float *xq = &x[(size_t)q * dim];
-                uint64_t bestk = ~0ull;
-                for (int64_t i = 0; i < t.size(); i++) {
-                    const float s = sq_l2(t.node(i), xq, dim);
-                    const bool pass = (mode == 0 ? t.cost[i] < bound[q] : sqrtf(s) < bound[q]) && s < FLT_MAX;
-                    if (!pass) continue;
-                    uint32_t sb;
-                    std::memcpy(&sb, &s, 4);
-                    const uint64_t k = ((uint64_t)sb << 32) | (uint64_t)(uint32_t)i;
-                    bestk = std::min(bestk, k);
-                }
-                if (bestk != ~0ull) {
-                    idx[q] = (int)(uint32_t)bestk;
-                    const uint32_t sb = (uint32_t)(bestk >> 32);
-                    std::memcpy(&sqd[q], &sb, 4);
+            for (int t = 0; t < 2; t++) {
+                const Tree &tr = T[t];
+                NNJob &J = jobs[t];
+                const int nq = (int)J.bound.size();
+#pragma omp parallel for schedule(dynamic, 4)
+                for (int q = 0; q < nq; q++) {
+                    const float *xq = &J.x[(size_t)q * dim];
+                    uint64_t bestk = ~0ull;
+                    for (int64_t i = 0; i < tr.size(); i++) {
+                        const float sv = sq_l2(tr.node(i), xq, dim);
+                        const bool pass = (mode == 0 ? tr.cost[i] < J.bound[q] : sqrtf(sv) < J.bound[q]) && sv < FLT_MAX;
+                        if (!pass) continue;
+                        uint32_t sb;
+                        std::memcpy(&sb, &sv, 4);
+                        const uint64_t k = ((uint64_t)sb << 32) | (uint64_t)(uint32_t)i;
+                        bestk = std::min(bestk, k);
+                    }
+                    if (bestk != ~0ull) {
+                        J.idx[q] = (int)(uint32_t)bestk;
+                        const uint32_t sb = (uint32_t)(bestk >> 32);
+                        std::memcpy(&J.sqd[q], &sb, 4);
+                    }
                 }
             }
             R->nn_ns += ns_since(t0);
             return 0;
         }
-        cudaError_t e = t.sync_device(stream);
-        for (int c0 = 0; c0 < nq && e == cudaSuccess; c0 += kNNChunk) {
-            const int m = std::min(kNNChunk, nq - c0);
-            e = cudaMemcpyAsync(d_qx, &x[(size_t)c0 * dim], (size_t)m * dim * sizeof(float), cudaMemcpyHostToDevice,
+        cudaError_t e = cudaSuccess;
+        if ((size_t)nq_total > d_cap_q) {
+            const size_t cap = (size_t)std::max(nq_total, 512);
+            if (d_qx) cudaFree(d_qx);
+            if (d_qb) cudaFree(d_qb);
+            if (d_best) cudaFree(d_best);
+            if (h_best) cudaFreeHost(h_best);
+            if (h_q) cudaFreeHost(h_q);
+            d_qx = d_qb = nullptr;
+            d_best = h_best = nullptr;
+            h_q = nullptr;
+            e = cudaMalloc(&d_qx, cap * (dim + 1) * sizeof(float));
+            if (e == cudaSuccess) e = cudaMalloc(&d_best, cap * sizeof(unsigned long long));
+            if (e == cudaSuccess) e = cudaHostAlloc(&h_best, cap * sizeof(unsigned long long), cudaHostAllocDefault);
+            if (e == cudaSuccess) e = cudaHostAlloc(&h_q, cap * (dim + 1) * sizeof(float), cudaHostAllocDefault);
+            if (e != cudaSuccess) return mrpop::fail_status(MRPOP_ERR_CUDA, "drrt: nearest-neighbour buffers");
+            d_qb = d_qx + cap * dim;
+            d_cap_q = cap;
+        }
+        // queries of tree 0 then tree 1, bounds after all queries
+        float *hx = h_q, *hb = h_q + d_cap_q * dim;
+        int off = 0;
+        for (int t = 0; t < 2; t++) {
+            const int nq = (int)jobs[t].bound.size();
+            std::memcpy(hx + (size_t)off * dim, jobs[t].x.data(), (size_t)nq * dim * sizeof(float));
+            std::memcpy(hb + off, jobs[t].bound.data(), (size_t)nq * sizeof(float));
+            off += nq;
+        }
+        for (int t = 0; t < 2 && e == cudaSuccess; t++)
+            if (!jobs[t].bound.empty()) e = T[t].sync_device(stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_qx, hx, (size_t)nq_total * dim * sizeof(float), cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_qb, hb, (size_t)nq_total * sizeof(float), cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(d_best, 0xFF, (size_t)nq_total * sizeof(unsigned long long), stream);
+        off = 0;
+        for (int t = 0; t < 2 && e == cudaSuccess; t++) {
+            const int nq = (int)jobs[t].bound.size();
+            for (int c0 = 0; c0 < nq && e == cudaSuccess; c0 += kNNChunk)
+                e = launch_tree_nn(dim, T[t], d_qx + (size_t)(off + c0) * dim, d_qb + off + c0,
+                                   std::min(kNNChunk, nq - c0), mode, d_best + off + c0, stream);
+            off += nq;
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(h_best, d_best, (size_t)nq_total * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                 stream);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(d_qb, &bound[c0], (size_t)m * sizeof(float), cudaMemcpyHostToDevice, stream);
-            if (e == cudaSuccess) e = cudaMemsetAsync(d_best, 0xFF, (size_t)m * sizeof(unsigned long long), stream);
-            if (e == cudaSuccess) e = launch_tree_nn(dim, t, d_qx, d_qb, m, mode, d_best, stream);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(h_best, d_best, (size_t)m * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                                    stream);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-            for (int q = 0; q < m && e == cudaSuccess; q++) {
-                const unsigned long long k = h_best[q];
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        off = 0;
+        for (int t = 0; t < 2 && e == cudaSuccess; t++) {
+            const int nq = (int)jobs[t].bound.size();
+            for (int q = 0; q < nq; q++) {
+                const unsigned long long k = h_best[off + q];
                 if (k == ~0ull) continue;
-                idx[c0 + q] = (int)(uint32_t)k;
+                jobs[t].idx[q] = (int)(uint32_t)k;
                 const uint32_t sb = (uint32_t)(k >> 32);
-                std::memcpy(&sqd[c0 + q], &sb, 4);
+                std::memcpy(&jobs[t].sqd[q], &sb, 4);
             }
+            off += nq;
         }
         R->nn_ns += ns_since(t0);
         if (e != cudaSuccess) return mrpop::fail_status(MRPOP_ERR_CUDA, "drrt: nearest-neighbour search");
@@ -524,18 +585,24 @@ struct Solver {
             // new node being the edge's end (roadmap_interior.cuh:183-240)
             const int n_old = M.size();
             const int n_new = std::min<int>((int)(nodes.size() / 7), kMaxRoadmap - n_old);
-            std::vector<int> ea, eb;
+            const auto t_nb = Clock::now();
+            std::vector<std::vector<int>> nbr(std::max(n_new, 0));
+#pragma omp parallel for schedule(dynamic, 16)
             for (int j = 0; j < n_new; j++) {
                 const float *x = &nodes[(size_t)j * 7];
                 const int id = n_old + j;
                 for (int i = 0; i < id; i++) {
                     const float *y = i < n_old ? M.node(i) : &nodes[(size_t)(i - n_old) * 7];
-                    if (l2(y, x, 7) < S.range) {
-                        ea.push_back(i);
-                        eb.push_back(id);
-                    }
+                    if (l2(y, x, 7) < S.range) nbr[j].push_back(i);
                 }
             }
+            std::vector<int> ea, eb;
+            for (int j = 0; j < n_new; j++)
+                for (int i : nbr[j]) {
+                    ea.push_back(i);
+                    eb.push_back(n_old + j);
+                }
+            R->roadmap_ns += ns_since(t_nb);
             for (int j = 0; j < n_new; j++) M.add(&nodes[(size_t)j * 7]);
             const int64_t ne = (int64_t)ea.size();
             a0.resize((size_t)ne * 7);
@@ -647,8 +714,8 @@ struct Solver {
     }
 
     // ---- direction oracle (nn_angle_mr, utils.cuh:688-759) ------------------
-    bool nn_angle(const float *sample, int near, float bound, bool optimize, float *out, int *ids) {
-        const Tree &t = T[tree_now];
+    bool nn_angle(int tree, const float *sample, int near, float bound, bool optimize, float *out, int *ids) const {
+        const Tree &t = T[tree];
         const float *vn = t.node(near);
         for (int a = 0; a < arms; a++) {
             const int r0 = t.rid[(size_t)near * arms + a];
@@ -673,7 +740,6 @@ struct Solver {
         }
         return true;
     }
-    int tree_now = 0;
 
     // ---- a solution (record_connected_path, path_processing.cu:11-70) -------
     void record_path(int t, int ti, int oi, int iter) {
@@ -704,22 +770,28 @@ struct Solver {
     }
 
     // ---- one rrtc launch (pop_planner.cu:220-737) -------------------------
-    // Returns the status; *solved = 1 when a connection was made.
+    // Returns the status; *solved = 1 when a connection was made.  Per
+    // iteration: every attempt's sample (in parallel: per-attempt random
+    // streams), one nearest-neighbour search per tree, the direction oracle
+    // and prunes (in parallel), one extend check, tree growth in attempt
+    // order, one connect search per tree, one connect check.
     int rrtc(bool optimize, int *solved) {
         *solved = 0;
         const int N = S.num_new_configs;
         if (optimize && S.phs) phs_setup();
-        std::vector<int> tsel(N, 0);
-        std::vector<float> x((size_t)N * dim), crand(N, FLT_MAX);
+        std::vector<int> tsel(N, 0), near(N), ext_ok(N), ext_exist(N);
+        std::vector<float> x((size_t)N * dim), crand(N, FLT_MAX), nd(N), ext_cost(N), ext_cfg((size_t)N * dim);
+        std::vector<int> ext_ids((size_t)N * arms);
         std::vector<char> live(N);
-        std::vector<int> idx, cidx;
-        std::vector<float> sqd, csqd;
+        NNJob job[2];
         for (int iter = 1;; iter++) {
             if (iter > S.max_iters || (optimize && iter > S.optimize_iters)) return 0;
             if (T[0].size() >= S.max_samples || T[1].size() >= S.max_samples) return 0;
             R->iterations++;
             const int64_t sz[2] = {T[0].size(), T[1].size()};
+            const float bc = best_cost;
             // tree choice, sample, cost bound
+#pragma omp parallel for schedule(static)
             for (int b = 0; b < N; b++) {
                 Rng &r = blk_rng[b];
                 if (iter == 1) {
@@ -735,105 +807,103 @@ struct Solver {
                 } else {
                     phs_sample(r, xb);
                 }
-                live[b] = !(l2(T[0].node(0), xb, dim) + l2(T[1].node(0), xb, dim) >= best_cost);
+                live[b] = !(l2(T[0].node(0), xb, dim) + l2(T[1].node(0), xb, dim) >= bc);
                 if (live[b] && optimize) {
                     const int t = tsel[b];
                     const float gh = l2(T[t].node(0), xb, dim);
                     const float hh = l2(T[1 - t].node(0), xb, dim);
-                    const float range = std::max(best_cost - (gh + hh), 0.0f);
+                    const float range = std::max(bc - (gh + hh), 0.0f);
                     crand[b] = fmaf(r.uniform(), range, gh);
                 }
             }
-            // nearest node of each live attempt in its tree (one search per tree)
-            std::vector<int> near(N, -1);
-            std::vector<float> nd(N, FLT_MAX);
-            for (int t = 0; t < 2; t++) {
-                std::vector<float> qx, qb;
-                std::vector<int> who;
-                for (int b = 0; b < N; b++)
-                    if (live[b] && tsel[b] == t) {
-                        qx.insert(qx.end(), &x[(size_t)b * dim], &x[(size_t)b * dim] + dim);
-                        qb.push_back(optimize ? crand[b] : FLT_MAX);
-                        who.push_back(b);
-                    }
-                const int rc = nearest(T[t], qx, qb, 0, idx, sqd);
-                if (rc) return rc;
-                for (size_t k = 0; k < who.size(); k++) {
-                    near[who[k]] = idx[k] < 0 ? 0 : idx[k];
-                    nd[who[k]] = sqrtf(idx[k] < 0 ? FLT_MAX : sqd[k]);
+            // nearest node of each live attempt in its tree
+            for (int t = 0; t < 2; t++) job[t].clear();
+            for (int b = 0; b < N; b++)
+                if (live[b]) {
+                    NNJob &J = job[tsel[b]];
+                    J.x.insert(J.x.end(), &x[(size_t)b * dim], &x[(size_t)b * dim] + dim);
+                    J.bound.push_back(optimize ? crand[b] : FLT_MAX);
+                    J.who.push_back(b);
                 }
-            }
-            // direction oracle, existing-node test, cost prunes; extend edges
-            struct Ext {
-                int b, t, near, exist;
-                float cost;
-                std::vector<float> cfg;
-                std::vector<int> ids;
-            };
-            std::vector<Ext> ext;
-            std::vector<float> cfg(dim);
-            std::vector<int> ids(arms);
+            int rc = nearest(job, 0);
+            if (rc) return rc;
+            for (int t = 0; t < 2; t++)
+                for (size_t k = 0; k < job[t].who.size(); k++) {
+                    const int b = job[t].who[k];
+                    near[b] = job[t].idx[k] < 0 ? 0 : job[t].idx[k];
+                    nd[b] = sqrtf(job[t].idx[k] < 0 ? FLT_MAX : job[t].sqd[k]);
+                }
+            // direction oracle, existing-node test, cost prunes
+            const auto t_or = Clock::now();
+#pragma omp parallel for schedule(dynamic, 8)
             for (int b = 0; b < N; b++) {
+                ext_ok[b] = 0;
                 if (!live[b]) continue;
                 const int t = tsel[b];
-                tree_now = t;
                 const int nr = near[b];
                 const float bound = optimize ? crand[b] - T[t].cost[nr] : FLT_MAX;
-                if (!nn_angle(&x[(size_t)b * dim], nr, bound, optimize, cfg.data(), ids.data())) continue;
-                const int ex = T[t].existing(cfg.data(), ids.data());
+                float *cfg = &ext_cfg[(size_t)b * dim];
+                int *ids = &ext_ids[(size_t)b * arms];
+                if (!nn_angle(t, &x[(size_t)b * dim], nr, bound, optimize, cfg, ids)) continue;
+                const int ex = T[t].existing(cfg, ids);
                 const float nc = T[t].cost[nr] + nd[b];
                 if (ex >= 0 && (!optimize || nc >= T[t].cost[ex])) continue;
-                if (optimize && nc >= best_cost) continue;
-                ext.push_back(Ext{b, t, nr, ex, nc, cfg, ids});
+                if (optimize && nc >= bc) continue;
+                ext_ok[b] = 1;
+                ext_exist[b] = ex;
+                ext_cost[b] = nc;
             }
+            R->oracle_ns += ns_since(t_or);
+            std::vector<int> ext;
+            for (int b = 0; b < N; b++)
+                if (ext_ok[b]) ext.push_back(b);
             const int64_t ne = (int64_t)ext.size();
             a0.resize((size_t)ne * dim);
             a1.resize((size_t)ne * dim);
             for (int64_t k = 0; k < ne; k++) {
-                std::memcpy(&a0[(size_t)k * dim], T[ext[k].t].node(ext[k].near), dim * sizeof(float));
-                std::memcpy(&a1[(size_t)k * dim], ext[k].cfg.data(), dim * sizeof(float));
+                const int b = ext[k];
+                std::memcpy(&a0[(size_t)k * dim], T[tsel[b]].node(near[b]), dim * sizeof(float));
+                std::memcpy(&a1[(size_t)k * dim], &ext_cfg[(size_t)b * dim], dim * sizeof(float));
             }
-            int rc = check(ne, MRPOP_RULE_PLAIN, 0.0f, MRPOP_CHECK_SELF, -1, g);
+            rc = check(ne, MRPOP_RULE_PLAIN, 0.0f, MRPOP_CHECK_SELF, -1, g);
             if (rc) return rc;
-            // grow the trees in block order; remember the new nodes to connect
+            // grow the trees in attempt order; remember the new nodes to connect
             struct Con {
                 int b, t, node;
             };
             std::vector<Con> con;
             for (int64_t k = 0; k < ne; k++) {
                 if (!ok[k]) continue;
-                Ext &e = ext[k];
-                Tree &tt = T[e.t];
-                if (e.exist >= 0) {  // rewire (pop_planner.cu:571-577)
-                    tt.parent[e.exist] = e.near;
-                    tt.cost[e.exist] = e.cost;
+                const int b = ext[k];
+                Tree &tt = T[tsel[b]];
+                if (ext_exist[b] >= 0) {  // rewire (pop_planner.cu:571-577)
+                    tt.parent[ext_exist[b]] = near[b];
+                    tt.cost[ext_exist[b]] = ext_cost[b];
                     tt.cost_dirty = true;
                     continue;
                 }
-                const int ni = tt.add(e.cfg.data(), e.near, e.cost, e.ids.data());
-                con.push_back(Con{e.b, e.t, ni});
+                const int ni = tt.add(&ext_cfg[(size_t)b * dim], near[b], ext_cost[b], &ext_ids[(size_t)b * arms]);
+                con.push_back(Con{b, tsel[b], ni});
             }
-            // connect: nearest node of the other tree, one search per tree
+            // connect: nearest node of the other tree
+            for (int t = 0; t < 2; t++) job[t].clear();
+            for (size_t k = 0; k < con.size(); k++) {
+                NNJob &J = job[1 - con[k].t];
+                const Tree &tt = T[con[k].t];
+                J.x.insert(J.x.end(), tt.node(con[k].node), tt.node(con[k].node) + dim);
+                J.bound.push_back(optimize ? best_cost - tt.cost[con[k].node] : FLT_MAX);
+                J.who.push_back((int)k);
+            }
+            rc = nearest(job, 1);
+            if (rc) return rc;
             std::vector<int> onear(con.size(), -1);
             std::vector<float> od(con.size(), 0.0f);
-            for (int o = 0; o < 2; o++) {
-                std::vector<float> qx, qb;
-                std::vector<int> who;
-                for (size_t k = 0; k < con.size(); k++)
-                    if (1 - con[k].t == o) {
-                        const Tree &tt = T[con[k].t];
-                        qx.insert(qx.end(), tt.node(con[k].node), tt.node(con[k].node) + dim);
-                        qb.push_back(optimize ? best_cost - tt.cost[con[k].node] : FLT_MAX);
-                        who.push_back((int)k);
+            for (int o = 0; o < 2; o++)
+                for (size_t k = 0; k < job[o].who.size(); k++)
+                    if (job[o].idx[k] >= 0) {
+                        onear[job[o].who[k]] = job[o].idx[k];
+                        od[job[o].who[k]] = sqrtf(job[o].sqd[k]);
                     }
-                rc = nearest(T[o], qx, qb, 1, cidx, csqd);
-                if (rc) return rc;
-                for (size_t k = 0; k < who.size(); k++)
-                    if (cidx[k] >= 0) {
-                        onear[who[k]] = cidx[k];
-                        od[who[k]] = sqrtf(csqd[k]);
-                    }
-            }
             std::vector<int> ck;
             for (size_t k = 0; k < con.size(); k++)
                 if (onear[k] >= 0) ck.push_back((int)k);
@@ -857,7 +927,7 @@ struct Solver {
                 std::vector<float> cur(tt.node(c.node), tt.node(c.node) + dim), vec(dim);
                 const float *target = T[1 - c.t].node(onear[ck[j]]);
                 for (int dd = 0; dd < dim; dd++) vec[dd] = (target[dd] - cur[dd]) / (float)next;
-                for (int s = 0; s < next; s++)
+                for (int s2 = 0; s2 < next; s2++)
                     for (int dd = 0; dd < dim; dd++) cur[dd] += vec[dd];
                 const float ncost = tt.cost[c.node] + d / (float)next;
                 const int ni = tt.add(cur.data(), c.node, ncost, nullptr);
@@ -1101,21 +1171,37 @@ extern "C" mrpop_status mrpop_drrt_settings_default(mrpop_drrt_settings *o) {
     return MRPOP_OK;
 }
 
-extern "C" mrpop_status mrpop_drrt_solve_with(int arms, mrpop_check_fn validate, void *ctx, const float *start,
-                                              const float *goals, int num_goals, const mrpop_drrt_settings *settings,
-                                              float *path_out, int64_t max_waypoints,
-                                              mrpop_drrt_solution_fn on_solution, void *solution_ctx,
-                                              mrpop_drrt_result *out) {
+namespace mrpop {
+
+// The planner with any validator; device_nn: nearest-neighbour searches as a
+// kernel on the current device (else on the host).
+mrpop_status drrt_run(int arms, mrpop_check_fn validate, void *ctx, bool device_nn, const float *start,
+                      const float *goals, int num_goals, const mrpop_drrt_settings *settings, float *path_out,
+                      int64_t max_waypoints, mrpop_drrt_solution_fn on_solution, void *solution_ctx,
+                      mrpop_drrt_result *out) {
     if (arms < 1 || arms > MRPOP_MAX_ARMS || !validate || !start || !goals || num_goals < 1 || !settings || !out)
-        return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "drrt_solve_with: bad argument");
+        return fail_status(MRPOP_ERR_INVALID_ARGUMENT, "drrt: bad argument");
     const mrpop_status st = check_settings(*settings);
     if (st != MRPOP_OK) return st;
     *out = mrpop_drrt_result{};
     Solver sv;
     sv.validate = validate;
     sv.vctx = ctx;
-    sv.device_nn = false;
+    sv.device_nn = device_nn;
+    if (device_nn && cudaStreamCreateWithFlags(&sv.stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail_status(MRPOP_ERR_CUDA, "drrt: stream");
     return solve(sv, arms, start, goals, num_goals, settings, path_out, max_waypoints, on_solution, solution_ctx, out);
+}
+
+}  // namespace mrpop
+
+extern "C" mrpop_status mrpop_drrt_solve_with(int arms, mrpop_check_fn validate, void *ctx, const float *start,
+                                              const float *goals, int num_goals, const mrpop_drrt_settings *settings,
+                                              float *path_out, int64_t max_waypoints,
+                                              mrpop_drrt_solution_fn on_solution, void *solution_ctx,
+                                              mrpop_drrt_result *out) {
+    return mrpop::drrt_run(arms, validate, ctx, false, start, goals, num_goals, settings, path_out, max_waypoints,
+                           on_solution, solution_ctx, out);
 }
 
 extern "C" mrpop_status mrpop_drrt_solve(const mrpop_scene *scene, const mrpop_robotset *robots, const float *start,
@@ -1123,24 +1209,11 @@ extern "C" mrpop_status mrpop_drrt_solve(const mrpop_scene *scene, const mrpop_r
                                          float *path_out, int64_t max_waypoints, mrpop_drrt_solution_fn on_solution,
                                          void *solution_ctx, mrpop_drrt_result *out) {
     const int arms = mrpop::robotset_arms(robots);
-    if (!scene || arms < 1 || !start || !goals || num_goals < 1 || !settings || !out)
-        return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "drrt_solve: bad argument");
-    const mrpop_status st = check_settings(*settings);
-    if (st != MRPOP_OK) return st;
-    *out = mrpop_drrt_result{};
+    if (!scene || arms < 1) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "drrt_solve: bad argument");
     GpuChecker chk;
     chk.scene = scene;
     chk.robots = robots;
     if (mrpop_workspace_create(&chk.ws) != MRPOP_OK) return MRPOP_ERR_CUDA;
-    Solver sv;
-    sv.validate = &GpuChecker::call;
-    sv.vctx = &chk;
-    sv.device_nn = true;
-    cudaError_t e = cudaStreamCreateWithFlags(&sv.stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&sv.d_qx, (size_t)kNNChunk * 7 * MRPOP_MAX_ARMS * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&sv.d_qb, (size_t)kNNChunk * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&sv.d_best, (size_t)kNNChunk * sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaHostAlloc(&sv.h_best, (size_t)kNNChunk * sizeof(unsigned long long), cudaHostAllocDefault);
-    if (e != cudaSuccess) return mrpop::fail_status(MRPOP_ERR_CUDA, "drrt_solve: set-up");
-    return solve(sv, arms, start, goals, num_goals, settings, path_out, max_waypoints, on_solution, solution_ctx, out);
+    return mrpop::drrt_run(arms, &GpuChecker::call, &chk, true, start, goals, num_goals, settings, path_out,
+                           max_waypoints, on_solution, solution_ctx, out);
 }

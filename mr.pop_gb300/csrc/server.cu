@@ -610,3 +610,62 @@ extern "C" mrpop_status mrpop_session_plan(mrpop_session *ss, const mrpop_scene 
     SessionValidator v{ss, scene, robots, flags, 7 * ss->arms};
     return mrpop_plan(ss->arms, start, goal, settings, session_validate, &v, path_out, max_waypoints, out);
 }
+
+namespace {
+
+// Validation of the dRRT planner's checks through a session: each call is cut
+// into steps of at most the session's edge count, each submitted and waited
+// for in turn (single-arm roadmap checks use 7 floats per configuration).
+struct SessionChecker {
+    mrpop_session *ss;
+    const mrpop_scene *scene;
+    const mrpop_robotset *robots;
+};
+
+int session_check(void *ctx, const float *q0, const float *q1, int64_t n, int g, int rule, float range,
+                  uint32_t flags, int arm, uint8_t *valid, int32_t *first_hit) {
+    auto *c = static_cast<SessionChecker *>(ctx);
+    mrpop_session *ss = c->ss;
+    const int dof = 7 * (arm >= 0 ? 1 : ss->arms);
+    for (int64_t e0 = 0; e0 < n; e0 += ss->max_edges) {
+        const int64_t m = std::min<int64_t>(ss->max_edges, n - e0);
+        std::memcpy(ss->h_q0, q0 + e0 * dof, (size_t)m * dof * sizeof(float));
+        std::memcpy(ss->h_q1, q1 + e0 * dof, (size_t)m * dof * sizeof(float));
+        mrpop_batch_item it{};
+        it.scene = c->scene;
+        it.robots = c->robots;
+        it.q0 = ss->h_q0;
+        it.q1 = ss->h_q1;
+        it.n_edges = m;
+        it.granularity = g;
+        it.flags = flags;
+        it.arm = arm;
+        it.valid = ss->h_valid;
+        it.first_hit = ss->h_first;
+        it.rule = rule;
+        it.range = range;
+        mrpop_status st = mrpop_session_submit(ss, &it);
+        if (st == MRPOP_OK) st = mrpop_session_wait(ss, -1);
+        if (st != MRPOP_OK) return st;
+        std::memcpy(valid + e0, ss->h_valid, (size_t)m);
+        std::memcpy(first_hit + e0, ss->h_first, (size_t)m * sizeof(int32_t));
+    }
+    return MRPOP_OK;
+}
+
+}  // namespace
+
+extern "C" mrpop_status mrpop_session_drrt(mrpop_session *ss, const mrpop_scene *scene, const mrpop_robotset *robots,
+                                           const float *start, const float *goals, int num_goals,
+                                           const mrpop_drrt_settings *settings, float *path_out,
+                                           int64_t max_waypoints, mrpop_drrt_solution_fn on_solution,
+                                           void *solution_ctx, mrpop_drrt_result *out) {
+    if (!ss || !settings) return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_drrt: null argument");
+    if (settings->granularity > ss->max_g)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_drrt: the session's granularity is below the settings'");
+    if (mrpop::robotset_arms(robots) != ss->arms)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_drrt: the robot set's arm count differs from the session's");
+    SessionChecker c{ss, scene, robots};
+    return mrpop::drrt_run(ss->arms, session_check, &c, true, start, goals, num_goals, settings, path_out,
+                           max_waypoints, on_solution, solution_ctx, out);
+}

@@ -98,6 +98,24 @@ def solve(scene: M.Scene, robots: M.RobotSet, start, goals, st: M.DrrtSettingsC 
     return _finish(r, sols, dof, arms)
 
 
+def solve_session(session: M.Session, scene: M.Scene, robots: M.RobotSet, start, goals,
+                  st: M.DrrtSettingsC | None = None) -> Result:
+    """dRRT::solve with every check served by a session of the validation
+    service (mrpop_session_drrt; one call, the GIL released throughout)."""
+    lib = scene.lib
+    arms = robots.n_arms
+    dof = 7 * arms
+    st = st or settings()
+    start = np.ascontiguousarray(np.asarray(start, np.float32).reshape(dof))
+    goals = np.ascontiguousarray(np.asarray(goals, np.float32).reshape(-1, dof))
+    sols: list = []
+    cb = _collector(dof, sols)
+    r = M.DrrtResultC()
+    M._check(lib, lib.mrpop_session_drrt(session.handle, scene.handle, robots.handle, start.ctypes.data,
+                                         goals.ctypes.data, len(goals), C.byref(st), None, 0, cb, None, C.byref(r)))
+    return _finish(r, sols, dof, arms)
+
+
 def solve_with(arms: int, validate, start, goals, st: M.DrrtSettingsC | None = None, lib=None) -> Result:
     """The same planner with any validator and nearest-neighbour searches on
     the host: validate(q0, q1, g, rule, range, flags, arm) -> (valid u8 [n],

@@ -34,7 +34,7 @@ EXPORTED = [
     "mrpop_batch_launch", "mrpop_batch_info", "mrpop_batch_destroy", "mrpop_server_create", "mrpop_server_destroy",
     "mrpop_server_get_stats", "mrpop_session_open", "mrpop_session_submit", "mrpop_session_wait",
     "mrpop_session_close", "mrpop_session_host_buffers", "mrpop_plan", "mrpop_session_plan",
-    "mrpop_drrt_settings_default", "mrpop_drrt_solve", "mrpop_drrt_solve_with",
+    "mrpop_drrt_settings_default", "mrpop_drrt_solve", "mrpop_drrt_solve_with", "mrpop_session_drrt",
 ]
 KERNEL_KINDS = ("fused", "broad", "narrow")
 NOALLOC_MAX_EDGES = 16384
@@ -105,7 +105,8 @@ class DrrtResultC(C.Structure):
                 ("goal_tree_size", C.c_int64), ("path_length", C.c_int64), ("roadmap_nodes", C.c_int64 * 5),
                 ("roadmap_edges", C.c_int64 * 5), ("validate_calls", C.c_int64), ("edges_validated", C.c_int64),
                 ("iterations", C.c_int64), ("wall_ns", C.c_int64), ("kernel_ns", C.c_int64),
-                ("validate_ns", C.c_int64), ("nn_ns", C.c_int64)]
+                ("validate_ns", C.c_int64), ("nn_ns", C.c_int64), ("oracle_ns", C.c_int64),
+                ("roadmap_ns", C.c_int64)]
 
 
 CHECK_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_float,
@@ -174,6 +175,8 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
                              C.POINTER(DrrtResultC)],
         "mrpop_drrt_solve_with": [i32, CHECK_FN, vp, vp, vp, i32, C.POINTER(DrrtSettingsC), vp, i64, SOLUTION_FN, vp,
                                   C.POINTER(DrrtResultC)],
+        "mrpop_session_drrt": [vp, vp, vp, vp, vp, i32, C.POINTER(DrrtSettingsC), vp, i64, SOLUTION_FN, vp,
+                               C.POINTER(DrrtResultC)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -1,8 +1,10 @@
-"""Served planning stream: queries arrive as a Poisson process, each runs the
-library's planner (mrpop_session_plan, one call per query with the GIL
-released) on a client thread with its own session of the validation service
+"""Served planning stream: queries arrive as a Poisson process, each runs a
+planner on a client thread with its own session of the validation service
 (`mrpop_server_*`), and all sessions' steps are co-batched on the GPU by the
-service's worker.
+service's worker.  The planner is the reference's dRRT / AO-x
+(mrpop_session_drrt, `drrt.py`) when the settings are mrpop_drrt_settings, or
+the library's compact planner (mrpop_session_plan) for PlanSettings; either
+runs as one library call per query with the GIL released.
 
 A query's latency runs from its arrival to its result, and includes waiting
 for admission (device-memory budget) and for a client thread, creating its
@@ -33,7 +35,34 @@ class Served:
         return 1e3 * (self.finish - self.arrival)
 
 
-def run_query(server: M.Server, q: Query, settings: PlanSettings, flags: int = M.CHECK_ENV | M.CHECK_SELF,
+DRRT_STEP_EDGES = 4096  # a dRRT session's step size: larger checks are cut into steps of this many edges
+
+
+def served_drrt_settings(**overrides):
+    """dRRT / AO-x settings of the served stream: the first pass plus five
+    optimising passes (rrtc_iter 6), as the served workload asks, each pass
+    capped at 25 iterations of 64 attempts and the roadmaps grown by 2 blocks
+    per arm -- a budget scaled down from the reference's 100k iterations per
+    pass so that 200 queries/s fit on one GPU and the host's cores."""
+    from . import drrt
+    base = dict(num_new_configs=64, granularity=32, range=1.5, rrtc_iter=6, max_iters=25, block_per_robot=2,
+                max_launches=4)
+    base.update(overrides)
+    return drrt.settings(**base)
+
+
+def drrt_result(qid: int, r) -> PlanResult:
+    """A dRRT result in the fields the stream's summary and comparison read
+    (the digest folds the solve's counters: equal solves have equal digests)."""
+    s = r.stats
+    digest = hash((s["iterations"], s["validate_calls"], s["edges_validated"], tuple(s["roadmap_edges"]),
+                   s["start_tree_size"], s["goal_tree_size"]))
+    return PlanResult(qid, r.solved, r.path, r.cost if r.solved else float("inf"), int(s["iterations"]),
+                      int(s["validate_calls"]), int(s["edges_validated"]), digest, int(s["start_tree_size"]),
+                      int(s["goal_tree_size"]), int(s["validate_ns"]))
+
+
+def run_query(server: M.Server, q: Query, settings, flags: int = M.CHECK_ENV | M.CHECK_SELF,
               timeout_ms: int = -1, keep: list | None = None) -> PlanResult:
     """One query through a session of `server`: scene and robot set created on
     the device for the query's lifetime, every step validated by the service.
@@ -44,6 +73,15 @@ def run_query(server: M.Server, q: Query, settings: PlanSettings, flags: int = M
     robots = M.RobotSet(q.arms, q.bases, lib=server.lib)
     if keep is not None:
         keep.append((scene, robots))
+    if isinstance(settings, M.DrrtSettingsC):
+        from . import drrt
+        st = M.DrrtSettingsC.from_buffer_copy(settings)
+        st.seed = q.seed
+        sess = server.session(q.arms, DRRT_STEP_EDGES, settings.granularity, timeout_ms)
+        try:
+            return drrt_result(q.qid, drrt.solve_session(sess, scene, robots, q.start, q.goal, st))
+        finally:
+            sess.close()
     max_edges = max(settings.batch, settings.shortcut_pairs)
     sess = server.session(q.arms, max_edges, settings.granularity, timeout_ms)
     try:
@@ -53,7 +91,7 @@ def run_query(server: M.Server, q: Query, settings: PlanSettings, flags: int = M
         sess.close()
 
 
-def isolated(server: M.Server, queries: list[Query], settings: PlanSettings) -> list[Served]:
+def isolated(server: M.Server, queries: list[Query], settings) -> list[Served]:
     """Each query alone: one after another, nothing else on the service."""
     out, keep = [], []
     for q in queries:
@@ -64,7 +102,7 @@ def isolated(server: M.Server, queries: list[Query], settings: PlanSettings) -> 
     return out
 
 
-def stream(server: M.Server, queries: list[Query], rate: float, settings: PlanSettings, seed: int = 0,
+def stream(server: M.Server, queries: list[Query], rate: float, settings, seed: int = 0,
            clients: int = 256) -> list[Served]:
     """Poisson arrivals at `rate` queries/s; each query starts on a free client
     thread (a query that finds none waits, and that wait counts as latency)."""

@@ -141,3 +141,29 @@ def test_served_plans_equal_isolated_plans(cuda, pkg):
     assert st["max_wave_steps"] >= 2  # steps of different queries shared waves
     assert st["bytes_in_use"] == 0
     shared.close()
+
+
+def test_served_drrt_solves_equal_isolated_solves(cuda, pkg):
+    """The reference's planner (dRRT / AO-x) served: each query's checks become
+    session steps co-batched with the other queries' steps.  Every query's
+    result -- path, cost, counters -- is the same alone and in the mix, and
+    equal to a solve on direct library calls."""
+    P, S = pkg.planner, pkg.serving
+    queries = P.make_queries(6, seed=21, collision_free=_collision_free(pkg, cuda))
+    st = pkg.drrt.settings(num_new_configs=48, granularity=16, range=1.5, rrtc_iter=2, max_iters=30,
+                           block_per_robot=2, max_launches=4)
+    server = pkg.Server(budget_bytes=512 << 20, streams=4)
+    alone = S.isolated(server, queries, st)
+    server.close()
+    shared = pkg.Server(budget_bytes=512 << 20, streams=1)
+    mixed = S.stream(shared, queries, rate=1e5, settings=st, seed=2, clients=6)
+    for a, m in zip(alone, mixed):
+        assert S.same_result(a.result, m.result), a.result.qid
+    assert shared.stats()["max_wave_steps"] >= 2
+    shared.close()
+    # the same solve on direct calls (mrpop_drrt_solve): same path and cost
+    q = queries[0]
+    s0 = pkg.drrt.settings(**{k: getattr(st, k) for k, _ in st._fields_})
+    s0.seed = q.seed
+    direct = pkg.drrt.solve(pkg.Scene(q.scene), pkg.RobotSet(q.arms, q.bases), q.start, q.goal, s0)
+    assert direct.solved == alone[0].result.solved and np.array_equal(direct.path, alone[0].result.path)
