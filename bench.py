@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--duration", type=float, default=60.0, help="config5: seconds of arrivals")
     ap.add_argument("--isolated", type=int, default=100, help="config5: queries also solved alone, for comparison")
     ap.add_argument("--instances", type=int, default=512, help="config4: planning instances in the batch")
+    ap.add_argument("--edges", type=int, default=0,
+                    help="config1/2/3: edges (0 = the workload's size); small cases for profiler captures")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle parity counts (CPU leg)")
@@ -158,8 +160,10 @@ def replica_throughput(units_per_rank: int, steps: int, seconds: list, world: in
     return world * units_per_rank * steps / t
 
 
-def load_workload(pkg, name):
+def load_workload(pkg, name, edges: int = 0):
     W = pkg.workloads
+    if edges and name in ("config1", "config2", "config3"):
+        return {"config1": W.config1, "config2": W.config2, "config3": W.config3}[name](n_edges=edges)
     return {"config1": W.config1, "config2": W.config2, "config3": W.config3,
             "config3s": W.config3_shortcuts}[name]()
 
@@ -641,7 +645,7 @@ def run_mine(args, world, rank, local):
         return run_batch(args, world, rank, local, pkg, torch)
     if args.workload in ("planner4", "planner5"):
         return run_planner(args, pkg, torch) if rank == 0 else None
-    wl = load_workload(pkg, args.workload)
+    wl = load_workload(pkg, args.workload, args.edges)
     scene = pkg.Scene(wl.scene)
     robots = pkg.RobotSet(len(wl.bases), wl.bases)
     q0 = torch.from_numpy(wl.q0).cuda()

@@ -409,7 +409,8 @@ mrpop_status mrpop_session_plan(mrpop_session *session, const mrpop_scene *scene
  * Settings: the fields of the reference's pop_settings (pop_settings.hh:3-32)
  * in order, bools as int32, then this library's additions.
  * mrpop_drrt_settings_default fills the reference's defaults (and
- * block_per_robot 8, max_launches 20, seed 1234).  dd_radius, dd_min_radius,
+ * block_per_robot 8, max_launches 20, seed 1234, host_threads 0).  The
+ * result does not depend on host_threads.  dd_radius, dd_min_radius,
  * resample_iter, cost_bound_resample and the perturb fields are carried but
  * read nowhere, as in the reference; dynamic_domain is honoured as the
  * reference computes it (its radii never leave FLT_MAX, so it never prunes).
@@ -467,6 +468,7 @@ typedef struct {
     int32_t block_per_robot;  /* roadmap blocks per arm, 230 samples each per round (8)   */
     int32_t max_launches;     /* bound on the first pass's roadmap + rrtc repeats (20)    */
     uint64_t seed;            /* random streams (1234, the reference's curand seed)       */
+    int32_t host_threads;     /* host threads for the attempts' work; 0: all (0)          */
 } mrpop_drrt_settings;
 
 typedef struct {

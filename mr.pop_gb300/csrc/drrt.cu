@@ -30,6 +30,7 @@
 // (:958-984), the PHS transform (:290-341, 398-442), and the path from the
 // goal to the start (path_processing.cu:11-70).
 #include <cuda_runtime.h>
+#include <omp.h>
 
 #include <algorithm>
 #include <cfloat>
@@ -373,6 +374,7 @@ struct GpuChecker {
 struct Solver {
     mrpop_drrt_settings S;
     int arms = 0, dim = 0, g = 0, num_goals = 0;
+    int nthreads = 1;  // OpenMP threads of the host work
     mrpop_check_fn validate = nullptr;
     void *vctx = nullptr;
     bool device_nn = false;
@@ -458,7 +460,7 @@ struct Solver {
                 const Tree &tr = T[t];
                 NNJob &J = jobs[t];
                 const int nq = (int)J.bound.size();
-#pragma omp parallel for schedule(dynamic, 4)
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
                 for (int q = 0; q < nq; q++) {
                     const float *xq = &J.x[(size_t)q * dim];
                     uint64_t bestk = ~0ull;
@@ -587,7 +589,7 @@ struct Solver {
             const int n_new = std::min<int>((int)(nodes.size() / 7), kMaxRoadmap - n_old);
             const auto t_nb = Clock::now();
             std::vector<std::vector<int>> nbr(std::max(n_new, 0));
-#pragma omp parallel for schedule(dynamic, 16)
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
             for (int j = 0; j < n_new; j++) {
                 const float *x = &nodes[(size_t)j * 7];
                 const int id = n_old + j;
@@ -791,7 +793,7 @@ struct Solver {
             const int64_t sz[2] = {T[0].size(), T[1].size()};
             const float bc = best_cost;
             // tree choice, sample, cost bound
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(nthreads)
             for (int b = 0; b < N; b++) {
                 Rng &r = blk_rng[b];
                 if (iter == 1) {
@@ -835,7 +837,7 @@ struct Solver {
                 }
             // direction oracle, existing-node test, cost prunes
             const auto t_or = Clock::now();
-#pragma omp parallel for schedule(dynamic, 8)
+#pragma omp parallel for schedule(dynamic, 8) num_threads(nthreads)
             for (int b = 0; b < N; b++) {
                 ext_ok[b] = 0;
                 if (!live[b]) continue;
@@ -1118,6 +1120,7 @@ mrpop_status solve(Solver &sv, int arms, const float *start, const float *goals,
                    const mrpop_drrt_settings *settings, float *path_out, int64_t max_waypoints,
                    mrpop_drrt_solution_fn on_solution, void *sctx, mrpop_drrt_result *out) {
     sv.S = *settings;
+    sv.nthreads = settings->host_threads > 0 ? settings->host_threads : omp_get_num_procs();
     sv.arms = arms;
     sv.dim = 7 * arms;
     sv.g = settings->granularity;
@@ -1168,6 +1171,7 @@ extern "C" mrpop_status mrpop_drrt_settings_default(mrpop_drrt_settings *o) {
     o->block_per_robot = 8;
     o->max_launches = 20;
     o->seed = 1234;
+    o->host_threads = 0;
     return MRPOP_OK;
 }
 

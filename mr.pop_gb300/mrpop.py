@@ -96,7 +96,7 @@ class DrrtSettingsC(C.Structure):
                 ("cost_bound_resample", C.c_int32), ("path_simplify", C.c_int32), ("phs", C.c_int32),
                 ("simplify_round", C.c_int32), ("bspline_step", C.c_int32), ("bspline_min_change", C.c_float),
                 ("perturb_step", C.c_int32), ("perturb_empty_step", C.c_int32), ("block_per_robot", C.c_int32),
-                ("max_launches", C.c_int32), ("seed", C.c_uint64)]
+                ("max_launches", C.c_int32), ("seed", C.c_uint64), ("host_threads", C.c_int32)]
 
 
 class DrrtResultC(C.Structure):

@@ -43,10 +43,12 @@ def served_drrt_settings(**overrides):
     optimising passes (rrtc_iter 6), as the served workload asks, each pass
     capped at 25 iterations of 64 attempts and the roadmaps grown by 2 blocks
     per arm -- a budget scaled down from the reference's 100k iterations per
-    pass so that 200 queries/s fit on one GPU and the host's cores."""
+    pass so that 200 queries/s fit on one GPU and the host's cores.  Each
+    query's host work runs on its own client thread (host_threads 1): the
+    concurrency comes from the queries."""
     from . import drrt
     base = dict(num_new_configs=64, granularity=32, range=1.5, rrtc_iter=6, max_iters=25, block_per_robot=2,
-                max_launches=4)
+                max_launches=4, host_threads=1)
     base.update(overrides)
     return drrt.settings(**base)
 
