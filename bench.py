@@ -442,9 +442,8 @@ def run_batch(args, world, rank, local, pkg, torch):
         "config": {"workload": f"config4_uneven_batch_{len(insts)}_instances", "instances": len(insts),
                    "edges": int(eoffs[-1]), "samples": samples, "arms_histogram_1_to_5": arms_hist,
                    "granularities": sorted({wl.granularity for wl in insts}),
-                   "kernel_groups": [{"arms": a, "samples_per_lane": s, "broad_grid": gb, "narrow_grid": gn}
-                                     for a, s, _, gb, gn in groups],
-                   "launch": "one CUDA graph of the batch kernels (tuned grids)",
+                   "kernel_groups": batch.shapes(),
+                   "launch": "one CUDA graph of the batch kernels (tuned chunk size, warps per CTA and grid)",
                    "per_instance_plain_calls_value": loop_value,
                    "l2": "flushed (256 MiB write) before every step",
                    "parallelism": f"replica x{world}, independent batches"},

@@ -219,8 +219,11 @@ mrpop_status mrpop_fk_spheres(const mrpop_robotset *robots, int arm, const float
  * segment of every undecided edge per round) and then one fused kernel for the
  * edges with segments left.  It allocates nothing and reads the inputs as they
  * are at execution time, so a batch can be rerun on refilled buffers.
- * mrpop_batch_tune picks each group's broad and narrow grids by timing
- * (synchronous).  It times launches on the items' own buffers, so it writes
+ * mrpop_batch_tune picks each group's launch shape by timing (synchronous):
+ * the chunk size (edges a CTA takes at a time: 24, 48, 96 or 192) and, for the
+ * broad and the narrow kernel, the warps per CTA (2, 3, 4 or 6; one edge per
+ * warp at a time) and the grid (multiples of the SM count up to the resident
+ * maximum at that CTA size).  It times launches on the items' own buffers, so it writes
  * their outputs: afterwards single-segment items hold their verdicts, but
  * segmented items hold only the first segment round's partial state (their
  * later rounds are not run) -- run the batch or launch its graph before
@@ -256,6 +259,17 @@ mrpop_status mrpop_batch_tune(mrpop_batch *batch, void *stream);
 mrpop_status mrpop_batch_capture(mrpop_batch *batch);
 mrpop_status mrpop_batch_launch(mrpop_batch *batch, void *stream);
 mrpop_status mrpop_batch_info(const mrpop_batch *batch, int64_t *n_groups, int32_t *grids, int64_t max_groups);
+/* Per group, MRPOP_BATCH_SHAPE_INTS values into out[12 * i ..]: {arms, samples
+ * per lane, segmented, chunk edges, chunks, broad warps per CTA, broad grid,
+ * narrow warps, narrow grid, fused warps, fused grid, 0}.
+ * mrpop_batch_set_shape sets one group's shape by hand (chunk_edges and
+ * warps[k] > 0 replace the current values; grids[k] > 0 is capped at the
+ * resident maximum, 0 selects it; k = broad, narrow, fused) and drops a
+ * captured graph.  Results do not depend on the shape. */
+#define MRPOP_BATCH_SHAPE_INTS 12
+mrpop_status mrpop_batch_shapes(const mrpop_batch *batch, int64_t *n_groups, int32_t *out, int64_t max_groups);
+mrpop_status mrpop_batch_set_shape(mrpop_batch *batch, int64_t group, int32_t chunk_edges, const int32_t *warps,
+                                   const int32_t *grids);
 mrpop_status mrpop_batch_destroy(mrpop_batch *batch);
 
 /*

@@ -81,7 +81,7 @@ cudaError_t scratch_pool(cudaMemPool_t *out) {
     return cudaSuccess;
 }
 
-size_t warp_scratch_bytes() { return sizeof(mrpop::WarpScratch) * mrpop::kWarpsPerBlock; }
+size_t block_scratch_bytes() { return sizeof(mrpop::WarpScratch) * mrpop::kWarpsPerBlock; }
 
 // Optional per-kernel timing (mrpop_kernel_timing): a pair of CUDA events is
 // recorded on the caller's stream around every validator launch while it is
@@ -249,7 +249,7 @@ mrpop_status mrpop_scene_create(const mrpop_scene_desc *desc, mrpop_scene **out)
     mrpop::SceneCounts c{(int)desc->num_spheres, (int)desc->num_capsules, (int)desc->num_z_capsules,
                          (int)desc->num_cuboids, (int)desc->num_z_cuboids};
     const mrpop::SceneLayout L = mrpop::scene_layout(c);
-    if ((size_t)L.total * sizeof(float4) + warp_scratch_bytes() > kMaxDynSmem)
+    if ((size_t)L.total * sizeof(float4) + block_scratch_bytes() > kMaxDynSmem)
         return fail(MRPOP_ERR_UNSUPPORTED, "scene_create: scene too large to stage in shared memory (" +
                                                std::to_string(L.total * 16) + " bytes)");
     std::vector<float4> h((size_t)L.total);
@@ -475,7 +475,7 @@ mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots,
     for (int a = 0; a < A; a++)
         for (int i = 0; i < 12; i++) p.base[a][i] = robots->base[arm >= 0 ? arm : a][i];
     p.fbp = broad_flops_per_sample(A, scene->env_test_flops, flags);
-    smem = (size_t)scene->total_f4 * sizeof(float4) + warp_scratch_bytes();
+    smem = (size_t)scene->total_f4 * sizeof(float4) + block_scratch_bytes();
     return MRPOP_OK;
 }
 
@@ -610,25 +610,27 @@ __global__ void trig_kernel(const float *x, long long n, float *c, float *s) {
 }  // namespace
 
 namespace mrpop {
-cudaError_t batch_occupancy(int arms, int mode, bool seg, int spl, size_t smem_bytes, int *blocks_per_sm) {
+size_t warp_scratch_bytes() { return sizeof(WarpScratch); }
+
+cudaError_t batch_occupancy(int arms, int mode, bool seg, int spl, size_t smem_bytes, int warps, int *blocks_per_sm) {
     switch (arms) {
-    case 1: return batch_occupancy_arms<1>(mode, seg, spl, smem_bytes, blocks_per_sm);
-    case 2: return batch_occupancy_arms<2>(mode, seg, spl, smem_bytes, blocks_per_sm);
-    case 3: return batch_occupancy_arms<3>(mode, seg, spl, smem_bytes, blocks_per_sm);
-    case 4: return batch_occupancy_arms<4>(mode, seg, spl, smem_bytes, blocks_per_sm);
-    case 5: return batch_occupancy_arms<5>(mode, seg, spl, smem_bytes, blocks_per_sm);
+    case 1: return batch_occupancy_arms<1>(mode, seg, spl, smem_bytes, warps, blocks_per_sm);
+    case 2: return batch_occupancy_arms<2>(mode, seg, spl, smem_bytes, warps, blocks_per_sm);
+    case 3: return batch_occupancy_arms<3>(mode, seg, spl, smem_bytes, warps, blocks_per_sm);
+    case 4: return batch_occupancy_arms<4>(mode, seg, spl, smem_bytes, warps, blocks_per_sm);
+    case 5: return batch_occupancy_arms<5>(mode, seg, spl, smem_bytes, warps, blocks_per_sm);
     default: return cudaErrorInvalidValue;
     }
 }
 
 cudaError_t launch_batch(int arms, int mode, bool seg, int spl, const BatchParams &b, size_t smem_bytes, int grid,
-                         cudaStream_t stream) {
+                         int warps, cudaStream_t stream) {
     switch (arms) {
-    case 1: return launch_batch_arms<1>(mode, seg, spl, b, smem_bytes, grid, stream);
-    case 2: return launch_batch_arms<2>(mode, seg, spl, b, smem_bytes, grid, stream);
-    case 3: return launch_batch_arms<3>(mode, seg, spl, b, smem_bytes, grid, stream);
-    case 4: return launch_batch_arms<4>(mode, seg, spl, b, smem_bytes, grid, stream);
-    case 5: return launch_batch_arms<5>(mode, seg, spl, b, smem_bytes, grid, stream);
+    case 1: return launch_batch_arms<1>(mode, seg, spl, b, smem_bytes, grid, warps, stream);
+    case 2: return launch_batch_arms<2>(mode, seg, spl, b, smem_bytes, grid, warps, stream);
+    case 3: return launch_batch_arms<3>(mode, seg, spl, b, smem_bytes, grid, warps, stream);
+    case 4: return launch_batch_arms<4>(mode, seg, spl, b, smem_bytes, grid, warps, stream);
+    case 5: return launch_batch_arms<5>(mode, seg, spl, b, smem_bytes, grid, warps, stream);
     default: return cudaErrorInvalidValue;
     }
 }

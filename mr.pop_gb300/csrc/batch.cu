@@ -5,12 +5,17 @@
 //
 // Instances are grouped by (arm count, samples per lane, segmented), the
 // template parameters of the kernels.  Each group gets a device array of
-// parameter blocks, a chunk table (up to kChunkEdges edges of one instance per
+// parameter blocks, a chunk table (up to `chunk` edges of one instance per
 // chunk, instances in order) and work counters; batch_kernel<A, SPL, MODE,
 // SEG> hands chunks to CTAs and edges to warps.  A group's run is a broad and
 // a narrow launch (each after its counter reset); a segmented group runs them
 // for kSegRounds rounds and then the fused kernel.  The captured graph runs
 // each group on its own branch so small groups overlap.
+//
+// Launch shape, per group: the chunk size (edges a CTA takes at a time), and
+// per kernel the warps per CTA (each warp one edge at a time, one lane per
+// sample; fewer warps per CTA put more scene copies -- and fewer warps -- on
+// an SM) and the grid.  mrpop_batch_tune picks all three by timing.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,9 +34,12 @@ struct mrpop_batch {
         int4 *d_chunks = nullptr;
         int n_chunks = 0;
         unsigned long long *d_work = nullptr;  // chunk counters of the broad, narrow and fused launches
-        size_t smem = 0;
+        size_t scene_bytes = 0;       // largest staged scene of the group's instances
+        std::vector<int64_t> edges;   // per instance
+        int chunk = 0;                // edges per chunk
+        int warps[3] = {0, 0, 0};     // warps per CTA of the broad / narrow / fused launch
         int grid[3] = {0, 0, 0};      // CTAs of the broad / narrow / fused launch
-        int max_grid[3] = {0, 0, 0};  // SMs x resident CTAs, at most the chunk count
+        size_t smem(int mode) const { return scene_bytes + (size_t)warps[mode] * mrpop::warp_scratch_bytes(); }
     };
     int device = 0;
     std::vector<Group> groups;
@@ -43,6 +51,8 @@ struct mrpop_batch {
 namespace {
 
 constexpr int kChunkEdges = 96;
+constexpr int kTuneChunks[] = {24, 48, 96, 192};
+constexpr int kTuneWarps[] = {2, 3, 4, 6};
 
 mrpop_status cuda_status(cudaError_t e, const char *what) {
     return mrpop::fail_status(MRPOP_ERR_CUDA, (std::string(what) + ": " + cudaGetErrorString(e)).c_str());
@@ -71,7 +81,35 @@ cudaError_t launch_group(const mrpop_batch::Group &g, int mode, int grid, int se
     p.seg0 = seg0;
     p.work = g.d_work + mode;
     cudaError_t err = cudaMemsetAsync(p.work, 0, sizeof(unsigned long long), s);
-    if (err == cudaSuccess) err = mrpop::launch_batch(g.arms, mode, g.seg, g.spl, p, g.smem, grid, s);
+    if (err == cudaSuccess) err = mrpop::launch_batch(g.arms, mode, g.seg, g.spl, p, g.smem(mode), grid, g.warps[mode], s);
+    return err;
+}
+
+// The chunk table of a group for a chunk size (synchronous upload; the table
+// grows when it needs more room).
+cudaError_t set_chunks(mrpop_batch::Group &g, int chunk) {
+    std::vector<int4> chunks;
+    for (size_t i = 0; i < g.edges.size(); i++)
+        for (int64_t e0 = 0; e0 < g.edges[i]; e0 += chunk)
+            chunks.push_back(make_int4((int)i, (int)e0, (int)std::min<int64_t>(chunk, g.edges[i] - e0), 0));
+    if ((int)chunks.size() > g.n_chunks || !g.d_chunks) {
+        cudaFree(g.d_chunks);
+        g.d_chunks = nullptr;
+        const cudaError_t err = cudaMalloc(&g.d_chunks, chunks.size() * sizeof(int4));
+        if (err != cudaSuccess) return err;
+    }
+    g.n_chunks = (int)chunks.size();
+    g.chunk = chunk;
+    return cudaMemcpy(g.d_chunks, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice);
+}
+
+// The largest grid of a group's kernel at its warps per CTA: SMs x resident
+// CTAs, at most the chunk count.
+cudaError_t max_grid(const mrpop_batch::Group &g, int mode, int warps, int sms, int *out) {
+    int nb = 0;
+    const size_t smem = g.scene_bytes + (size_t)warps * mrpop::warp_scratch_bytes();
+    const cudaError_t err = mrpop::batch_occupancy(g.arms, mode, g.seg, g.spl, smem, warps, &nb);
+    *out = (int)std::max(1LL, std::min<long long>((long long)sms * std::max(nb, 1), g.n_chunks));
     return err;
 }
 
@@ -149,35 +187,26 @@ mrpop_status mrpop_batch_create(const mrpop_batch_item *items, int64_t n_items, 
             g.spl = spl;
             g.seg = seg;
             std::vector<mrpop::EdgeParams> ps;
-            std::vector<int4> chunks;
             for (const Entry &e : ent) {
                 if (e.arms != arms || e.spl != spl || e.seg != seg) continue;
                 if (e.p.n_edges > INT32_MAX) {
                     release(b);
                     return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_create: an item has 2^31 edges or more");
                 }
-                const int item = (int)ps.size();
-                for (int64_t e0 = 0; e0 < e.p.n_edges; e0 += kChunkEdges)
-                    chunks.push_back(make_int4(item, (int)e0, (int)std::min<int64_t>(kChunkEdges, e.p.n_edges - e0), 0));
                 ps.push_back(e.p);
-                g.smem = std::max(g.smem, e.smem);
+                g.edges.push_back(e.p.n_edges);
+                g.scene_bytes = std::max(g.scene_bytes, e.smem - (size_t)mrpop::kWarpsPerBlock * mrpop::warp_scratch_bytes());
             }
             if (ps.empty()) continue;
             g.n_items = (int64_t)ps.size();
-            g.n_chunks = (int)chunks.size();
             err = cudaMalloc(&g.d_items, ps.size() * sizeof(mrpop::EdgeParams));
-            if (err == cudaSuccess) err = cudaMalloc(&g.d_chunks, chunks.size() * sizeof(int4));
             if (err == cudaSuccess) err = cudaMalloc(&g.d_work, 3 * sizeof(unsigned long long));
             if (err == cudaSuccess)
                 err = cudaMemcpy(g.d_items, ps.data(), ps.size() * sizeof(mrpop::EdgeParams), cudaMemcpyHostToDevice);
-            if (err == cudaSuccess)
-                err = cudaMemcpy(g.d_chunks, chunks.data(), chunks.size() * sizeof(int4), cudaMemcpyHostToDevice);
+            if (err == cudaSuccess) err = set_chunks(g, kChunkEdges);
             for (int k = 0; k < (seg ? 3 : 2) && err == cudaSuccess; k++) {
-                int nb = 0;
-                err = mrpop::batch_occupancy(arms, k, seg, spl, g.smem, &nb);
-                const long long cap = (long long)sms * std::max(nb, 1);
-                g.max_grid[k] = (int)std::max(1LL, std::min<long long>(cap, g.n_chunks));
-                g.grid[k] = g.max_grid[k];
+                g.warps[k] = mrpop::kWarpsPerBlock;
+                err = max_grid(g, k, g.warps[k], sms, &g.grid[k]);
             }
             b->groups.push_back(g);
             if (err != cudaSuccess) {
@@ -200,12 +229,16 @@ mrpop_status mrpop_batch_run(mrpop_batch *b, void *stream) {
     return MRPOP_OK;
 }
 
-// Launch-shape tuner: per group and kernel, the grid (CTAs; multiples of the
-// SM count up to the resident maximum, and the chunk count) with the shortest
-// device time over three runs.  Broad launches are tuned first (the narrow
-// kernel reads their output); a segmented group is tuned on its first round
-// and keeps the fused kernel's largest grid.  Synchronous; not for use during
-// capture.
+// Launch-shape tuner.  Per group, for each chunk size (edges per chunk) and
+// each kernel of the split pipeline, every warps-per-CTA choice with every
+// grid (multiples of the SM count up to the resident maximum at that CTA
+// size, and that maximum) is timed over three launches; the group keeps the
+// chunk size whose best broad + narrow times sum lowest, with those shapes.
+// The narrow kernel reads the broad kernel's output, so each narrow timing
+// follows a broad launch.  A segmented group is tuned on its first round and
+// its fused kernel keeps the default shape at the largest grid.  Synchronous;
+// not for use during capture.  It launches on the items' own buffers (see
+// mrpop.h).
 mrpop_status mrpop_batch_tune(mrpop_batch *b, void *stream) {
     if (!b) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_tune: null batch");
     const cudaStream_t s = (cudaStream_t)stream;
@@ -215,37 +248,81 @@ mrpop_status mrpop_batch_tune(mrpop_batch *b, void *stream) {
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
         return cuda_status(cudaGetLastError(), "batch_tune: events");
     cudaError_t err = cudaSuccess;
-    for (int k = 0; k < 2 && err == cudaSuccess; k++) {
-        for (auto &g : b->groups) {
-            std::vector<int> cand;
-            for (int m = 1; (long long)m * sms <= g.max_grid[k]; m++) cand.push_back(m * sms);
-            cand.push_back(g.max_grid[k]);
-            std::sort(cand.begin(), cand.end());
-            cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
-            float best = 1e30f;
-            int best_grid = g.grid[k];
-            for (int grid : cand) {
-                // narrow reads the broad output
-                if (k == 1) err = launch_group(g, mrpop::kBatchBroad, g.grid[0], 0, s);
-                float tot = 0.0f;
-                for (int r = 0; r < 3 && err == cudaSuccess; r++) {
-                    err = cudaEventRecord(e0, s);
-                    if (err == cudaSuccess) err = launch_group(g, k, grid, 0, s);
-                    if (err == cudaSuccess) err = cudaEventRecord(e1, s);
-                    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-                    float ms = 0.0f;
-                    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-                    tot += ms;
-                }
-                if (err != cudaSuccess) break;
-                if (tot < best) {
-                    best = tot;
-                    best_grid = grid;
-                }
-            }
-            g.grid[k] = best_grid;
-            if (err != cudaSuccess) break;
+    auto time3 = [&](mrpop_batch::Group &g, int k, float *out) {
+        float tot = 0.0f;
+        for (int r = 0; r < 3 && err == cudaSuccess; r++) {
+            if (k == 1) err = launch_group(g, mrpop::kBatchBroad, g.grid[0], 0, s);
+            if (err == cudaSuccess) err = cudaEventRecord(e0, s);
+            if (err == cudaSuccess) err = launch_group(g, k, g.grid[k], 0, s);
+            if (err == cudaSuccess) err = cudaEventRecord(e1, s);
+            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+            tot += ms;
         }
+        *out = tot;
+    };
+    for (auto &g : b->groups) {
+        float best_sum = 1e30f;
+        int best_chunk = g.chunk, best_w[2] = {g.warps[0], g.warps[1]}, best_g[2] = {g.grid[0], g.grid[1]};
+        int last_chunks = -1;
+        for (int chunk : kTuneChunks) {
+            if (err != cudaSuccess) break;
+            err = set_chunks(g, chunk);
+            if (err != cudaSuccess || g.n_chunks == last_chunks) continue;  // same table as the last size
+            last_chunks = g.n_chunks;
+            float sum = 0.0f;
+            int cw[2], cg[2];
+            for (int k = 0; k < 2 && err == cudaSuccess; k++) {
+                float best = 1e30f;
+                cw[k] = g.warps[k];
+                cg[k] = g.grid[k];
+                for (int w : kTuneWarps) {
+                    int mg = 0;
+                    err = max_grid(g, k, w, sms, &mg);
+                    if (err != cudaSuccess) break;
+                    std::vector<int> cand;
+                    for (int m = 1; (long long)m * sms <= mg; m++) cand.push_back(m * sms);
+                    cand.push_back(mg);
+                    std::sort(cand.begin(), cand.end());
+                    cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+                    for (int grid : cand) {
+                        g.warps[k] = w;
+                        g.grid[k] = grid;
+                        float t = 0.0f;
+                        time3(g, k, &t);
+                        if (err != cudaSuccess) break;
+                        if (t < best) {
+                            best = t;
+                            cw[k] = w;
+                            cg[k] = grid;
+                        }
+                    }
+                    if (err != cudaSuccess) break;
+                }
+                g.warps[k] = cw[k];  // the narrow kernel is timed behind the best broad shape
+                g.grid[k] = cg[k];
+                sum += best;
+            }
+            if (err == cudaSuccess && sum < best_sum) {
+                best_sum = sum;
+                best_chunk = chunk;
+                best_w[0] = cw[0];
+                best_w[1] = cw[1];
+                best_g[0] = cg[0];
+                best_g[1] = cg[1];
+            }
+        }
+        if (err == cudaSuccess) err = set_chunks(g, best_chunk);
+        g.warps[0] = best_w[0];
+        g.warps[1] = best_w[1];
+        g.grid[0] = best_g[0];
+        g.grid[1] = best_g[1];
+        if (g.seg && err == cudaSuccess) {
+            g.warps[2] = mrpop::kWarpsPerBlock;
+            err = max_grid(g, 2, g.warps[2], sms, &g.grid[2]);
+        }
+        if (err != cudaSuccess) break;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -315,6 +392,50 @@ mrpop_status mrpop_batch_info(const mrpop_batch *b, int64_t *n_groups, int32_t *
         grids[5 * i + 2] = g.seg ? 1 : 0;
         grids[5 * i + 3] = g.grid[0];
         grids[5 * i + 4] = g.grid[1];
+    }
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_batch_shapes(const mrpop_batch *b, int64_t *n_groups, int32_t *out, int64_t max_groups) {
+    if (!b || !n_groups) return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_shapes: null argument");
+    *n_groups = (int64_t)b->groups.size();
+    for (int64_t i = 0; out && i < max_groups && i < (int64_t)b->groups.size(); i++) {
+        const auto &g = b->groups[i];
+        int32_t *o = out + MRPOP_BATCH_SHAPE_INTS * i;
+        const int32_t v[MRPOP_BATCH_SHAPE_INTS] = {g.arms, g.spl, g.seg ? 1 : 0, g.chunk, g.n_chunks,
+                                                   g.warps[0], g.grid[0], g.warps[1], g.grid[1],
+                                                   g.warps[2], g.grid[2], 0};
+        for (int k = 0; k < MRPOP_BATCH_SHAPE_INTS; k++) o[k] = v[k];
+    }
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_batch_set_shape(mrpop_batch *b, int64_t group, int32_t chunk_edges, const int32_t *warps,
+                                   const int32_t *grids) {
+    if (!b || group < 0 || group >= (int64_t)b->groups.size() || !warps || !grids)
+        return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_set_shape: bad argument");
+    auto &g = b->groups[(size_t)group];
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);  // the captured graph used the old shape
+        b->exec = nullptr;
+    }
+    if (chunk_edges > 0 && chunk_edges != g.chunk) {
+        const cudaError_t err = set_chunks(g, chunk_edges);
+        if (err != cudaSuccess) return cuda_status(err, "batch_set_shape: chunks");
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    for (int k = 0; k < 3; k++) {
+        if (k == 2 && !g.seg) continue;
+        if (warps[k] > 0) {
+            if (warps[k] > mrpop::kWarpsPerBlock)
+                return mrpop::fail_status(MRPOP_ERR_INVALID_ARGUMENT, "batch_set_shape: too many warps per CTA");
+            g.warps[k] = warps[k];
+        }
+        int mg = 0;
+        const cudaError_t err = max_grid(g, k, g.warps[k], sms, &mg);
+        if (err != cudaSuccess) return cuda_status(err, "batch_set_shape: occupancy");
+        g.grid[k] = grids[k] > 0 ? std::min(grids[k], mg) : mg;
     }
     return MRPOP_OK;
 }

@@ -19,17 +19,18 @@ cudaError_t launch_validate_arms(KernelKind kind, const EdgeParams &p, size_t sm
 
 // Batch kernels (BatchParams: the instances of one arm count, samples per
 // lane and segmentation kind; mode = kBatchBroad / kBatchNarrow / kBatchFused,
-// seg = segmented instances): resident CTAs per SM at a shared-memory size,
-// and a launch on `grid` CTAs.  The dispatchers switch on the arm count
+// seg = segmented instances): resident CTAs per SM at a shared-memory size
+// and CTA size (warps of 32 threads, 1..kWarpsPerBlock), and a launch on
+// `grid` CTAs of `warps` warps.  The dispatchers switch on the arm count
 // (api.cu).
-cudaError_t batch_occupancy(int arms, int mode, bool seg, int spl, size_t smem_bytes, int *blocks_per_sm);
+cudaError_t batch_occupancy(int arms, int mode, bool seg, int spl, size_t smem_bytes, int warps, int *blocks_per_sm);
 cudaError_t launch_batch(int arms, int mode, bool seg, int spl, const BatchParams &b, size_t smem_bytes, int grid,
-                         cudaStream_t stream);
+                         int warps, cudaStream_t stream);
 template <int A>
-cudaError_t batch_occupancy_arms(int mode, bool seg, int spl, size_t smem_bytes, int *blocks_per_sm);
+cudaError_t batch_occupancy_arms(int mode, bool seg, int spl, size_t smem_bytes, int warps, int *blocks_per_sm);
 template <int A>
 cudaError_t launch_batch_arms(int mode, bool seg, int spl, const BatchParams &b, size_t smem_bytes, int grid,
-                              cudaStream_t stream);
+                              int warps, cudaStream_t stream);
 
 }  // namespace mrpop
 
@@ -52,6 +53,10 @@ mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots,
                          int64_t n_edges, int g, int rule, float range, uint32_t flags, int arm, uint8_t *valid,
                          int32_t *first_hit, int32_t *n_seg_out, double *flops, EdgeParams &p, int &A,
                          size_t &smem);
+
+// Shared-memory scratch of one warp (the per-CTA dynamic size is the staged
+// scene plus this times the warps per CTA).
+size_t warp_scratch_bytes();
 
 // Scratch of the single-segment pipeline (staged flags, candidate masks and
 // reference-sphere bounds): its size, and its slices in p.  Two work counters,

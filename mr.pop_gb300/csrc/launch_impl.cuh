@@ -120,20 +120,26 @@ cudaError_t launch_validate_impl(KernelKind kind, const EdgeParams &p, size_t sm
     return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
-// Batch kernels: the attribute is raised when a batch is created, so launches
-// (and graph capture) do not touch it.
+// Batch kernels: the attribute is raised when a batch is created (or tuned),
+// so launches (and graph capture) do not touch it.  A CTA may have fewer warps
+// than kWarpsPerBlock (the kernel indexes its per-warp scratch by warp).
 template <int A>
-cudaError_t batch_occupancy_impl(int mode, bool seg, int spl, size_t smem_bytes, int *blocks_per_sm) {
+cudaError_t batch_occupancy_impl(int mode, bool seg, int spl, size_t smem_bytes, int warps, int *blocks_per_sm) {
     const void *fn = spl == 2 ? batch_fn<A, 2>(mode, seg) : batch_fn<A, 1>(mode, seg);
-    return prepare_kernel(fn, smem_bytes, blocks_per_sm);
+    cudaError_t err = prepare_kernel(fn, smem_bytes, nullptr);
+    if (err != cudaSuccess) return err;
+    int nb = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * warps, smem_bytes);
+    if (err == cudaSuccess) *blocks_per_sm = nb > 0 ? nb : 1;
+    return err;
 }
 
 template <int A>
 cudaError_t launch_batch_impl(int mode, bool seg, int spl, const BatchParams &b, size_t smem_bytes, int grid,
-                              cudaStream_t stream) {
+                              int warps, cudaStream_t stream) {
     const void *fn = spl == 2 ? batch_fn<A, 2>(mode, seg) : batch_fn<A, 1>(mode, seg);
     void *args[] = {(void *)&b};
-    return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(32 * kWarpsPerBlock), args, smem_bytes, stream);
+    return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(32 * warps), args, smem_bytes, stream);
 }
 
 }  // namespace mrpop
@@ -147,13 +153,13 @@ cudaError_t launch_batch_impl(int mode, bool seg, int spl, const BatchParams &b,
         return launch_validate_impl<A>(kind, p, smem_bytes, stream);                                    \
     }                                                                                                   \
     template <>                                                                                         \
-    cudaError_t batch_occupancy_arms<A>(int mode, bool seg, int spl, size_t smem_bytes,                \
+    cudaError_t batch_occupancy_arms<A>(int mode, bool seg, int spl, size_t smem_bytes, int warps,     \
                                         int *blocks_per_sm) {                                           \
-        return batch_occupancy_impl<A>(mode, seg, spl, smem_bytes, blocks_per_sm);                      \
+        return batch_occupancy_impl<A>(mode, seg, spl, smem_bytes, warps, blocks_per_sm);               \
     }                                                                                                   \
     template <>                                                                                         \
     cudaError_t launch_batch_arms<A>(int mode, bool seg, int spl, const BatchParams &b,                \
-                                     size_t smem_bytes, int grid, cudaStream_t stream) {               \
-        return launch_batch_impl<A>(mode, seg, spl, b, smem_bytes, grid, stream);                       \
+                                     size_t smem_bytes, int grid, int warps, cudaStream_t stream) {    \
+        return launch_batch_impl<A>(mode, seg, spl, b, smem_bytes, grid, warps, stream);                \
     }                                                                                                   \
     }

@@ -194,13 +194,13 @@ cudaError_t launch_one(mrpop_server *s, int arms, bool seg, int spl, size_t smem
     auto it = s->occupancy.find(key);
     if (it == s->occupancy.end()) {
         int nb = 0;
-        const cudaError_t err = mrpop::batch_occupancy(arms, mode, seg, spl, smem, &nb);
+        const cudaError_t err = mrpop::batch_occupancy(arms, mode, seg, spl, smem, mrpop::kWarpsPerBlock, &nb);
         if (err != cudaSuccess) return err;
         it = s->occupancy.emplace(key, std::max(nb, 1)).first;
     }
     const int grid = (int)std::max(1LL, std::min<long long>((long long)s->sms * it->second, n_chunks));
     s->launches++;
-    return mrpop::launch_batch(arms, mode, seg, spl, b, smem, grid, stream);
+    return mrpop::launch_batch(arms, mode, seg, spl, b, smem, grid, mrpop::kWarpsPerBlock, stream);
 }
 
 // Builds the wave's tables in the slot, uploads them and launches every group.

@@ -35,6 +35,7 @@ EXPORTED = [
     "mrpop_server_get_stats", "mrpop_session_open", "mrpop_session_submit", "mrpop_session_wait",
     "mrpop_session_close", "mrpop_session_host_buffers", "mrpop_plan", "mrpop_session_plan",
     "mrpop_drrt_settings_default", "mrpop_drrt_solve", "mrpop_drrt_solve_with", "mrpop_session_drrt",
+    "mrpop_batch_shapes", "mrpop_batch_set_shape",
 ]
 KERNEL_KINDS = ("fused", "broad", "narrow")
 NOALLOC_MAX_EDGES = 16384
@@ -160,6 +161,8 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
         "mrpop_batch_launch": [vp, vp],
         "mrpop_batch_info": [vp, C.POINTER(C.c_int64), vp, i64],
         "mrpop_batch_destroy": [vp],
+        "mrpop_batch_shapes": [vp, C.POINTER(C.c_int64), vp, i64],
+        "mrpop_batch_set_shape": [vp, i64, i32, vp, vp],
         "mrpop_server_create": [C.POINTER(ServerConfig), C.POINTER(vp)],
         "mrpop_server_destroy": [vp],
         "mrpop_server_get_stats": [vp, C.POINTER(ServerStats)],
@@ -431,6 +434,22 @@ class Batch:
         grids = np.zeros(5 * 32, np.int32)
         _check(self.lib, self.lib.mrpop_batch_info(self.handle, C.byref(n), grids.ctypes.data, 32))
         return [tuple(int(x) for x in grids[5 * i:5 * i + 5]) for i in range(min(n.value, 32))]
+
+    SHAPE_KEYS = ("arms", "samples_per_lane", "segmented", "chunk_edges", "chunks", "broad_warps", "broad_grid",
+                  "narrow_warps", "narrow_grid", "fused_warps", "fused_grid")
+
+    def shapes(self) -> list[dict]:
+        """Per group: the launch shape (mrpop_batch_shapes)."""
+        n = C.c_int64()
+        out = np.zeros(12 * 32, np.int32)
+        _check(self.lib, self.lib.mrpop_batch_shapes(self.handle, C.byref(n), out.ctypes.data, 32))
+        return [dict(zip(self.SHAPE_KEYS, (int(x) for x in out[12 * i:12 * i + 11]))) for i in range(min(n.value, 32))]
+
+    def set_shape(self, group: int, chunk_edges: int = 0, warps=(0, 0, 0), grids=(0, 0, 0)):
+        w = np.asarray(warps, np.int32)
+        g = np.asarray(grids, np.int32)
+        _check(self.lib, self.lib.mrpop_batch_set_shape(self.handle, group, chunk_edges, w.ctypes.data,
+                                                        g.ctypes.data))
 
     def __del__(self):
         if getattr(self, "handle", None):

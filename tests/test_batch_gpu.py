@@ -74,6 +74,54 @@ def test_batch_equals_per_instance_calls(cuda, pkg):
         assert it[0].status() == 0
 
 
+def test_batch_every_launch_shape_gives_the_same_results(cuda, pkg):
+    """Every chunk size and warps-per-CTA choice the tuner searches, and a
+    small grid, leave the verdicts unchanged (plain and segmented groups)."""
+    items = _instances(pkg, cuda, 24, 0.06, seed=7)
+    seg_items = []
+    for k, (scene, rb, q0, q1, g, flags, arm) in enumerate(items[:10]):
+        if len(q0) and arm < 0:
+            seg_items.append((scene, rb, q0, q1, g, pkg.CHECK_ENV | pkg.CHECK_SELF, -1, None, None,
+                              pkg.RULE_SHORTCUT, 0.8))
+    ref = _reference(pkg, cuda, items)
+    sref = []
+    for scene, rb, q0, q1, g, flags, arm, _, _, rule, rg in seg_items:
+        v, f = pkg.validate(scene, rb, q0, q1, g, flags, arm, rule, rg)[:2]
+        sref.append((v.cpu().numpy(), f.cpu().numpy()))
+    b = pkg.Batch(items)
+    sb = pkg.Batch(seg_items)
+    for batch, expect in ((b, ref), (sb, sref)):
+        n_groups = len(batch.shapes())
+        for chunk in (24, 48, 96, 192):
+            for w in (2, 3, 4, 6):
+                for gi in range(n_groups):
+                    batch.set_shape(gi, chunk, (w, w, w), (0, 0, 0))
+                for v, f in zip(batch.valid, batch.first_hit):
+                    v.fill_(7)
+                    f.fill_(-9)
+                batch.run()
+                cuda.cuda.synchronize()
+                _check(batch, expect)
+                sh = batch.shapes()
+                assert all(s["chunk_edges"] == chunk and s["broad_warps"] == w and s["narrow_warps"] == w for s in sh)
+        for gi in range(n_groups):  # a grid smaller than the SM count
+            batch.set_shape(gi, 48, (3, 4, 6), (7, 5, 3))
+        batch.run()
+        cuda.cuda.synchronize()
+        _check(batch, expect)
+        batch.tune()
+        for v, f in zip(batch.valid, batch.first_hit):
+            v.fill_(7)
+            f.fill_(-9)
+        batch.capture()
+        batch.launch()
+        cuda.cuda.synchronize()
+        _check(batch, expect)
+        for s in batch.shapes():
+            assert s["chunk_edges"] in (24, 48, 96, 192) and s["broad_warps"] in (2, 3, 4, 6)
+            assert s["narrow_warps"] in (2, 3, 4, 6) and s["broad_grid"] >= 1
+
+
 def test_batch_refilled_inputs(cuda, pkg):
     """A captured batch reads its input buffers at execution time."""
     items = _instances(pkg, cuda, 12, 0.05, seed=2)
