@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle parity counts (CPU leg)")
+    ap.add_argument("--no-others", action="store_true",
+                    help="skip the secondary device-timed lines of configs 1, 3 and the shortcut set")
     return ap.parse_args()
 
 
@@ -331,6 +333,90 @@ def parity_counts(orc, pkg, torch, wl, valid: np.ndarray, first: np.ndarray, ban
             "edges_differ_unambiguous": int(len(idx)), "edges_differ_after_device_trig_replay": replay,
             "ambiguous_edges": int(amb.sum()), "ambiguous_samples": int(o["amb_samples"].sum()), "band_m": band,
             "invalid_edges": int((valid == 0).sum()), "oracle_s": round(time.perf_counter() - t, 1)}
+
+
+def timed_steps(step, steps: int, warmup: int, torch, flush) -> float:
+    """Seconds per step: CUDA events around each step, L2 flushed before each."""
+    for _ in range(warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for s_, e_ in ev:
+        flush.zero_()
+        s_.record()
+        step()
+        e_.record()
+    torch.cuda.synchronize()
+    return sum(s_.elapsed_time(e_) for s_, e_ in ev) / 1e3 / steps
+
+
+def segment_counts(orc, wl) -> np.ndarray:
+    L = orc.lib()
+    return np.array([L.oracle_segment_count(a.ctypes.data, b.ctypes.data, a.shape[0], wl.rule, float(wl.range_))
+                     for a, b in zip(wl.q0, wl.q1)], np.int64)
+
+
+def other_workloads_mine(pkg, torch, steps: int = 5, warmup: int = 3) -> dict:
+    """Secondary lines: configs 1 and 3 and the config-3 shortcut set, device-timed
+    (CUDA events, L2 flushed before every step), through mrpop_validate_*."""
+    out = {}
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for name in ("config1", "config3", "config3s"):
+        wl = load_workload(pkg, name)
+        scene = pkg.Scene(wl.scene)
+        rb = pkg.RobotSet(len(wl.bases), wl.bases)
+        q0, q1 = torch.from_numpy(wl.q0).cuda(), torch.from_numpy(wl.q1).cuda()
+        n = len(wl.q0)
+        v = torch.empty(n, dtype=torch.uint8, device="cuda")
+        f = torch.empty(n, dtype=torch.int32, device="cuda")
+        ns = torch.empty(n, dtype=torch.int32, device="cuda") if wl.rule else None
+
+        def step():
+            pkg.validate(scene, rb, q0, q1, wl.granularity, wl.flags, wl.arm, wl.rule, wl.range_, valid=v,
+                         first_hit=f, n_seg=ns)
+
+        dt = timed_steps(step, steps, warmup, torch, flush)
+        samples = n * wl.granularity
+        if wl.rule:
+            # segments up to the first colliding one (the reference's loop stops there) x g
+            vv, ff = v.cpu().numpy(), f.cpu().numpy().astype(np.int64)
+            nn = ns.cpu().numpy().astype(np.int64)
+            segs = np.where(vv == 1, np.maximum(nn, 0), np.where(ff > 0, (ff - 1) // wl.granularity + 1, 0))
+            samples = int(segs.sum()) * wl.granularity
+        out[wl.name] = {"value": samples / dt, "unit": UNIT, "ms_per_step": dt * 1e3, "edges": n,
+                        "granularity": wl.granularity, "steps": steps, "warmup": warmup}
+    return out
+
+
+def other_workloads_reference(pkg, torch, orc, R, flush, steps: int = 3, warmup: int = 1) -> dict:
+    """The same secondary lines on the reference's own edge check (harness
+    launches of 8 blocks per SM, one edge per block at a time)."""
+    out = {}
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    for name in ("config1", "config3", "config3s"):
+        wl = load_workload(pkg, name)
+        kind = R.KIND_SINGLE if wl.arm >= 0 else R.KIND_COMPOSITE
+        arms = len(wl.bases)
+        if kind == R.KIND_COMPOSITE:
+            R.set_bases(arms, wl.bases)
+        env = R.make_env(wl.scene)
+        q0, q1 = torch.from_numpy(wl.q0).cuda(), torch.from_numpy(wl.q1).cuda()
+        n = len(wl.q0)
+        res = (torch.empty(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda"))
+
+        def step():
+            R.validate(env, q0, q1, wl.granularity, kind, wl.rule, wl.range_, arms if kind == R.KIND_COMPOSITE else 1,
+                       max(wl.arm, 0), blocks=sms * 8, out=res)
+
+        dt = timed_steps(step, steps, warmup, torch, flush)
+        samples = n * wl.granularity
+        if wl.rule:
+            v, sf = res[0].cpu().numpy(), res[1].cpu().numpy().astype(np.int64)
+            samples = int(np.where(v == 1, np.maximum(segment_counts(orc, wl), 0), sf + 1).sum()) * wl.granularity
+        out[wl.name] = {"value": samples / dt, "unit": UNIT, "ms_per_step": dt * 1e3, "edges": n,
+                        "granularity": wl.granularity, "steps": steps, "warmup": warmup}
+    return out
 
 
 def run_batch(args, world, rank, local, pkg, torch):
@@ -742,6 +828,8 @@ def run_mine(args, world, rank, local):
                       "path": "mrpop_validate_edges_host with pinned host buffers, which the kernels read "
                               "(endpoints) and write (verdicts) in place over NVLink-C2C; sync inside"}
         assert np.array_equal(av, valid.cpu().numpy())
+    if rank == 0 and world == 1 and not args.no_others and args.workload == "config2" and not args.edges:
+        out["other_workloads"] = other_workloads_mine(pkg, torch)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as orc
         out["cpu_baseline"] = cpu_baseline(orc, wl, min(n, 65536))
@@ -881,6 +969,8 @@ def run_reference(args, world, rank, local):
                                      "sample": "the reference's own CUDA edge check (fkcc_single_buffer*, "
                                                "utils.cuh:447-686) compiled from its sources for sm_103a and run "
                                                "on this GB300 over the full workload"}})
+        if args.workload == "config2" and not args.no_others:
+            out["other_workloads"] = other_workloads_reference(pkg, torch, orc, R, flush)
     else:
         threads = orc.max_threads()
         m = min(n, 4096)
