@@ -38,6 +38,7 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <string>
 #include <unordered_map>
 #include <vector>
 
@@ -309,6 +310,46 @@ cudaError_t launch_tree_nn(int dim, const Tree &t, const float *d_qx, const floa
     return cudaGetLastError();
 }
 
+// Roadmap neighbour pairs: for every new node j in [n_old, n) and every node
+// i < j, the pair (i, j) when the reference's distance (utils.cuh:123-133;
+// node i minus node j, squares fused) is below `range`.  Pairs go to `out` in
+// no particular order (the host sorts them); `count` receives how many there
+// are, also beyond `cap`, so the caller can grow the buffer and search again.
+__global__ void __launch_bounds__(256) roadmap_pairs_kernel(const float *__restrict__ q, int n_old, int n,
+                                                            float range, int2 *__restrict__ out,
+                                                            unsigned int *__restrict__ count, unsigned int cap) {
+    const int j = n_old + (int)blockIdx.y;
+    if (j >= n) return;
+    float x[7];
+#pragma unroll
+    for (int d = 0; d < 7; d++) x[d] = q[(size_t)j * 7 + d];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < j; i += gridDim.x * blockDim.x) {
+        float s = 0.0f;
+#pragma unroll
+        for (int d = 0; d < 7; d++) {
+            const float t = q[(size_t)i * 7 + d] - x[d];
+            s = __fmaf_rn(t, t, s);
+        }
+        if (sqrtf(s) < range) {
+            const unsigned int k = atomicAdd(count, 1u);
+            if (k < cap) out[k] = make_int2(i, j);
+        }
+    }
+}
+
+cudaError_t launch_roadmap_pairs(const float *q, int n_old, int n, float range, int2 *out, unsigned int *count,
+                                 unsigned int cap, cudaStream_t s) {
+    const int n_new = n - n_old;
+    if (n_new <= 0) return cudaSuccess;
+    const unsigned gx = (unsigned)std::min<int64_t>(64, ((int64_t)n + 255) / 256);
+    for (int y0 = 0; y0 < n_new; y0 += 65535) {  // gridDim.y limit
+        const int ny = std::min(65535, n_new - y0);
+        roadmap_pairs_kernel<<<dim3(gx, (unsigned)ny), 256, 0, s>>>(q, n_old + y0, n_old + y0 + ny, range, out,
+                                                                    count, cap);
+    }
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Validation on this library's kernels: page-locked staging buffers that the
 // kernels read and write in place (mrpop_validate_edges_host).
@@ -413,6 +454,11 @@ struct Solver {
         if (d_best) cudaFree(d_best);
         if (h_best) cudaFreeHost(h_best);
         if (h_q) cudaFreeHost(h_q);
+        for (float *p : d_rm)
+            if (p) cudaFree(p);
+        if (d_pairs) cudaFree(d_pairs);
+        if (d_npairs) cudaFree(d_npairs);
+        if (h_npairs) cudaFreeHost(h_npairs);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -563,6 +609,84 @@ struct Solver {
     }
 
     // One round: `blocks[a]` blocks of 230 samples grow arm a's roadmap.
+    // Roadmap neighbour pairs on the device: the arm's nodes [0, n) mirrored
+    // in device memory, every (i, j) with n_old <= j, i < j and the reference's
+    // distance below `range` found by roadmap_pairs_kernel, then sorted by (j, i)
+    // -- the host loop's order, so both paths give the same edges.
+    std::vector<float *> d_rm;
+    std::vector<int64_t> d_rm_cap, d_rm_up;
+    int2 *d_pairs = nullptr;
+    unsigned int *d_npairs = nullptr, *h_npairs = nullptr;
+    size_t d_pairs_cap = 0;
+
+    int roadmap_pairs_device(int a, int n_old, std::vector<int> &ea, std::vector<int> &eb) {
+        const Roadmap &M = rm[a];
+        const int n = M.size();
+        cudaError_t e = cudaSuccess;
+        if (d_rm.size() < (size_t)arms) {
+            d_rm.assign(arms, nullptr);
+            d_rm_cap.assign(arms, 0);
+            d_rm_up.assign(arms, 0);
+        }
+        if (n > d_rm_cap[a]) {
+            int64_t cap = std::max<int64_t>(2 * d_rm_cap[a], 16384);
+            while (cap < n) cap *= 2;
+            float *p = nullptr;
+            e = cudaMalloc(&p, (size_t)cap * 7 * sizeof(float));
+            if (e != cudaSuccess) return fail_cuda(e, "roadmap mirror");
+            if (d_rm[a]) cudaFree(d_rm[a]);
+            d_rm[a] = p;
+            d_rm_cap[a] = cap;
+            d_rm_up[a] = 0;
+        }
+        if (n > d_rm_up[a])
+            e = cudaMemcpyAsync(d_rm[a] + d_rm_up[a] * 7, M.node((int)d_rm_up[a]),
+                                (size_t)(n - d_rm_up[a]) * 7 * sizeof(float), cudaMemcpyHostToDevice, stream);
+        d_rm_up[a] = n;
+        if (!d_npairs) {
+            if (e == cudaSuccess) e = cudaMalloc(&d_npairs, sizeof(unsigned int));
+            if (e == cudaSuccess) e = cudaHostAlloc(&h_npairs, sizeof(unsigned int), cudaHostAllocDefault);
+        }
+        const int n_new = n - n_old;
+        for (int attempt = 0; attempt < 2 && e == cudaSuccess && n_new > 0; attempt++) {
+            if (!d_pairs) {
+                d_pairs_cap = std::max<size_t>(d_pairs_cap, (size_t)1 << 20);
+                e = cudaMalloc(&d_pairs, d_pairs_cap * sizeof(int2));
+                if (e != cudaSuccess) break;
+            }
+            e = cudaMemsetAsync(d_npairs, 0, sizeof(unsigned int), stream);
+            if (e == cudaSuccess) e = launch_roadmap_pairs(d_rm[a], n_old, n, S.range, d_pairs, d_npairs,
+                                                           (unsigned int)d_pairs_cap, stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(h_npairs, d_npairs, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+            if (e != cudaSuccess) break;
+            const size_t np = *h_npairs;
+            if (np > d_pairs_cap) {  // grow and search again
+                cudaFree(d_pairs);
+                d_pairs = nullptr;
+                d_pairs_cap = np + (np >> 2);
+                continue;
+            }
+            std::vector<int2> pairs(np);
+            if (np) e = cudaMemcpy(pairs.data(), d_pairs, np * sizeof(int2), cudaMemcpyDeviceToHost);
+            std::sort(pairs.begin(), pairs.end(),
+                      [](const int2 &p, const int2 &q) { return p.y != q.y ? p.y < q.y : p.x < q.x; });
+            ea.resize(np);
+            eb.resize(np);
+            for (size_t k = 0; k < np; k++) {
+                ea[k] = pairs[k].x;
+                eb[k] = pairs[k].y;
+            }
+            break;
+        }
+        if (e != cudaSuccess) return fail_cuda(e, "roadmap neighbour search");
+        return 0;
+    }
+    static int fail_cuda(cudaError_t e, const char *what) {
+        return mrpop::fail_status(MRPOP_ERR_CUDA, (std::string("drrt: ") + what + ": " + cudaGetErrorString(e)).c_str());
+    }
+
     int roadmap_round(const std::vector<int> &blocks) {
         for (int a = 0; a < arms; a++) {
             const int nb = blocks[a];
@@ -584,28 +708,31 @@ struct Solver {
             for (int64_t k = 0; k < K; k++)
                 if (ok[k]) nodes.insert(nodes.end(), &a0[(size_t)k * 7], &a0[(size_t)k * 7] + 7);
             // edges: every existing node within `range` of each new node, the
-            // new node being the edge's end (roadmap_interior.cuh:183-240)
+            // new node being the edge's end (roadmap_interior.cuh:183-240),
+            // ordered by new node, then old node
             const int n_old = M.size();
             const int n_new = std::min<int>((int)(nodes.size() / 7), kMaxRoadmap - n_old);
             const auto t_nb = Clock::now();
-            std::vector<std::vector<int>> nbr(std::max(n_new, 0));
-#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
-            for (int j = 0; j < n_new; j++) {
-                const float *x = &nodes[(size_t)j * 7];
-                const int id = n_old + j;
-                for (int i = 0; i < id; i++) {
-                    const float *y = i < n_old ? M.node(i) : &nodes[(size_t)(i - n_old) * 7];
-                    if (l2(y, x, 7) < S.range) nbr[j].push_back(i);
-                }
-            }
-            std::vector<int> ea, eb;
-            for (int j = 0; j < n_new; j++)
-                for (int i : nbr[j]) {
-                    ea.push_back(i);
-                    eb.push_back(n_old + j);
-                }
-            R->roadmap_ns += ns_since(t_nb);
             for (int j = 0; j < n_new; j++) M.add(&nodes[(size_t)j * 7]);
+            std::vector<int> ea, eb;
+            if (device_nn) {
+                rc = roadmap_pairs_device(a, n_old, ea, eb);
+                if (rc) return rc;
+            } else {
+                std::vector<std::vector<int>> nbr(std::max(n_new, 0));
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+                for (int j = 0; j < n_new; j++) {
+                    const float *x = M.node(n_old + j);
+                    for (int i = 0; i < n_old + j; i++)
+                        if (l2(M.node(i), x, 7) < S.range) nbr[j].push_back(i);
+                }
+                for (int j = 0; j < n_new; j++)
+                    for (int i : nbr[j]) {
+                        ea.push_back(i);
+                        eb.push_back(n_old + j);
+                    }
+            }
+            R->roadmap_ns += ns_since(t_nb);
             const int64_t ne = (int64_t)ea.size();
             a0.resize((size_t)ne * 7);
             a1.resize((size_t)ne * 7);
