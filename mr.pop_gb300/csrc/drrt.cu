@@ -420,8 +420,7 @@ struct Solver {
     void *vctx = nullptr;
     bool device_nn = false;
     cudaStream_t stream = nullptr;
-    float *d_qx = nullptr, *d_qb = nullptr, *h_q = nullptr;
-    unsigned long long *d_best = nullptr, *h_best = nullptr;
+    void *d_stage = nullptr, *h_stage = nullptr;  // nearest-neighbour staging block (device, page-locked)
     mrpop_drrt_result *R = nullptr;
     mrpop_drrt_solution_fn on_solution = nullptr;
     void *sctx = nullptr;
@@ -450,10 +449,8 @@ struct Solver {
     ~Solver() {
         T[0].free_device();
         T[1].free_device();
-        if (d_qx) cudaFree(d_qx);  // d_qb lies inside it
-        if (d_best) cudaFree(d_best);
-        if (h_best) cudaFreeHost(h_best);
-        if (h_q) cudaFreeHost(h_q);
+        if (d_stage) cudaFree(d_stage);
+        if (h_stage) cudaFreeHost(h_stage);
         for (float *p : d_rm)
             if (p) cudaFree(p);
         if (d_pairs) cudaFree(d_pairs);
@@ -529,27 +526,26 @@ struct Solver {
             R->nn_ns += ns_since(t0);
             return 0;
         }
+        // one staging block per search, uploaded with one copy: the result
+        // words preset to "none", then tree 0's queries and tree 1's, then
+        // their bounds
         cudaError_t e = cudaSuccess;
-        if ((size_t)nq_total > d_cap_q) {
-            const size_t cap = (size_t)std::max(nq_total, 512);
-            if (d_qx) cudaFree(d_qx);
-            if (d_qb) cudaFree(d_qb);
-            if (d_best) cudaFree(d_best);
-            if (h_best) cudaFreeHost(h_best);
-            if (h_q) cudaFreeHost(h_q);
-            d_qx = d_qb = nullptr;
-            d_best = h_best = nullptr;
-            h_q = nullptr;
-            e = cudaMalloc(&d_qx, cap * (dim + 1) * sizeof(float));
-            if (e == cudaSuccess) e = cudaMalloc(&d_best, cap * sizeof(unsigned long long));
-            if (e == cudaSuccess) e = cudaHostAlloc(&h_best, cap * sizeof(unsigned long long), cudaHostAllocDefault);
-            if (e == cudaSuccess) e = cudaHostAlloc(&h_q, cap * (dim + 1) * sizeof(float), cudaHostAllocDefault);
+        const size_t stage_bytes = (size_t)nq_total * (sizeof(unsigned long long) + (dim + 1) * sizeof(float));
+        if (stage_bytes > d_cap_q) {
+            const size_t cap = std::max(stage_bytes, (size_t)512 * (sizeof(unsigned long long) + 36 * sizeof(float)));
+            if (d_stage) cudaFree(d_stage);
+            if (h_stage) cudaFreeHost(h_stage);
+            d_stage = h_stage = nullptr;
+            e = cudaMalloc(&d_stage, cap);
+            if (e == cudaSuccess) e = cudaHostAlloc(&h_stage, cap, cudaHostAllocDefault);
             if (e != cudaSuccess) return mrpop::fail_status(MRPOP_ERR_CUDA, "drrt: nearest-neighbour buffers");
-            d_qb = d_qx + cap * dim;
             d_cap_q = cap;
         }
-        // queries of tree 0 then tree 1, bounds after all queries
-        float *hx = h_q, *hb = h_q + d_cap_q * dim;
+        auto *h_best = reinterpret_cast<unsigned long long *>(h_stage);
+        float *hx = reinterpret_cast<float *>(h_best + nq_total), *hb = hx + (size_t)nq_total * dim;
+        auto *d_best = reinterpret_cast<unsigned long long *>(d_stage);
+        float *d_qx = reinterpret_cast<float *>(d_best + nq_total), *d_qb = d_qx + (size_t)nq_total * dim;
+        std::memset(h_best, 0xFF, (size_t)nq_total * sizeof(unsigned long long));
         int off = 0;
         for (int t = 0; t < 2; t++) {
             const int nq = (int)jobs[t].bound.size();
@@ -559,11 +555,7 @@ struct Solver {
         }
         for (int t = 0; t < 2 && e == cudaSuccess; t++)
             if (!jobs[t].bound.empty()) e = T[t].sync_device(stream);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(d_qx, hx, (size_t)nq_total * dim * sizeof(float), cudaMemcpyHostToDevice, stream);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(d_qb, hb, (size_t)nq_total * sizeof(float), cudaMemcpyHostToDevice, stream);
-        if (e == cudaSuccess) e = cudaMemsetAsync(d_best, 0xFF, (size_t)nq_total * sizeof(unsigned long long), stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_stage, h_stage, stage_bytes, cudaMemcpyHostToDevice, stream);
         off = 0;
         for (int t = 0; t < 2 && e == cudaSuccess; t++) {
             const int nq = (int)jobs[t].bound.size();
