@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--problems", type=int, default=50, help="planner4/5: reference problems solved")
     ap.add_argument("--planner", choices=["drrt", "compact"], default="drrt",
                     help="config5: the client planner of the served stream")
+    ap.add_argument("--streams", type=int, default=0, help="config5: the service's wave slots (0: the planner's default)")
+    ap.add_argument("--clients", type=int, default=0, help="config5: client threads (0: the planner's default)")
+    ap.add_argument("--fused-edges", type=int, default=0,
+                    help="config5: wave groups of at most this many edges run fused (0: the service default, -1: never)")
     ap.add_argument("--rate", type=float, default=200.0, help="config5: query arrivals per second (Poisson)")
     ap.add_argument("--duration", type=float, default=60.0, help="config5: seconds of arrivals")
     ap.add_argument("--isolated", type=int, default=100, help="config5: queries also solved alone, for comparison")
@@ -76,7 +80,7 @@ class ClockSampler:
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
 
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
@@ -115,8 +119,21 @@ class ClockSampler:
         mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({n for r in self.rows for n, v in zip(names, r[5:9]) if v.lower().startswith("active")})
+        util = [float(r[9]) for r in self.rows if len(r) > 9 and r[9].replace(".", "").isdigit()]
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(self.rows),
+                "gpu_util_pct_median": statistics.median(util) if util else None}
+
+
+def host_cpu_times() -> tuple[int, int] | None:
+    """(busy, total) jiffies of all host cores from /proc/stat, or None."""
+    try:
+        with open("/proc/stat") as f:
+            v = [int(x) for x in f.readline().split()[1:]]
+    except (OSError, ValueError):
+        return None
+    idle = v[3] + (v[4] if len(v) > 4 else 0)
+    return sum(v) - idle, sum(v)
 
 
 def dist_setup(backend: str = "nccl"):
@@ -578,7 +595,9 @@ def run_serving(args, world, rank, local, pkg, torch):
         settings = P.PlanSettings()
         planner_desc = "batched bidirectional RRT with connect checks and shortcut passes (this library's compact planner)"
         settings_desc = settings.__dict__
-    server = pkg.Server(budget_bytes=2 << 30, streams=4)
+    streams = args.streams or (S.SERVED_DRRT_STREAMS if args.planner == "drrt" else 4)
+    clients = args.clients or (S.SERVED_DRRT_CLIENTS if args.planner == "drrt" else 256)
+    server = pkg.Server(budget_bytes=2 << 30, streams=streams, fused_edges=args.fused_edges)
     S.isolated(server, queries[:min(3, n)], settings)  # warm-up (first-use set-up of the library)
     m = min(args.isolated, n)
     alone = S.isolated(server, queries[:m], settings)
@@ -586,11 +605,14 @@ def run_serving(args, world, rank, local, pkg, torch):
     barrier(world)
     clocks = ClockSampler(local)
     clocks.start()
+    cpu0 = host_cpu_times()
     t0 = time.perf_counter()
-    served = S.stream(server, queries, args.rate, settings, seed=rank)
+    served = S.stream(server, queries, args.rate, settings, seed=rank, clients=clients)
     wall = time.perf_counter() - t0
+    cpu1 = host_cpu_times()
     clk = clocks.stop()
     after = server.stats()
+    cpu_busy = (cpu1[0] - cpu0[0]) / max(1, cpu1[1] - cpu0[1]) if cpu0 and cpu1 else None
     wall = max_over_ranks(wall, world)
     same = sum(S.same_result(a.result, b.result) for a, b in zip(alone, served[:m]))
     sv, iso = S.summary(served), S.summary(alone)
@@ -605,7 +627,7 @@ def run_serving(args, world, rank, local, pkg, torch):
            "config": {"workload": "config5_served_planning", "rate_qps": args.rate, "duration_s": args.duration,
                       "queries": n, "arms": "2-5 (uniform)", "scenes": "single-arm or bin-picking generator",
                       "planner": planner_desc,
-                      "settings": settings_desc, "service": "mrpop_server: 2 GiB budget, 4 streams",
+                      "settings": settings_desc, "service": f"mrpop_server: 2 GiB budget, {streams} streams, {clients} client threads",
                       "query_generation_s": round(gen_s, 2)},
            "latency": {"served_p50_ms": sv["p50_ms"], "served_p99_ms": sv["p99_ms"],
                        "isolated_p50_ms": iso["p50_ms"], "isolated_p99_ms": iso["p99_ms"],
@@ -614,14 +636,22 @@ def run_serving(args, world, rank, local, pkg, torch):
            "solve_rate": {"served": sv["solve_rate"], "isolated": iso["solve_rate"]},
            "mean_cost": {"served": sv["mean_cost"], "isolated": iso["mean_cost"]},
            "same_result_alone_and_mixed": f"{same}/{m}",
+           "phase_mean_ms": {"served": sv["phase_mean_ms"], "isolated": iso["phase_mean_ms"]},
            "throughput": {"queries_per_s": n / wall, "steps": sv["steps"], "edges": sv["edges"],
                           "edge_samples_per_s_lower_bound": samples / wall,
                           "waves": after["waves"] - before["waves"],
                           "steps_per_wave": (after["steps"] - before["steps"]) / max(1, after["waves"] - before["waves"]),
                           "max_wave_steps": after["max_wave_steps"],
                           "max_waves_in_flight": after["max_waves_in_flight"],
-                          "admission_waits": after["admission_waits"]},
+                          "admission_waits": after["admission_waits"],
+                          "step_queue_mean_us": (after["queue_ns"] - before["queue_ns"]) / 1e3 /
+                          max(1, after["steps"] - before["steps"]),
+                          "step_flight_mean_us": (after["flight_ns"] - before["flight_ns"]) / 1e3 /
+                          max(1, after["steps"] - before["steps"]),
+                          "wave_device_mean_us": (after["device_ns"] - before["device_ns"]) / 1e3 /
+                          max(1, after["waves"] - before["waves"])},
            "gpu_launches": after["kernel_launches"] - before["kernel_launches"],
+           "host_cpu_busy": {"fraction": cpu_busy, "cores": os.cpu_count()},
            "clocks": clk,
            "e2e": {"value": sv["p99_ms"], "unit": "ms", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                    "path": "host wall clock from each query's arrival to its plan; endpoints and verdicts in "

@@ -301,7 +301,8 @@ mrpop_status mrpop_batch_destroy(mrpop_batch *batch);
  * mrpop_server_destroy, which finishes the pending steps and frees the server.
  * A session also reserves page-locked host buffers for its steps in a host
  * arena of host_bytes (mrpop_session_host_buffers).  Zero in a config field
- * selects the default: 1 GiB, 4 streams, 1024 steps, 16384 chunks, 256 MiB.
+ * selects the default: 1 GiB, 4 streams, 1024 steps, 16384 chunks, 256 MiB,
+ * 4096 fused edges.
  */
 typedef struct {
     int64_t budget_bytes;    /* device arena for the sessions' step scratch            */
@@ -309,6 +310,8 @@ typedef struct {
     int32_t max_wave_steps;
     int64_t max_wave_chunks;
     int64_t host_bytes;      /* page-locked host arena for the sessions' buffers       */
+    int64_t fused_edges;     /* groups of at most this many edges in a wave run as one
+                                fused launch instead of the split kernels; -1: never   */
 } mrpop_server_config;
 
 typedef struct {
@@ -323,6 +326,9 @@ typedef struct {
     int64_t max_wave_steps;      /* most steps in one wave                            */
     int64_t max_waves_in_flight; /* most waves on the device at once                  */
     int64_t kernel_launches;     /* validator kernels launched                        */
+    int64_t queue_ns;            /* summed over steps: submit to its wave's launch    */
+    int64_t flight_ns;           /* summed over steps: wave launch to wave done       */
+    int64_t device_ns;           /* summed over waves: first to last command on the GPU */
 } mrpop_server_stats;
 
 typedef struct mrpop_server mrpop_server;
@@ -423,8 +429,10 @@ mrpop_status mrpop_session_plan(mrpop_session *session, const mrpop_scene *scene
  * Settings: the fields of the reference's pop_settings (pop_settings.hh:3-32)
  * in order, bools as int32, then this library's additions.
  * mrpop_drrt_settings_default fills the reference's defaults (and
- * block_per_robot 8, max_launches 20, seed 1234, host_threads 0).  The
- * result does not depend on host_threads.  dd_radius, dd_min_radius,
+ * block_per_robot 8, max_launches 20, seed 1234, host_threads 0,
+ * blocking_wait 0).  The result depends on neither host_threads nor
+ * blocking_wait: they trade one solve's latency against the share of the
+ * host that many concurrent solves leave each other.  dd_radius, dd_min_radius,
  * resample_iter, cost_bound_resample and the perturb fields are carried but
  * read nowhere, as in the reference; dynamic_domain is honoured as the
  * reference computes it (its radii never leave FLT_MAX, so it never prunes).
@@ -483,6 +491,7 @@ typedef struct {
     int32_t max_launches;     /* bound on the first pass's roadmap + rrtc repeats (20)    */
     uint64_t seed;            /* random streams (1234, the reference's curand seed)       */
     int32_t host_threads;     /* host threads for the attempts' work; 0: all (0)          */
+    int32_t blocking_wait;    /* 1: sleep while the call's device work runs; 0: spin (0)  */
 } mrpop_drrt_settings;
 
 typedef struct {
@@ -517,6 +526,13 @@ mrpop_status mrpop_drrt_solve_with(int arms, mrpop_check_fn validate, void *ctx,
                                    const float *goals, int num_goals, const mrpop_drrt_settings *settings,
                                    float *path_out, int64_t max_waypoints, mrpop_drrt_solution_fn on_solution,
                                    void *solution_ctx, mrpop_drrt_result *out);
+/* Device resources of the solves (a stream, the trees' device rows, staging
+ * blocks, roadmap mirrors) are kept in a per-process pool between solves, so
+ * that a stream of solves allocates and frees nothing once warm; at most 64
+ * idle sets are kept.  mrpop_drrt_release_pool frees the idle sets (after
+ * waiting for their streams) and returns how many it freed; sets in use by
+ * running solves are untouched. */
+int64_t mrpop_drrt_release_pool(void);
 /* The same planner with its checks served by a session of the validation
  * service (below): every check becomes steps of at most the session's edge
  * count, co-batched with the steps of the other sessions; the tree searches

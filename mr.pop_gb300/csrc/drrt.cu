@@ -37,6 +37,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <unordered_map>
@@ -144,18 +145,19 @@ struct Roadmap {
 };
 
 // ---------------------------------------------------------------------------
-// Trees: host master copy plus a device copy for the nearest-neighbour kernel.
+// Trees: host master copy plus a device copy for the nearest-neighbour kernel
+// (rows of dim + 1 floats: the configuration, then the node's cost).
 // ---------------------------------------------------------------------------
 struct Tree {
     int dim = 0, arms = 0;
-    std::vector<float> q, cost;
+    std::vector<float> q, cost, rows;
     std::vector<int> parent, rid;  // rid [n][arms]: roadmap vertex of each arm, -1 for connect nodes
     std::unordered_map<uint64_t, std::vector<int>> by_ids;
     std::vector<int> connect_nodes;
-    // device copy
-    float *d_q = nullptr, *d_cost = nullptr;
-    int64_t d_cap = 0, uploaded = 0;
-    bool cost_dirty = false;
+    // device copy: rows [0, dirty_from) are current there
+    float *d_rows = nullptr;
+    size_t d_bytes = 0;
+    int64_t dirty_from = 0;
 
     int64_t size() const { return (int64_t)parent.size(); }
     const float *node(int64_t i) const { return &q[(size_t)i * dim]; }
@@ -170,17 +172,19 @@ struct Tree {
     void clear() {
         q.clear();
         cost.clear();
+        rows.clear();
         parent.clear();
         rid.clear();
         by_ids.clear();
         connect_nodes.clear();
-        uploaded = 0;
-        cost_dirty = false;
+        dirty_from = 0;
     }
     int add(const float *x, int par, float c, const int *ids) {
         const int i = (int)size();
         q.insert(q.end(), x, x + dim);
         cost.push_back(c);
+        rows.insert(rows.end(), x, x + dim);
+        rows.push_back(c);
         parent.push_back(par < 0 ? i : par);
         if (ids) {
             rid.insert(rid.end(), ids, ids + arms);
@@ -190,6 +194,11 @@ struct Tree {
             connect_nodes.push_back(i);
         }
         return i;
+    }
+    void set_cost(int i, float c) {
+        cost[i] = c;
+        rows[(size_t)i * (dim + 1) + dim] = c;
+        dirty_from = std::min<int64_t>(dirty_from, i);
     }
     // An existing node within the reference's 1e-5 squared distance of x
     // (pop_planner.cu:522-528), looked up by roadmap-vertex tuple and among
@@ -203,41 +212,26 @@ struct Tree {
             if (sq_l2(node(i), x, dim) <= kExistSq) return i;
         return -1;
     }
-    void free_device() {
-        if (d_q) cudaFree(d_q);
-        if (d_cost) cudaFree(d_cost);
-        d_q = d_cost = nullptr;
-        d_cap = uploaded = 0;
-    }
+    // One copy of the rows added or re-costed since the last one.
     cudaError_t sync_device(cudaStream_t s) {
         const int64_t n = size();
-        if (n > d_cap) {
-            int64_t cap = std::max<int64_t>(d_cap * 2, 65536);
-            while (cap < n) cap *= 2;
-            float *nq = nullptr, *nc = nullptr;
-            cudaError_t e = cudaMalloc(&nq, (size_t)cap * dim * sizeof(float));
-            if (e == cudaSuccess) e = cudaMalloc(&nc, (size_t)cap * sizeof(float));
-            if (e != cudaSuccess) {
-                cudaFree(nq);
-                return e;
-            }
-            cudaFree(d_q);
-            cudaFree(d_cost);
-            d_q = nq;
-            d_cost = nc;
-            d_cap = cap;
-            uploaded = 0;
-            cost_dirty = false;
+        const size_t row = (size_t)(dim + 1) * sizeof(float);
+        if ((size_t)n * row > d_bytes) {
+            size_t bytes = std::max<size_t>(d_bytes * 2, (size_t)65536 * row);
+            while (bytes < (size_t)n * row) bytes *= 2;
+            float *nr = nullptr;
+            const cudaError_t e = cudaMalloc(&nr, bytes);
+            if (e != cudaSuccess) return e;
+            if (d_rows) cudaFree(d_rows);
+            d_rows = nr;
+            d_bytes = bytes;
+            dirty_from = 0;
         }
         cudaError_t e = cudaSuccess;
-        if (n > uploaded)
-            e = cudaMemcpyAsync(d_q + uploaded * dim, node(uploaded), (size_t)(n - uploaded) * dim * sizeof(float),
-                                cudaMemcpyHostToDevice, s);
-        const int64_t c0 = cost_dirty ? 0 : uploaded;
-        if (e == cudaSuccess && n > c0)
-            e = cudaMemcpyAsync(d_cost + c0, &cost[c0], (size_t)(n - c0) * sizeof(float), cudaMemcpyHostToDevice, s);
-        uploaded = n;
-        cost_dirty = false;
+        if (n > dirty_from)
+            e = cudaMemcpyAsync(d_rows + dirty_from * (dim + 1), &rows[(size_t)dirty_from * (dim + 1)],
+                                (size_t)(n - dirty_from) * (dim + 1) * sizeof(float), cudaMemcpyHostToDevice, s);
+        dirty_from = n;
         return e;
     }
 };
@@ -249,24 +243,38 @@ struct Tree {
 //   mode 1 (connect search): sqrt(distance) < bound (pop_planner.cu:642)
 // One thread per node (held in registers); queries in shared memory.
 // ---------------------------------------------------------------------------
+constexpr int kNNMaxJobs = 8;
+
+// One launch for the query chunks of both trees: job j = (tree, first query,
+// queries); blockIdx.y is the job, blockIdx.x a block of 256 nodes.
+struct NNLaunch {
+    const float *rows[2];  // per tree [n][dim + 1]: configuration, cost
+    long long n[2];
+    const float *qx, *qb;  // every job's queries [.][dim] and bounds [.]
+    unsigned long long *best;
+    int mode;
+    int tree[kNNMaxJobs], q0[kNNMaxJobs], nq[kNNMaxJobs];
+};
+
 template <int DIM>
-__global__ void __launch_bounds__(256) tree_nn_kernel(const float *__restrict__ nodes, const float *__restrict__ cost,
-                                                      long long n, const float *__restrict__ qx,
-                                                      const float *__restrict__ qb, int nq, int mode,
-                                                      unsigned long long *__restrict__ best) {
+__global__ void __launch_bounds__(256) tree_nn_kernel(const __grid_constant__ NNLaunch L) {
     __shared__ float sx[kNNChunk * DIM];
     __shared__ float sb[kNNChunk];
     __shared__ unsigned long long red[8][kNNChunk];
+    const int job = blockIdx.y, t = L.tree[job], nq = L.nq[job];
+    const long long n = L.n[t];
+    if ((long long)blockIdx.x * blockDim.x >= n) return;  // whole block past this tree's nodes
+    const float *qx = L.qx + (size_t)L.q0[job] * DIM, *qb = L.qb + L.q0[job];
     for (int i = threadIdx.x; i < nq * DIM; i += blockDim.x) sx[i] = qx[i];
     for (int i = threadIdx.x; i < nq; i += blockDim.x) sb[i] = qb[i];
     __syncthreads();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool have = i < n;
+    const float *row = L.rows[t] + (size_t)(have ? i : 0) * (DIM + 1);
     float x[DIM];
-    float c = 0.0f;
 #pragma unroll
-    for (int d = 0; d < DIM; d++) x[d] = have ? nodes[i * DIM + d] : 0.0f;
-    if (have && mode == 0) c = cost[i];
+    for (int d = 0; d < DIM; d++) x[d] = have ? row[d] : 0.0f;
+    const float c = have ? row[DIM] : 0.0f;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int q = 0; q < nq; q++) {
         unsigned long long key = ~0ull;
@@ -274,10 +282,10 @@ __global__ void __launch_bounds__(256) tree_nn_kernel(const float *__restrict__ 
             float s = 0.0f;
 #pragma unroll
             for (int d = 0; d < DIM; d++) {
-                const float t = x[d] - sx[q * DIM + d];
-                s = __fmaf_rn(t, t, s);
+                const float u = x[d] - sx[q * DIM + d];
+                s = __fmaf_rn(u, u, s);
             }
-            const bool ok = (mode == 0 ? c < sb[q] : sqrtf(s) < sb[q]) && s < FLT_MAX;
+            const bool ok = (L.mode == 0 ? c < sb[q] : sqrtf(s) < sb[q]) && s < FLT_MAX;
             if (ok) key = ((unsigned long long)__float_as_uint(s) << 32) | (unsigned long long)(unsigned)i;
         }
 #pragma unroll
@@ -288,6 +296,7 @@ __global__ void __launch_bounds__(256) tree_nn_kernel(const float *__restrict__ 
         if (lane == 0) red[warp][q] = key;
     }
     __syncthreads();
+    unsigned long long *best = L.best + L.q0[job];
     for (int q = threadIdx.x; q < nq; q += blockDim.x) {
         unsigned long long k = red[0][q];
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) k = red[w][q] < k ? red[w][q] : k;
@@ -295,16 +304,14 @@ __global__ void __launch_bounds__(256) tree_nn_kernel(const float *__restrict__ 
     }
 }
 
-cudaError_t launch_tree_nn(int dim, const Tree &t, const float *d_qx, const float *d_qb, int nq, int mode,
-                           unsigned long long *d_best, cudaStream_t s) {
-    const long long n = t.size();
-    const unsigned grid = (unsigned)std::max<long long>(1, (n + 255) / 256);
+cudaError_t launch_tree_nn(int dim, const NNLaunch &L, int njobs, long long max_n, cudaStream_t s) {
+    const dim3 grid((unsigned)std::max<long long>(1, (max_n + 255) / 256), (unsigned)njobs);
     switch (dim) {
-        case 7: tree_nn_kernel<7><<<grid, 256, 0, s>>>(t.d_q, t.d_cost, n, d_qx, d_qb, nq, mode, d_best); break;
-        case 14: tree_nn_kernel<14><<<grid, 256, 0, s>>>(t.d_q, t.d_cost, n, d_qx, d_qb, nq, mode, d_best); break;
-        case 21: tree_nn_kernel<21><<<grid, 256, 0, s>>>(t.d_q, t.d_cost, n, d_qx, d_qb, nq, mode, d_best); break;
-        case 28: tree_nn_kernel<28><<<grid, 256, 0, s>>>(t.d_q, t.d_cost, n, d_qx, d_qb, nq, mode, d_best); break;
-        case 35: tree_nn_kernel<35><<<grid, 256, 0, s>>>(t.d_q, t.d_cost, n, d_qx, d_qb, nq, mode, d_best); break;
+        case 7: tree_nn_kernel<7><<<grid, 256, 0, s>>>(L); break;
+        case 14: tree_nn_kernel<14><<<grid, 256, 0, s>>>(L); break;
+        case 21: tree_nn_kernel<21><<<grid, 256, 0, s>>>(L); break;
+        case 28: tree_nn_kernel<28><<<grid, 256, 0, s>>>(L); break;
+        case 35: tree_nn_kernel<35><<<grid, 256, 0, s>>>(L); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -410,6 +417,78 @@ struct GpuChecker {
 };
 
 // ---------------------------------------------------------------------------
+// Device resources of one solve (its stream, the trees' device rows, the
+// nearest-neighbour staging block, the roadmap mirrors and pair buffers).
+// Solves take them from a per-process pool and give them back, so a stream of
+// solves allocates and frees nothing once warm: cudaFree waits for the whole
+// device, and page-locked allocations take milliseconds.
+// ---------------------------------------------------------------------------
+struct DeviceWork {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done_ev = nullptr;
+    float *rows[2] = {nullptr, nullptr};
+    size_t rows_bytes[2] = {0, 0};
+    void *d_stage = nullptr, *h_stage = nullptr;
+    size_t stage_cap = 0;
+    std::vector<float *> d_rm;  // per arm, [cap][7]
+    std::vector<int64_t> d_rm_cap;
+    int2 *d_pairs = nullptr;
+    size_t d_pairs_cap = 0;
+    unsigned int *d_npairs = nullptr, *h_npairs = nullptr;
+
+    void free_all() {
+        if (stream) cudaStreamSynchronize(stream);
+        for (float *&p : rows)
+            if (p) cudaFree(p);
+        if (d_stage) cudaFree(d_stage);
+        if (h_stage) cudaFreeHost(h_stage);
+        for (float *p : d_rm)
+            if (p) cudaFree(p);
+        if (d_pairs) cudaFree(d_pairs);
+        if (d_npairs) cudaFree(d_npairs);
+        if (h_npairs) cudaFreeHost(h_npairs);
+        if (done_ev) cudaEventDestroy(done_ev);
+        if (stream) cudaStreamDestroy(stream);
+        *this = DeviceWork{};
+    }
+};
+
+constexpr size_t kPoolKeep = 64;  // idle sets kept; more are freed on return
+std::mutex g_pool_mu;
+std::vector<DeviceWork> g_pool;
+
+DeviceWork take_work(int device) {
+    {
+        std::lock_guard<std::mutex> lk(g_pool_mu);
+        for (size_t i = g_pool.size(); i-- > 0;)
+            if (g_pool[i].device == device) {
+                DeviceWork w = std::move(g_pool[i]);
+                g_pool.erase(g_pool.begin() + (ptrdiff_t)i);
+                return w;
+            }
+    }
+    DeviceWork w;
+    w.device = device;
+    return w;
+}
+
+void give_work(DeviceWork &&w) {
+    if (w.stream && cudaStreamSynchronize(w.stream) != cudaSuccess) {
+        w.free_all();  // a failed stream is not reused
+        return;
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_pool_mu);
+        if (g_pool.size() < kPoolKeep) {
+            g_pool.push_back(std::move(w));
+            return;
+        }
+    }
+    w.free_all();
+}
+
+// ---------------------------------------------------------------------------
 // The planner.
 // ---------------------------------------------------------------------------
 struct Solver {
@@ -419,8 +498,23 @@ struct Solver {
     mrpop_check_fn validate = nullptr;
     void *vctx = nullptr;
     bool device_nn = false;
+    bool pooled = false;  // device resources taken from the pool (returned by the destructor)
     cudaStream_t stream = nullptr;
     void *d_stage = nullptr, *h_stage = nullptr;  // nearest-neighbour staging block (device, page-locked)
+    cudaEvent_t done_ev = nullptr;  // blocking-sync event (settings.blocking_wait)
+
+    // Waits for the solve's stream: by spinning (the CUDA default), or, with
+    // blocking_wait, asleep on a blocking-sync event, so that many concurrent
+    // solves leave the host's cores to each other.
+    cudaError_t wait_stream() {
+        if (!S.blocking_wait) return cudaStreamSynchronize(stream);
+        if (!done_ev) {
+            const cudaError_t e = cudaEventCreateWithFlags(&done_ev, cudaEventBlockingSync | cudaEventDisableTiming);
+            if (e != cudaSuccess) return e;
+        }
+        const cudaError_t e = cudaEventRecord(done_ev, stream);
+        return e == cudaSuccess ? cudaEventSynchronize(done_ev) : e;
+    }
     mrpop_drrt_result *R = nullptr;
     mrpop_drrt_solution_fn on_solution = nullptr;
     void *sctx = nullptr;
@@ -446,17 +540,57 @@ struct Solver {
     std::vector<uint8_t> ok;
     std::vector<int32_t> fh;
 
+    // Takes a pooled set of device resources (device_nn solves).
+    cudaError_t adopt_device() {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        DeviceWork w = take_work(dev);
+        if (!w.stream) {
+            e = cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking);
+            if (e != cudaSuccess) return e;
+        }
+        stream = w.stream;
+        done_ev = w.done_ev;
+        for (int t = 0; t < 2; t++) {
+            T[t].d_rows = w.rows[t];
+            T[t].d_bytes = w.rows_bytes[t];
+            T[t].dirty_from = 0;
+        }
+        d_stage = w.d_stage;
+        h_stage = w.h_stage;
+        d_cap_q = w.stage_cap;
+        d_rm = std::move(w.d_rm);
+        d_rm_cap = std::move(w.d_rm_cap);
+        d_rm_up.assign(d_rm.size(), 0);
+        d_pairs = w.d_pairs;
+        d_pairs_cap = w.d_pairs_cap;
+        d_npairs = w.d_npairs;
+        h_npairs = w.h_npairs;
+        pooled = true;
+        return cudaSuccess;
+    }
+
     ~Solver() {
-        T[0].free_device();
-        T[1].free_device();
-        if (d_stage) cudaFree(d_stage);
-        if (h_stage) cudaFreeHost(h_stage);
-        for (float *p : d_rm)
-            if (p) cudaFree(p);
-        if (d_pairs) cudaFree(d_pairs);
-        if (d_npairs) cudaFree(d_npairs);
-        if (h_npairs) cudaFreeHost(h_npairs);
-        if (stream) cudaStreamDestroy(stream);
+        if (!pooled) return;
+        DeviceWork w;
+        cudaGetDevice(&w.device);
+        w.stream = stream;
+        w.done_ev = done_ev;
+        for (int t = 0; t < 2; t++) {
+            w.rows[t] = T[t].d_rows;
+            w.rows_bytes[t] = T[t].d_bytes;
+        }
+        w.d_stage = d_stage;
+        w.h_stage = h_stage;
+        w.stage_cap = d_cap_q;
+        w.d_rm = std::move(d_rm);
+        w.d_rm_cap = std::move(d_rm_cap);
+        w.d_pairs = d_pairs;
+        w.d_pairs_cap = d_pairs_cap;
+        w.d_npairs = d_npairs;
+        w.h_npairs = h_npairs;
+        give_work(std::move(w));
     }
 
     int check(int64_t n, int rule, float range, uint32_t flags, int arm, int gran) {
@@ -556,18 +690,38 @@ struct Solver {
         for (int t = 0; t < 2 && e == cudaSuccess; t++)
             if (!jobs[t].bound.empty()) e = T[t].sync_device(stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(d_stage, h_stage, stage_bytes, cudaMemcpyHostToDevice, stream);
+        NNLaunch L{};
+        L.qx = d_qx;
+        L.qb = d_qb;
+        L.best = d_best;
+        L.mode = mode;
+        for (int t = 0; t < 2; t++) {
+            L.rows[t] = T[t].d_rows;
+            L.n[t] = T[t].size();
+        }
+        int njobs = 0;
+        long long max_n = 0;
         off = 0;
         for (int t = 0; t < 2 && e == cudaSuccess; t++) {
             const int nq = (int)jobs[t].bound.size();
-            for (int c0 = 0; c0 < nq && e == cudaSuccess; c0 += kNNChunk)
-                e = launch_tree_nn(dim, T[t], d_qx + (size_t)(off + c0) * dim, d_qb + off + c0,
-                                   std::min(kNNChunk, nq - c0), mode, d_best + off + c0, stream);
+            for (int c0 = 0; c0 < nq && e == cudaSuccess; c0 += kNNChunk) {
+                L.tree[njobs] = t;
+                L.q0[njobs] = off + c0;
+                L.nq[njobs] = std::min(kNNChunk, nq - c0);
+                max_n = std::max<long long>(max_n, L.n[t]);
+                if (++njobs == kNNMaxJobs) {
+                    e = launch_tree_nn(dim, L, njobs, max_n, stream);
+                    njobs = 0;
+                    max_n = 0;
+                }
+            }
             off += nq;
         }
+        if (e == cudaSuccess && njobs) e = launch_tree_nn(dim, L, njobs, max_n, stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(h_best, d_best, (size_t)nq_total * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                 stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e == cudaSuccess) e = wait_stream();
         off = 0;
         for (int t = 0; t < 2 && e == cudaSuccess; t++) {
             const int nq = (int)jobs[t].bound.size();
@@ -616,9 +770,9 @@ struct Solver {
         const int n = M.size();
         cudaError_t e = cudaSuccess;
         if (d_rm.size() < (size_t)arms) {
-            d_rm.assign(arms, nullptr);
-            d_rm_cap.assign(arms, 0);
-            d_rm_up.assign(arms, 0);
+            d_rm.resize(arms, nullptr);
+            d_rm_cap.resize(arms, 0);
+            d_rm_up.resize(arms, 0);
         }
         if (n > d_rm_cap[a]) {
             int64_t cap = std::max<int64_t>(2 * d_rm_cap[a], 16384);
@@ -651,7 +805,7 @@ struct Solver {
                                                            (unsigned int)d_pairs_cap, stream);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(h_npairs, d_npairs, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+            if (e == cudaSuccess) e = wait_stream();
             if (e != cudaSuccess) break;
             const size_t np = *h_npairs;
             if (np > d_pairs_cap) {  // grow and search again
@@ -999,8 +1153,7 @@ struct Solver {
                 Tree &tt = T[tsel[b]];
                 if (ext_exist[b] >= 0) {  // rewire (pop_planner.cu:571-577)
                     tt.parent[ext_exist[b]] = near[b];
-                    tt.cost[ext_exist[b]] = ext_cost[b];
-                    tt.cost_dirty = true;
+                    tt.set_cost(ext_exist[b], ext_cost[b]);
                     continue;
                 }
                 const int ni = tt.add(&ext_cfg[(size_t)b * dim], near[b], ext_cost[b], &ext_ids[(size_t)b * arms]);
@@ -1291,6 +1444,7 @@ extern "C" mrpop_status mrpop_drrt_settings_default(mrpop_drrt_settings *o) {
     o->max_launches = 20;
     o->seed = 1234;
     o->host_threads = 0;
+    o->blocking_wait = 0;
     return MRPOP_OK;
 }
 
@@ -1311,12 +1465,27 @@ mrpop_status drrt_run(int arms, mrpop_check_fn validate, void *ctx, bool device_
     sv.validate = validate;
     sv.vctx = ctx;
     sv.device_nn = device_nn;
-    if (device_nn && cudaStreamCreateWithFlags(&sv.stream, cudaStreamNonBlocking) != cudaSuccess)
-        return fail_status(MRPOP_ERR_CUDA, "drrt: stream");
+    if (device_nn && sv.adopt_device() != cudaSuccess) return fail_status(MRPOP_ERR_CUDA, "drrt: device resources");
     return solve(sv, arms, start, goals, num_goals, settings, path_out, max_waypoints, on_solution, solution_ctx, out);
 }
 
 }  // namespace mrpop
+
+extern "C" int64_t mrpop_drrt_release_pool(void) {
+    std::vector<DeviceWork> idle;
+    {
+        std::lock_guard<std::mutex> lk(g_pool_mu);
+        idle.swap(g_pool);
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    for (auto &w : idle) {
+        cudaSetDevice(w.device);
+        w.free_all();
+    }
+    cudaSetDevice(dev);
+    return (int64_t)idle.size();
+}
 
 extern "C" mrpop_status mrpop_drrt_solve_with(int arms, mrpop_check_fn validate, void *ctx, const float *start,
                                               const float *goals, int num_goals, const mrpop_drrt_settings *settings,

@@ -75,8 +75,13 @@ const void *kernel_fn(KernelKind kind, bool seg) {
 
 template <int A, int SPL>
 const void *batch_fn(int mode, bool seg) {
-    if (!seg) return mode == kBatchNarrow ? (const void *)batch_kernel<A, SPL, kBatchNarrow, false>
-                                          : (const void *)batch_kernel<A, SPL, kBatchBroad, false>;
+    if (!seg) {
+        switch (mode) {
+        case kBatchBroad: return (const void *)batch_kernel<A, SPL, kBatchBroad, false>;
+        case kBatchNarrow: return (const void *)batch_kernel<A, SPL, kBatchNarrow, false>;
+        default: return (const void *)batch_kernel<A, SPL, kBatchFused, false>;
+        }
+    }
     switch (mode) {
     case kBatchBroad: return (const void *)batch_kernel<A, SPL, kBatchBroad, true>;
     case kBatchNarrow: return (const void *)batch_kernel<A, SPL, kBatchNarrow, true>;

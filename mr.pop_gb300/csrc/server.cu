@@ -42,10 +42,12 @@ constexpr int kChunkEdges = 96;    // largest chunk (the batch entry points' chu
 // dozen edges then spreads over several CTAs instead of running through one
 // CTA's warps in turn.
 constexpr int kWaveCtasPerSm = 3;
-// Segmented groups of at most this many edges in a wave run as one fused
-// launch from segment 0 instead of the split rounds (2 launches instead of
-// 2 * kSegRounds + 1: launch latency dominates small waves).
-constexpr int64_t kFusedOnlyEdges = 4096;
+// Groups of at most this many edges in a wave (mrpop_server_config.fused_edges)
+// run as one fused launch -- broad and narrow phase per edge in one warp, from
+// segment 0 -- instead of the split kernels (1 launch instead of 2, or of
+// 2 * kSegRounds + 1 for segmented rules): launch latency and the serial
+// dependency between the split kernels dominate small waves.
+constexpr int64_t kFusedEdgesDefault = 4096;
 // Work counters per group and wave: one per launch (split rounds + fused
 // tail), zeroed together with the parameter upload so that no launch needs a
 // memset of its own.
@@ -54,6 +56,11 @@ constexpr int kGroupKeys = 4 * MRPOP_MAX_ARMS;
 constexpr size_t kAlign = 256;
 
 size_t round_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
+
+int64_t host_ns() {
+    return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
 
 }  // namespace
 
@@ -68,6 +75,7 @@ struct mrpop_server {
         bool seg = false;
         size_t smem = 0;
         int n_chunks = 0;
+        int64_t t_submit = 0;  // host clock, ns
     };
     // A ring slot: stream, device tables (work counters, parameter blocks and
     // chunk lists of one wave) and their page-locked host mirror.
@@ -76,8 +84,10 @@ struct mrpop_server {
         char *d_tab = nullptr;
         char *h_tab = nullptr;
         bool busy = false;
+        int64_t t_launch = 0;  // host clock when the wave was formed, ns
+        cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // before the wave's first command, after its last
+        int64_t device_ns = 0;                     // ev0 to ev1 of the last finished wave
         std::vector<Step> steps;
-        mrpop_server *server = nullptr;
     };
 
     int device = 0;
@@ -93,8 +103,10 @@ struct mrpop_server {
     size_t tab_params_off = 0, tab_chunks_off = 0, tab_bytes = 0;
 
     std::mutex mu;
-    std::condition_variable cv;  // worker: steps pending or a slot freed; waiters: a step done or a block freed
+    std::condition_variable work_cv;  // the worker: a step pending, a slot freed, or stop
+    std::condition_variable room_cv;  // admission: blocks freed
     std::deque<Step> pending;
+    std::atomic<int64_t> n_pending{0};  // pending.size(), read by the dispatcher without the lock
     bool stop = false;
     std::thread worker;
     mrpop_server_stats stats{};
@@ -113,6 +125,7 @@ struct mrpop_session {
     uint8_t *h_valid = nullptr;
     int32_t *h_first = nullptr;
     // guarded by server->mu
+    std::condition_variable done_cv;  // this session's step done
     bool in_flight = false;
     mrpop_status result = MRPOP_OK;
     std::string error;
@@ -162,19 +175,6 @@ bool take_blocks(mrpop_server *s, mrpop_session *ss) {
         return false;
     }
     return true;
-}
-
-// Runs on the CUDA callback thread behind a wave: marks its steps done.
-void CUDART_CB wave_done(void *arg) {
-    auto *slot = static_cast<mrpop_server::Slot *>(arg);
-    mrpop_server *s = slot->server;
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        for (auto &st : slot->steps) st.session->in_flight = false;
-        slot->steps.clear();
-        slot->busy = false;
-    }
-    s->cv.notify_all();
 }
 
 // One kernel of a group of the wave (its counter was zeroed by the wave's
@@ -251,7 +251,8 @@ cudaError_t launch_wave(mrpop_server *s, mrpop_server::Slot &slot) {
         r.nc = nc - r.c0;
     }
     // work counters (zero) and parameter blocks in one copy, chunk lists in another
-    cudaError_t err = cudaMemcpyAsync(d_work, h_work, s->tab_params_off + (size_t)np * sizeof(mrpop::EdgeParams),
+    cudaError_t err = cudaEventRecord(slot.ev0, slot.stream);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(d_work, h_work, s->tab_params_off + (size_t)np * sizeof(mrpop::EdgeParams),
                                       cudaMemcpyHostToDevice, slot.stream);
     if (err == cudaSuccess)
         err = cudaMemcpyAsync(d_chunks, h_chunks, (size_t)nc * sizeof(int4), cudaMemcpyHostToDevice, slot.stream);
@@ -263,7 +264,7 @@ cudaError_t launch_wave(mrpop_server *s, mrpop_server::Slot &slot) {
         unsigned long long *work = d_work + (size_t)kCountersPerGroup * key;
         const mrpop::EdgeParams *items = d_params + r.p0;
         const int4 *chunks = d_chunks + r.c0;
-        if (seg && r.edges <= kFusedOnlyEdges) {
+        if (r.edges <= s->cfg.fused_edges) {
             err = launch_one(s, arms, seg, spl, r.smem, mrpop::kBatchFused, 0, items, chunks, r.nc, work, slot.stream);
             continue;
         }
@@ -282,59 +283,107 @@ cudaError_t launch_wave(mrpop_server *s, mrpop_server::Slot &slot) {
     return err;
 }
 
-// The worker: forms a wave from the pending steps whenever a slot is free.
+// Moves pending steps (FIFO, while the wave's tables have room) into a free
+// slot (caller holds the lock).
+void form_wave(mrpop_server *s, mrpop_server::Slot &slot) {
+    int items = 0;
+    int64_t chunks = 0;
+    while (!s->pending.empty()) {
+        const auto &st = s->pending.front();
+        if (items + 1 > s->cfg.max_wave_steps || chunks + st.n_chunks > s->cfg.max_wave_chunks) break;
+        items++;
+        chunks += st.n_chunks;
+        slot.steps.push_back(st);
+        s->pending.pop_front();
+    }
+    s->n_pending.store((int64_t)s->pending.size(), std::memory_order_relaxed);
+    slot.busy = true;
+    slot.t_launch = host_ns();
+    for (const auto &st : slot.steps) s->stats.queue_ns += slot.t_launch - st.t_submit;
+    s->stats.waves++;
+    s->stats.steps += items;
+    s->stats.max_wave_steps = std::max<int64_t>(s->stats.max_wave_steps, items);
+    int in_flight = 0;
+    for (auto &sl : s->slots) in_flight += sl.busy ? 1 : 0;
+    s->stats.max_waves_in_flight = std::max<int64_t>(s->stats.max_waves_in_flight, in_flight);
+}
+
+// Marks a finished (or failed) wave's steps done and frees its slot (caller
+// holds the lock).
+void retire_wave(mrpop_server *s, mrpop_server::Slot &slot, cudaError_t err) {
+    s->stats.flight_ns += (host_ns() - slot.t_launch) * (int64_t)slot.steps.size();
+    const std::string msg = err == cudaSuccess ? std::string() : std::string("server: wave failed: ") + cudaGetErrorString(err);
+    for (auto &st : slot.steps) {
+        if (err != cudaSuccess) {
+            st.session->result = MRPOP_ERR_CUDA;
+            st.session->error = msg;
+        }
+        st.session->in_flight = false;
+        st.session->done_cv.notify_one();
+    }
+    slot.steps.clear();
+    slot.busy = false;
+}
+
+// The dispatcher: forms a wave from the pending steps whenever a slot is
+// free, and retires each wave when the event after its last command has
+// completed.  While any wave is in flight it polls those events (one host
+// core, completions seen within microseconds); with none in flight and
+// nothing pending it sleeps until a step is submitted.  The slots are this
+// thread's alone; the lock guards the queue, the sessions' flags and the
+// statistics.
 void worker_loop(mrpop_server *s) {
     cudaSetDevice(s->device);
-    std::unique_lock<std::mutex> lk(s->mu);
     for (;;) {
-        mrpop_server::Slot *slot = nullptr;
-        s->cv.wait(lk, [&] {
-            if (s->stop && s->pending.empty()) return true;
-            if (s->pending.empty()) return false;
-            for (auto &sl : s->slots)
-                if (!sl.busy) {
-                    slot = &sl;
-                    return true;
-                }
-            return false;
-        });
-        if (!slot) break;  // stopping with nothing pending
-        // FIFO: take steps while the wave's tables have room
-        int items = 0;
-        int64_t chunks = 0;
-        while (!s->pending.empty()) {
-            const auto &st = s->pending.front();
-            if (items + 1 > s->cfg.max_wave_steps || chunks + st.n_chunks > s->cfg.max_wave_chunks) break;
-            items++;
-            chunks += st.n_chunks;
-            slot->steps.push_back(st);
-            s->pending.pop_front();
-        }
-        slot->busy = true;
-        s->stats.waves++;
-        s->stats.steps += items;
-        s->stats.max_wave_steps = std::max<int64_t>(s->stats.max_wave_steps, items);
-        int in_flight = 0;
-        for (auto &sl : s->slots) in_flight += sl.busy ? 1 : 0;
-        s->stats.max_waves_in_flight = std::max<int64_t>(s->stats.max_waves_in_flight, in_flight);
-        lk.unlock();
-        cudaError_t err = launch_wave(s, *slot);
-        if (err == cudaSuccess) err = cudaLaunchHostFunc(slot->stream, wave_done, slot);
-        lk.lock();
-        if (err != cudaSuccess) {
-            // the wave's launches are not all enqueued: wait for what was, then fail its steps
-            lk.unlock();
-            cudaStreamSynchronize(slot->stream);
-            lk.lock();
-            const std::string msg = std::string("server: wave launch failed: ") + cudaGetErrorString(err);
-            for (auto &st : slot->steps) {
-                st.session->result = MRPOP_ERR_CUDA;
-                st.session->error = msg;
-                st.session->in_flight = false;
+        // poll the waves in flight, without the lock
+        bool any_busy = false, any_free = false;
+        mrpop_server::Slot *done[64];
+        cudaError_t done_err[64];
+        int n_done = 0;
+        for (auto &sl : s->slots) {
+            if (!sl.busy) {
+                any_free = true;
+                continue;
             }
-            slot->steps.clear();
-            slot->busy = false;
-            s->cv.notify_all();
+            const cudaError_t q = cudaEventQuery(sl.ev1);
+            if (q == cudaErrorNotReady) {
+                any_busy = true;
+                continue;
+            }
+            float ms = 0.0f;
+            if (q == cudaSuccess && cudaEventElapsedTime(&ms, sl.ev0, sl.ev1) == cudaSuccess)
+                sl.device_ns = (int64_t)(ms * 1e6);
+            done[n_done] = &sl;
+            done_err[n_done++] = q;
+            any_free = true;
+        }
+        const bool launchable = any_free && s->n_pending.load(std::memory_order_relaxed) > 0;
+        if (!n_done && !launchable) {
+            if (any_busy) {
+                std::this_thread::yield();
+                continue;
+            }
+            std::unique_lock<std::mutex> lk(s->mu);
+            if (s->stop && s->pending.empty()) break;
+            s->work_cv.wait(lk, [&] { return s->stop || !s->pending.empty(); });
+            continue;
+        }
+        std::unique_lock<std::mutex> lk(s->mu);
+        for (int i = 0; i < n_done; i++) {
+            s->stats.device_ns += done[i]->device_ns;
+            retire_wave(s, *done[i], done_err[i]);
+        }
+        // launch: one wave per free slot while steps are pending
+        for (auto &sl : s->slots) {
+            if (s->pending.empty()) break;
+            if (sl.busy) continue;
+            form_wave(s, sl);
+            lk.unlock();
+            cudaError_t err = launch_wave(s, sl);
+            if (err == cudaSuccess) err = cudaEventRecord(sl.ev1, sl.stream);
+            if (err != cudaSuccess) cudaStreamSynchronize(sl.stream);  // what was enqueued, before failing the steps
+            lk.lock();
+            if (err != cudaSuccess) retire_wave(s, sl, err);
         }
     }
 }
@@ -345,7 +394,7 @@ void destroy_server(mrpop_server *s) {
             std::lock_guard<std::mutex> lk(s->mu);
             s->stop = true;
         }
-        s->cv.notify_all();
+        s->work_cv.notify_all();
         s->worker.join();
     }
     for (auto &sl : s->slots) {
@@ -353,6 +402,8 @@ void destroy_server(mrpop_server *s) {
             cudaStreamSynchronize(sl.stream);
             cudaStreamDestroy(sl.stream);
         }
+        if (sl.ev0) cudaEventDestroy(sl.ev0);
+        if (sl.ev1) cudaEventDestroy(sl.ev1);
         cudaFree(sl.d_tab);
         cudaFreeHost(sl.h_tab);
     }
@@ -375,6 +426,7 @@ mrpop_status mrpop_server_create(const mrpop_server_config *cfg, mrpop_server **
     if (c.max_wave_steps <= 0) c.max_wave_steps = 1024;
     if (c.max_wave_chunks <= 0) c.max_wave_chunks = 16384;
     if (c.host_bytes <= 0) c.host_bytes = (int64_t)256 << 20;
+    if (c.fused_edges == 0) c.fused_edges = kFusedEdgesDefault;
     if (c.streams > 16 || c.max_wave_steps > (1 << 20) || c.max_wave_chunks > (1 << 24))
         return fail(MRPOP_ERR_INVALID_ARGUMENT, "server_create: streams <= 16, max_wave_steps <= 2^20, "
                                                 "max_wave_chunks <= 2^24");
@@ -404,8 +456,9 @@ mrpop_status mrpop_server_create(const mrpop_server_config *cfg, mrpop_server **
     s->tab_bytes = round_up(s->tab_chunks_off + (size_t)c.max_wave_chunks * sizeof(int4));
     s->slots.resize(c.streams);
     for (auto &sl : s->slots) {
-        sl.server = s;
         if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        if (err == cudaSuccess) err = cudaEventCreate(&sl.ev0);
+        if (err == cudaSuccess) err = cudaEventCreate(&sl.ev1);
         if (err == cudaSuccess) err = cudaMalloc(&sl.d_tab, s->tab_bytes);
         if (err == cudaSuccess) err = cudaHostAlloc(&sl.h_tab, s->tab_bytes, cudaHostAllocDefault);
         sl.steps.reserve(c.max_wave_steps);
@@ -463,10 +516,10 @@ mrpop_status mrpop_session_open(mrpop_server *s, int arms, int64_t max_edges, in
         bool ok = false;
         const auto fits = [&] { return take_blocks(s, ss); };
         if (timeout_ms < 0) {
-            s->cv.wait(lk, fits);
+            s->room_cv.wait(lk, fits);
             ok = true;
         } else if (timeout_ms > 0) {
-            ok = s->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), fits);
+            ok = s->room_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), fits);
         }
         if (!ok) {
             s->stats.admission_timeouts++;
@@ -511,9 +564,11 @@ mrpop_status mrpop_session_submit(mrpop_session *ss, const mrpop_batch_item *it)
         ss->error.clear();
         if (it->n_edges == 0) return MRPOP_OK;
         ss->in_flight = true;
+        st.t_submit = host_ns();
         s->pending.push_back(st);
+        s->n_pending.store((int64_t)s->pending.size(), std::memory_order_relaxed);
     }
-    s->cv.notify_all();
+    s->work_cv.notify_one();
     return MRPOP_OK;
 }
 
@@ -522,8 +577,8 @@ mrpop_status mrpop_session_wait(mrpop_session *ss, int64_t timeout_ms) {
     mrpop_server *s = ss->server;
     std::unique_lock<std::mutex> lk(s->mu);
     if (timeout_ms < 0) {
-        s->cv.wait(lk, [&] { return !ss->in_flight; });
-    } else if (!s->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return !ss->in_flight; })) {
+        ss->done_cv.wait(lk, [&] { return !ss->in_flight; });
+    } else if (!ss->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return !ss->in_flight; })) {
         return fail(MRPOP_ERR_DEVICE_TIMEOUT, "session_wait: the step is still running");
     }
     if (ss->result != MRPOP_OK) return fail(ss->result, ss->error);
@@ -535,11 +590,11 @@ mrpop_status mrpop_session_close(mrpop_session *ss) {
     mrpop_server *s = ss->server;
     {
         std::unique_lock<std::mutex> lk(s->mu);
-        s->cv.wait(lk, [&] { return !ss->in_flight; });
+        ss->done_cv.wait(lk, [&] { return !ss->in_flight; });
         arena_give(s->free_blocks, s->in_use, ss->offset, ss->bytes);
         arena_give(s->free_host, s->host_in_use, ss->host_off, ss->host_bytes);
     }
-    s->cv.notify_all();
+    s->room_cv.notify_all();
     delete ss;
     return MRPOP_OK;
 }

@@ -152,6 +152,12 @@ def solve_with(arms: int, validate, start, goals, st: M.DrrtSettingsC | None = N
     return _finish(r, sols, dof, arms)
 
 
+def release_pool(lib=None) -> int:
+    """Frees the idle pooled device resources of past solves (mrpop_drrt_release_pool);
+    returns how many sets were freed."""
+    return int((lib or M.library()).mrpop_drrt_release_pool())
+
+
 def path_cost(path: np.ndarray) -> float:
     """Sum of composite Euclidean segment lengths, in float32 as the reference sums them."""
     c = np.float32(0.0)

@@ -35,7 +35,7 @@ EXPORTED = [
     "mrpop_server_get_stats", "mrpop_session_open", "mrpop_session_submit", "mrpop_session_wait",
     "mrpop_session_close", "mrpop_session_host_buffers", "mrpop_plan", "mrpop_session_plan",
     "mrpop_drrt_settings_default", "mrpop_drrt_solve", "mrpop_drrt_solve_with", "mrpop_session_drrt",
-    "mrpop_batch_shapes", "mrpop_batch_set_shape",
+    "mrpop_batch_shapes", "mrpop_batch_set_shape", "mrpop_drrt_release_pool",
 ]
 KERNEL_KINDS = ("fused", "broad", "narrow")
 NOALLOC_MAX_EDGES = 16384
@@ -68,7 +68,7 @@ class BatchItem(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("budget_bytes", C.c_int64), ("streams", C.c_int32), ("max_wave_steps", C.c_int32),
-                ("max_wave_chunks", C.c_int64), ("host_bytes", C.c_int64)]
+                ("max_wave_chunks", C.c_int64), ("host_bytes", C.c_int64), ("fused_edges", C.c_int64)]
 
 
 class PlanSettingsC(C.Structure):
@@ -97,7 +97,8 @@ class DrrtSettingsC(C.Structure):
                 ("cost_bound_resample", C.c_int32), ("path_simplify", C.c_int32), ("phs", C.c_int32),
                 ("simplify_round", C.c_int32), ("bspline_step", C.c_int32), ("bspline_min_change", C.c_float),
                 ("perturb_step", C.c_int32), ("perturb_empty_step", C.c_int32), ("block_per_robot", C.c_int32),
-                ("max_launches", C.c_int32), ("seed", C.c_uint64), ("host_threads", C.c_int32)]
+                ("max_launches", C.c_int32), ("seed", C.c_uint64), ("host_threads", C.c_int32),
+                ("blocking_wait", C.c_int32)]
 
 
 class DrrtResultC(C.Structure):
@@ -118,7 +119,8 @@ SOLUTION_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int32, C.c_float, C.c_void_p, C.
 class ServerStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "budget_bytes", "bytes_in_use", "peak_bytes_in_use", "sessions", "admission_waits", "admission_timeouts",
-        "waves", "steps", "max_wave_steps", "max_waves_in_flight", "kernel_launches")]
+        "waves", "steps", "max_wave_steps", "max_waves_in_flight", "kernel_launches", "queue_ns", "flight_ns",
+        "device_ns")]
 
 
 _LIBS: dict[str, C.CDLL] = {}
@@ -185,6 +187,8 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = C.c_int
+    lib.mrpop_drrt_release_pool.argtypes = []
+    lib.mrpop_drrt_release_pool.restype = C.c_int64
     lib.mrpop_last_error.restype = C.c_char_p
     lib.mrpop_last_error.argtypes = []
     lib.mrpop_version.restype = C.c_char_p
@@ -498,9 +502,10 @@ class Server:
     admitted against a fixed device-memory budget and their steps co-batched."""
 
     def __init__(self, budget_bytes: int = 1 << 30, streams: int = 4, max_wave_steps: int = 1024,
-                 max_wave_chunks: int = 16384, host_bytes: int = 256 << 20, lib: C.CDLL | None = None):
+                 max_wave_chunks: int = 16384, host_bytes: int = 256 << 20, fused_edges: int = 0,
+                 lib: C.CDLL | None = None):
         self.lib = lib or library()
-        cfg = ServerConfig(budget_bytes, streams, max_wave_steps, max_wave_chunks, host_bytes)
+        cfg = ServerConfig(budget_bytes, streams, max_wave_steps, max_wave_chunks, host_bytes, fused_edges)
         h = C.c_void_p()
         _check(self.lib, self.lib.mrpop_server_create(C.byref(cfg), C.byref(h)))
         self.handle = h

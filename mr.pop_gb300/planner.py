@@ -64,6 +64,7 @@ class PlanResult:
     start_tree: int = 0
     goal_tree: int = 0
     validate_ns: int = 0
+    phases_ns: dict | None = None  # planner phases (dRRT: wall, validate, nn, roadmap, oracle)
 
 
 def result_from_c(qid: int, r: M.PlanResultC, path: np.ndarray) -> PlanResult:

@@ -38,18 +38,25 @@ class Served:
 DRRT_STEP_EDGES = 4096  # a dRRT session's step size: larger checks are cut into steps of this many edges
 
 
+# The service shape for dRRT clients: wave slots (CUDA streams) and client
+# threads.  Each dRRT query issues a short device call per tree search, so a
+# few clients per slot keep the GPU fed without the host's cores spinning.
+SERVED_DRRT_STREAMS = 8
+SERVED_DRRT_CLIENTS = 16
+
+
 def served_drrt_settings(**overrides):
     """dRRT / AO-x settings of the served stream: the first pass plus five
     optimising passes (rrtc_iter 6), as the served workload asks, each pass
-    capped at 25 iterations of 64 attempts and the roadmaps grown by 2 blocks
-    per arm -- a budget scaled down from the reference's 100k iterations per
-    pass so that 200 queries/s fit on one GPU and the host's cores.  Each
-    query's host work runs on its own client thread (host_threads 1): the
-    concurrency comes from the queries."""
+    capped at 12 iterations of 64 attempts and the roadmaps grown by 4 blocks
+    per arm for at most 8 rounds -- a budget scaled down from the reference's
+    100k iterations per pass so that 200 queries/s fit on one GPU and the
+    host's cores.  Each query's host work runs on its own client thread
+    (host_threads 1), which sleeps while its device work runs (blocking_wait):
+    the concurrency comes from the queries."""
     from . import drrt
-    base = dict(num_new_configs=64, granularity=32, range=1.5, rrtc_iter=6, max_iters=25, block_per_robot=2,
-                max_launches=4, host_threads=1)
-    base.update(overrides)
+    base = dict(num_new_configs=64, granularity=32, range=1.5, rrtc_iter=6, max_iters=12, block_per_robot=4,
+                max_launches=8, host_threads=1, blocking_wait=1)
     return drrt.settings(**base)
 
 
@@ -61,7 +68,8 @@ def drrt_result(qid: int, r) -> PlanResult:
                    s["start_tree_size"], s["goal_tree_size"]))
     return PlanResult(qid, r.solved, r.path, r.cost if r.solved else float("inf"), int(s["iterations"]),
                       int(s["validate_calls"]), int(s["edges_validated"]), digest, int(s["start_tree_size"]),
-                      int(s["goal_tree_size"]), int(s["validate_ns"]))
+                      int(s["goal_tree_size"]), int(s["validate_ns"]),
+                      {k: int(s[k + "_ns"]) for k in ("wall", "validate", "nn", "roadmap", "oracle")})
 
 
 def run_query(server: M.Server, q: Query, settings, flags: int = M.CHECK_ENV | M.CHECK_SELF,
@@ -147,7 +155,21 @@ def summary(served: list[Served]) -> dict:
         "mean_cost": float(np.mean([s.result.cost for s in solved])) if solved else None,
         "steps": int(sum(s.result.steps for s in served)),
         "edges": int(sum(s.result.edges for s in served)),
+        "phase_mean_ms": phase_means(served),
     }
+
+
+def phase_means(served: list[Served]) -> dict | None:
+    """Mean milliseconds per query in each planner phase (dRRT clients):
+    validation (queueing and device time of the checks), nearest-neighbour
+    searches, roadmap pair searches, the direction oracle, and the rest of the
+    host work ("other" = wall minus those)."""
+    ph = [s.result.phases_ns for s in served if s.result.phases_ns]
+    if not ph:
+        return None
+    out = {k: float(np.mean([p[k] for p in ph])) / 1e6 for k in ("wall", "validate", "nn", "roadmap", "oracle")}
+    out["other"] = out["wall"] - out["validate"] - out["nn"] - out["roadmap"] - out["oracle"]
+    return {k: round(v, 3) for k, v in out.items()}
 
 
 def same_result(a: PlanResult, b: PlanResult) -> bool:

@@ -72,3 +72,42 @@ def test_reference_problems_with_the_drivers_settings(cuda, pkg):
         print(f"drrt arms={arms} problem={prob} solved={r.solved} cost={r.cost:.4f} "
               f"wall_ms={r.stats['wall_ns'] / 1e6:.1f} iterations={r.stats['iterations']} "
               f"validate_calls={r.stats['validate_calls']} edges={r.stats['edges_validated']}")
+
+
+def test_blocking_wait_and_host_threads_do_not_change_the_solve(cuda, pkg):
+    """blocking_wait (sleep on a blocking-sync event instead of spinning) and
+    host_threads change only how the host waits and splits its work."""
+    z = _fixture()
+    bases = z["a4_bases"]
+    scene = pkg.Scene(pkg.SceneArrays(cuboids=z["a4_p1_boxes"]))
+    rb = pkg.RobotSet(4, bases)
+    start, goal = z["a4_p1_start"], z["a4_p1_goal"]
+    kw = dict(num_new_configs=64, granularity=32, range=1.5, rrtc_iter=3, max_iters=12, block_per_robot=4,
+              max_launches=8)
+    a = pkg.drrt.solve(scene, rb, start, goal, pkg.drrt.settings(**kw))
+    b = pkg.drrt.solve(scene, rb, start, goal, pkg.drrt.settings(**kw, blocking_wait=1, host_threads=1))
+    assert scene.status() == 0
+    assert a.solved == b.solved and a.cost == b.cost and np.array_equal(a.path, b.path)
+    for k in ("iterations", "validate_calls", "edges_validated", "roadmap_nodes", "roadmap_edges",
+              "start_tree_size", "goal_tree_size"):
+        assert a.stats[k] == b.stats[k], k
+
+
+def test_pooled_device_resources_are_reused_and_released(cuda, pkg):
+    """Solves take their device resources from a pool and give them back:
+    back-to-back solves leave one idle set, releasing frees it, and a solve
+    after the release (on fresh resources) gives the same result."""
+    z = _fixture()
+    scene = pkg.Scene(pkg.SceneArrays(cuboids=z["a4_p0_boxes"]))
+    rb = pkg.RobotSet(4, z["a4_bases"])
+    st = pkg.drrt.settings(num_new_configs=48, granularity=16, range=2.0, rrtc_iter=2, max_iters=20,
+                           block_per_robot=2, max_launches=4)
+    pkg.drrt.release_pool(scene.lib)
+    a = pkg.drrt.solve(scene, rb, z["a4_p0_start"], z["a4_p0_goal"], st)
+    b = pkg.drrt.solve(scene, rb, z["a4_p0_start"], z["a4_p0_goal"], st)
+    assert pkg.drrt.release_pool(scene.lib) == 1
+    assert pkg.drrt.release_pool(scene.lib) == 0
+    c = pkg.drrt.solve(scene, rb, z["a4_p0_start"], z["a4_p0_goal"], st)
+    assert scene.status() == 0
+    for r in (b, c):
+        assert r.solved == a.solved and r.cost == a.cost and np.array_equal(r.path, a.path)

@@ -17,11 +17,15 @@ def _direct(pkg, cuda, scene, rb, q0, q1, g, flags, arm, rule, range_):
     return out[0].cpu().numpy(), out[1].cpu().numpy()
 
 
-def test_steps_equal_direct_calls(cuda, pkg):
+@pytest.mark.parametrize("fused_edges", [-1, 0, 1 << 40], ids=["split", "default", "fused"])
+def test_steps_equal_direct_calls(cuda, pkg, fused_edges):
+    """Waves run each group split (broad + narrow kernels), fused (one kernel
+    per group) or by the default size rule: every form gives the direct calls'
+    verdicts."""
     W = pkg.workloads
     insts = W.config4_instances(n_instances=16, seed=3, scale=0.05)
     rules = [(pkg.RULE_PLAIN, 0.0), (pkg.RULE_CONNECT, 0.6), (pkg.RULE_BSPLINE, 0.5), (pkg.RULE_SHORTCUT, 0.7)]
-    server = pkg.Server(budget_bytes=512 << 20, streams=3)
+    server = pkg.Server(budget_bytes=512 << 20, streams=3, fused_edges=fused_edges)
     jobs, arms = [], []
     for k, wl in enumerate(insts):
         scene = pkg.Scene(wl.scene)
