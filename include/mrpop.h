@@ -340,6 +340,13 @@ mrpop_status mrpop_server_get_stats(mrpop_server *server, mrpop_server_stats *ou
 mrpop_status mrpop_session_open(mrpop_server *server, int arms, int64_t max_edges, int max_granularity,
                                 int64_t timeout_ms, mrpop_session **out);
 mrpop_status mrpop_session_submit(mrpop_session *session, const mrpop_batch_item *step);
+/* Several steps submitted together (at most MRPOP_SESSION_MAX_ITEMS, their
+ * edge counts summing to at most the session's max_edges): they enter the
+ * pending queue together, so they normally share one wave, and
+ * mrpop_session_wait returns when all are done.  Each item keeps its own
+ * arm count (at most the session's), granularity and rule. */
+#define MRPOP_SESSION_MAX_ITEMS 16
+mrpop_status mrpop_session_submit_many(mrpop_session *session, const mrpop_batch_item *steps, int n_steps);
 mrpop_status mrpop_session_wait(mrpop_session *session, int64_t timeout_ms);
 mrpop_status mrpop_session_close(mrpop_session *session);
 /* The session's page-locked host buffers for its steps, carved from the host
@@ -459,6 +466,20 @@ mrpop_status mrpop_session_plan(mrpop_session *session, const mrpop_scene *scene
  */
 typedef int (*mrpop_check_fn)(void *ctx, const float *q0, const float *q1, int64_t n_edges, int granularity,
                               int rule, float range, uint32_t flags, int arm, uint8_t *valid, int32_t *first_hit);
+/* One check of a group handed to a validator at once (the planner's roadmap
+ * rounds check every arm's nodes, then every arm's edges, as one group). */
+typedef struct {
+    const float *q0;
+    const float *q1;
+    int64_t n_edges;
+    int32_t granularity;
+    int32_t rule;
+    float range;
+    uint32_t flags;
+    int32_t arm;
+    uint8_t *valid;
+    int32_t *first_hit;
+} mrpop_check_call;
 typedef void (*mrpop_drrt_solution_fn)(void *ctx, int32_t pass, float cost, const float *path, int64_t n_waypoints,
                                        const float *raw_path, int64_t n_raw);
 

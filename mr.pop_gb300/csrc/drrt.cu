@@ -496,6 +496,7 @@ struct Solver {
     int arms = 0, dim = 0, g = 0, num_goals = 0;
     int nthreads = 1;  // OpenMP threads of the host work
     mrpop_check_fn validate = nullptr;
+    mrpop::check_many_fn validate_many = nullptr;  // optional: a group of checks in one call
     void *vctx = nullptr;
     bool device_nn = false;
     bool pooled = false;  // device resources taken from the pool (returned by the destructor)
@@ -603,6 +604,46 @@ struct Solver {
         R->validate_calls++;
         R->edges_validated += n;
         return rc;
+    }
+
+    // A group of checks (calls with no edges are dropped): one call of
+    // validate_many when the validator has it, else one validate call each.
+    int check_many(std::vector<mrpop_check_call> &calls) {
+        calls.erase(std::remove_if(calls.begin(), calls.end(), [](const mrpop_check_call &c) { return c.n_edges == 0; }),
+                    calls.end());
+        if (calls.empty()) return 0;
+        const auto t0 = Clock::now();
+        int rc = 0;
+        if (validate_many) {
+            rc = validate_many(vctx, calls.data(), (int)calls.size());
+        } else {
+            for (const auto &c : calls) {
+                rc = validate(vctx, c.q0, c.q1, c.n_edges, c.granularity, c.rule, c.range, c.flags, c.arm, c.valid,
+                              c.first_hit);
+                if (rc) break;
+            }
+        }
+        R->validate_ns += ns_since(t0);
+        for (const auto &c : calls) {
+            R->validate_calls++;
+            R->edges_validated += c.n_edges;
+        }
+        return rc;
+    }
+    static mrpop_check_call plain_call(const float *q0, const float *q1, int64_t n, int g, int arm, uint8_t *valid,
+                                       int32_t *first_hit) {
+        mrpop_check_call c{};
+        c.q0 = q0;
+        c.q1 = q1;
+        c.n_edges = n;
+        c.granularity = g;
+        c.rule = MRPOP_RULE_PLAIN;
+        c.range = 0.0f;
+        c.flags = MRPOP_CHECK_ENV | MRPOP_CHECK_SELF;
+        c.arm = arm;
+        c.valid = valid;
+        c.first_hit = first_hit;
+        return c;
     }
 
     // ---- nearest neighbours ------------------------------------------------
@@ -754,75 +795,86 @@ struct Solver {
         return false;
     }
 
-    // One round: `blocks[a]` blocks of 230 samples grow arm a's roadmap.
-    // Roadmap neighbour pairs on the device: the arm's nodes [0, n) mirrored
+    // Roadmap neighbour pairs on the device: each arm's nodes [0, n) mirrored
     // in device memory, every (i, j) with n_old <= j, i < j and the reference's
-    // distance below `range` found by roadmap_pairs_kernel, then sorted by (j, i)
-    // -- the host loop's order, so both paths give the same edges.
+    // distance below `range` found by roadmap_pairs_kernel -- one launch per
+    // arm, one read-back of the counts for all arms -- then sorted by (j, i),
+    // the host loop's order, so both paths give the same edges.
     std::vector<float *> d_rm;
     std::vector<int64_t> d_rm_cap, d_rm_up;
-    int2 *d_pairs = nullptr;
-    unsigned int *d_npairs = nullptr, *h_npairs = nullptr;
+    int2 *d_pairs = nullptr;     // MRPOP_MAX_ARMS regions of d_pairs_cap pairs
+    unsigned int *d_npairs = nullptr, *h_npairs = nullptr;  // MRPOP_MAX_ARMS counters
     size_t d_pairs_cap = 0;
 
-    int roadmap_pairs_device(int a, int n_old, std::vector<int> &ea, std::vector<int> &eb) {
-        const Roadmap &M = rm[a];
-        const int n = M.size();
+    int roadmap_pairs_device(const std::vector<int> &n_old, std::vector<std::vector<int>> &ea,
+                             std::vector<std::vector<int>> &eb) {
         cudaError_t e = cudaSuccess;
         if (d_rm.size() < (size_t)arms) {
             d_rm.resize(arms, nullptr);
             d_rm_cap.resize(arms, 0);
             d_rm_up.resize(arms, 0);
         }
-        if (n > d_rm_cap[a]) {
-            int64_t cap = std::max<int64_t>(2 * d_rm_cap[a], 16384);
-            while (cap < n) cap *= 2;
-            float *p = nullptr;
-            e = cudaMalloc(&p, (size_t)cap * 7 * sizeof(float));
-            if (e != cudaSuccess) return fail_cuda(e, "roadmap mirror");
-            if (d_rm[a]) cudaFree(d_rm[a]);
-            d_rm[a] = p;
-            d_rm_cap[a] = cap;
-            d_rm_up[a] = 0;
+        for (int a = 0; a < arms && e == cudaSuccess; a++) {
+            const Roadmap &M = rm[a];
+            const int n = M.size();
+            if (n > d_rm_cap[a]) {
+                int64_t cap = std::max<int64_t>(2 * d_rm_cap[a], 16384);
+                while (cap < n) cap *= 2;
+                float *p = nullptr;
+                e = cudaMalloc(&p, (size_t)cap * 7 * sizeof(float));
+                if (e != cudaSuccess) break;
+                if (d_rm[a]) cudaFree(d_rm[a]);
+                d_rm[a] = p;
+                d_rm_cap[a] = cap;
+                d_rm_up[a] = 0;
+            }
+            if (n > d_rm_up[a])
+                e = cudaMemcpyAsync(d_rm[a] + d_rm_up[a] * 7, M.node((int)d_rm_up[a]),
+                                    (size_t)(n - d_rm_up[a]) * 7 * sizeof(float), cudaMemcpyHostToDevice, stream);
+            d_rm_up[a] = n;
         }
-        if (n > d_rm_up[a])
-            e = cudaMemcpyAsync(d_rm[a] + d_rm_up[a] * 7, M.node((int)d_rm_up[a]),
-                                (size_t)(n - d_rm_up[a]) * 7 * sizeof(float), cudaMemcpyHostToDevice, stream);
-        d_rm_up[a] = n;
-        if (!d_npairs) {
-            if (e == cudaSuccess) e = cudaMalloc(&d_npairs, sizeof(unsigned int));
-            if (e == cudaSuccess) e = cudaHostAlloc(&h_npairs, sizeof(unsigned int), cudaHostAllocDefault);
+        if (e == cudaSuccess && !d_npairs) {
+            e = cudaMalloc(&d_npairs, MRPOP_MAX_ARMS * sizeof(unsigned int));
+            if (e == cudaSuccess) e = cudaHostAlloc(&h_npairs, MRPOP_MAX_ARMS * sizeof(unsigned int), cudaHostAllocDefault);
         }
-        const int n_new = n - n_old;
-        for (int attempt = 0; attempt < 2 && e == cudaSuccess && n_new > 0; attempt++) {
+        for (int attempt = 0; attempt < 2 && e == cudaSuccess; attempt++) {
             if (!d_pairs) {
-                d_pairs_cap = std::max<size_t>(d_pairs_cap, (size_t)1 << 20);
-                e = cudaMalloc(&d_pairs, d_pairs_cap * sizeof(int2));
+                d_pairs_cap = std::max<size_t>(d_pairs_cap, (size_t)1 << 18);
+                e = cudaMalloc(&d_pairs, (size_t)MRPOP_MAX_ARMS * d_pairs_cap * sizeof(int2));
                 if (e != cudaSuccess) break;
             }
-            e = cudaMemsetAsync(d_npairs, 0, sizeof(unsigned int), stream);
-            if (e == cudaSuccess) e = launch_roadmap_pairs(d_rm[a], n_old, n, S.range, d_pairs, d_npairs,
-                                                           (unsigned int)d_pairs_cap, stream);
+            e = cudaMemsetAsync(d_npairs, 0, MRPOP_MAX_ARMS * sizeof(unsigned int), stream);
+            for (int a = 0; a < arms && e == cudaSuccess; a++)
+                if (rm[a].size() > n_old[a])
+                    e = launch_roadmap_pairs(d_rm[a], n_old[a], rm[a].size(), S.range, d_pairs + (size_t)a * d_pairs_cap,
+                                             d_npairs + a, (unsigned int)d_pairs_cap, stream);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(h_npairs, d_npairs, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream);
+                e = cudaMemcpyAsync(h_npairs, d_npairs, MRPOP_MAX_ARMS * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                    stream);
             if (e == cudaSuccess) e = wait_stream();
             if (e != cudaSuccess) break;
-            const size_t np = *h_npairs;
-            if (np > d_pairs_cap) {  // grow and search again
+            size_t most = 0;
+            for (int a = 0; a < arms; a++) most = std::max<size_t>(most, h_npairs[a]);
+            if (most > d_pairs_cap) {  // grow and search again
                 cudaFree(d_pairs);
                 d_pairs = nullptr;
-                d_pairs_cap = np + (np >> 2);
+                d_pairs_cap = most + (most >> 2);
                 continue;
             }
-            std::vector<int2> pairs(np);
-            if (np) e = cudaMemcpy(pairs.data(), d_pairs, np * sizeof(int2), cudaMemcpyDeviceToHost);
-            std::sort(pairs.begin(), pairs.end(),
-                      [](const int2 &p, const int2 &q) { return p.y != q.y ? p.y < q.y : p.x < q.x; });
-            ea.resize(np);
-            eb.resize(np);
-            for (size_t k = 0; k < np; k++) {
-                ea[k] = pairs[k].x;
-                eb[k] = pairs[k].y;
+            for (int a = 0; a < arms && e == cudaSuccess; a++) {
+                const size_t np = h_npairs[a];
+                std::vector<int2> pairs(np);
+                if (np)
+                    e = cudaMemcpy(pairs.data(), d_pairs + (size_t)a * d_pairs_cap, np * sizeof(int2),
+                                   cudaMemcpyDeviceToHost);
+                std::sort(pairs.begin(), pairs.end(),
+                          [](const int2 &p, const int2 &q) { return p.y != q.y ? p.y < q.y : p.x < q.x; });
+                ea[a].resize(np);
+                eb[a].resize(np);
+                for (size_t k = 0; k < np; k++) {
+                    ea[a][k] = pairs[k].x;
+                    eb[a][k] = pairs[k].y;
+                }
             }
             break;
         }
@@ -833,66 +885,100 @@ struct Solver {
         return mrpop::fail_status(MRPOP_ERR_CUDA, (std::string("drrt: ") + what + ": " + cudaGetErrorString(e)).c_str());
     }
 
+    // One round: `blocks[a]` blocks of 230 samples grow arm a's roadmap.  The
+    // reference grows every arm's roadmap in one launch (roadmap_interior.cuh:
+    // 88-339); here the round's node checks of all arms go to the validator as
+    // one group, then every arm's neighbour pairs are found, then the edge
+    // checks of all arms go as one group.  Each arm draws from its own random
+    // streams, so the grouping changes no sample.
     int roadmap_round(const std::vector<int> &blocks) {
+        std::vector<std::vector<float>> smp(arms), e0(arms), e1(arms);
+        std::vector<std::vector<uint8_t>> okv(arms);
+        std::vector<std::vector<int32_t>> fhv(arms);
+        std::vector<mrpop_check_call> calls;
         for (int a = 0; a < arms; a++) {
             const int nb = blocks[a];
             if (nb <= 0) continue;
-            Roadmap &M = rm[a];
             // samples in time order: iteration-major, block-minor
             const int64_t K = (int64_t)nb * kRoadmapIters;
-            a0.resize((size_t)K * 7);
+            smp[a].resize((size_t)K * 7);
             for (int xx = 0; xx < kRoadmapIters; xx++)
                 for (int b = 0; b < nb; b++) {
                     Rng &r = rm_rng[(size_t)a * S.block_per_robot + (b % S.block_per_robot)];
-                    float *x = &a0[((size_t)xx * nb + b) * 7];
+                    float *x = &smp[a][((size_t)xx * nb + b) * 7];
                     for (int j = 0; j < 7; j++) x[j] = fmaf(r.uniform(), kSm[j], kSa[j]);
                 }
-            a1 = a0;
-            int rc = check(K, MRPOP_RULE_PLAIN, 0.0f, MRPOP_CHECK_ENV | MRPOP_CHECK_SELF, a, 1);
+            okv[a].resize((size_t)K);
+            fhv[a].resize((size_t)K);
+            calls.push_back(plain_call(smp[a].data(), smp[a].data(), K, 1, a, okv[a].data(), fhv[a].data()));
+        }
+        int rc = check_many(calls);
+        if (rc) return rc;
+        // the valid samples become nodes; edges: every existing node within
+        // `range` of each new node, the new node being the edge's end
+        // (roadmap_interior.cuh:183-240), ordered by new node, then old node
+        const auto t_nb = Clock::now();
+        std::vector<int> n_old(arms, 0);
+        for (int a = 0; a < arms; a++) {
+            Roadmap &M = rm[a];
+            n_old[a] = M.size();
+            if (blocks[a] <= 0) continue;
+            const int64_t K = (int64_t)okv[a].size();
+            int added = 0;
+            for (int64_t k = 0; k < K && n_old[a] + added < kMaxRoadmap; k++)
+                if (okv[a][k]) {
+                    M.add(&smp[a][(size_t)k * 7]);
+                    added++;
+                }
+        }
+        std::vector<std::vector<int>> ea(arms), eb(arms);
+        if (device_nn) {
+            rc = roadmap_pairs_device(n_old, ea, eb);
             if (rc) return rc;
-            std::vector<float> nodes;
-            for (int64_t k = 0; k < K; k++)
-                if (ok[k]) nodes.insert(nodes.end(), &a0[(size_t)k * 7], &a0[(size_t)k * 7] + 7);
-            // edges: every existing node within `range` of each new node, the
-            // new node being the edge's end (roadmap_interior.cuh:183-240),
-            // ordered by new node, then old node
-            const int n_old = M.size();
-            const int n_new = std::min<int>((int)(nodes.size() / 7), kMaxRoadmap - n_old);
-            const auto t_nb = Clock::now();
-            for (int j = 0; j < n_new; j++) M.add(&nodes[(size_t)j * 7]);
-            std::vector<int> ea, eb;
-            if (device_nn) {
-                rc = roadmap_pairs_device(a, n_old, ea, eb);
-                if (rc) return rc;
-            } else {
-                std::vector<std::vector<int>> nbr(std::max(n_new, 0));
+        } else {
+            for (int a = 0; a < arms; a++) {
+                const Roadmap &M = rm[a];
+                const int n_new = M.size() - n_old[a];
+                if (n_new <= 0) continue;
+                std::vector<std::vector<int>> nbr(n_new);
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
                 for (int j = 0; j < n_new; j++) {
-                    const float *x = M.node(n_old + j);
-                    for (int i = 0; i < n_old + j; i++)
+                    const float *x = M.node(n_old[a] + j);
+                    for (int i = 0; i < n_old[a] + j; i++)
                         if (l2(M.node(i), x, 7) < S.range) nbr[j].push_back(i);
                 }
                 for (int j = 0; j < n_new; j++)
                     for (int i : nbr[j]) {
-                        ea.push_back(i);
-                        eb.push_back(n_old + j);
+                        ea[a].push_back(i);
+                        eb[a].push_back(n_old[a] + j);
                     }
             }
-            R->roadmap_ns += ns_since(t_nb);
-            const int64_t ne = (int64_t)ea.size();
-            a0.resize((size_t)ne * 7);
-            a1.resize((size_t)ne * 7);
+        }
+        R->roadmap_ns += ns_since(t_nb);
+        calls.clear();
+        for (int a = 0; a < arms; a++) {
+            const Roadmap &M = rm[a];
+            const int64_t ne = (int64_t)ea[a].size();
+            if (!ne) continue;
+            e0[a].resize((size_t)ne * 7);
+            e1[a].resize((size_t)ne * 7);
             for (int64_t e = 0; e < ne; e++) {
-                std::memcpy(&a0[(size_t)e * 7], M.node(ea[e]), 7 * sizeof(float));
-                std::memcpy(&a1[(size_t)e * 7], M.node(eb[e]), 7 * sizeof(float));
+                std::memcpy(&e0[a][(size_t)e * 7], M.node(ea[a][e]), 7 * sizeof(float));
+                std::memcpy(&e1[a][(size_t)e * 7], M.node(eb[a][e]), 7 * sizeof(float));
             }
-            rc = check(ne, MRPOP_RULE_PLAIN, 0.0f, MRPOP_CHECK_ENV | MRPOP_CHECK_SELF, a, g);
-            if (rc) return rc;
+            okv[a].resize((size_t)ne);
+            fhv[a].resize((size_t)ne);
+            calls.push_back(plain_call(e0[a].data(), e1[a].data(), ne, g, a, okv[a].data(), fhv[a].data()));
+        }
+        rc = check_many(calls);
+        if (rc) return rc;
+        for (int a = 0; a < arms; a++) {
             std::vector<std::pair<int, int>> good;
-            for (int64_t e = 0; e < ne; e++)
-                if (ok[e]) good.emplace_back(ea[e], eb[e]);
-            std::sort(good.begin(), good.end(), [](auto &x, auto &y) { return x.second != y.second ? x.second < y.second : x.first < y.first; });
-            for (auto &p : good) M.link(p.first, p.second);
+            for (size_t e = 0; e < ea[a].size(); e++)
+                if (okv[a][e]) good.emplace_back(ea[a][e], eb[a][e]);
+            std::sort(good.begin(), good.end(),
+                      [](auto &x, auto &y) { return x.second != y.second ? x.second < y.second : x.first < y.first; });
+            for (auto &p : good) rm[a].link(p.first, p.second);
         }
         return 0;
     }
@@ -1452,9 +1538,9 @@ namespace mrpop {
 
 // The planner with any validator; device_nn: nearest-neighbour searches as a
 // kernel on the current device (else on the host).
-mrpop_status drrt_run(int arms, mrpop_check_fn validate, void *ctx, bool device_nn, const float *start,
-                      const float *goals, int num_goals, const mrpop_drrt_settings *settings, float *path_out,
-                      int64_t max_waypoints, mrpop_drrt_solution_fn on_solution, void *solution_ctx,
+mrpop_status drrt_run(int arms, mrpop_check_fn validate, check_many_fn validate_many, void *ctx, bool device_nn,
+                      const float *start, const float *goals, int num_goals, const mrpop_drrt_settings *settings,
+                      float *path_out, int64_t max_waypoints, mrpop_drrt_solution_fn on_solution, void *solution_ctx,
                       mrpop_drrt_result *out) {
     if (arms < 1 || arms > MRPOP_MAX_ARMS || !validate || !start || !goals || num_goals < 1 || !settings || !out)
         return fail_status(MRPOP_ERR_INVALID_ARGUMENT, "drrt: bad argument");
@@ -1463,6 +1549,7 @@ mrpop_status drrt_run(int arms, mrpop_check_fn validate, void *ctx, bool device_
     *out = mrpop_drrt_result{};
     Solver sv;
     sv.validate = validate;
+    sv.validate_many = validate_many;
     sv.vctx = ctx;
     sv.device_nn = device_nn;
     if (device_nn && sv.adopt_device() != cudaSuccess) return fail_status(MRPOP_ERR_CUDA, "drrt: device resources");
@@ -1492,7 +1579,7 @@ extern "C" mrpop_status mrpop_drrt_solve_with(int arms, mrpop_check_fn validate,
                                               float *path_out, int64_t max_waypoints,
                                               mrpop_drrt_solution_fn on_solution, void *solution_ctx,
                                               mrpop_drrt_result *out) {
-    return mrpop::drrt_run(arms, validate, ctx, false, start, goals, num_goals, settings, path_out, max_waypoints,
+    return mrpop::drrt_run(arms, validate, nullptr, ctx, false, start, goals, num_goals, settings, path_out, max_waypoints,
                            on_solution, solution_ctx, out);
 }
 
@@ -1506,6 +1593,6 @@ extern "C" mrpop_status mrpop_drrt_solve(const mrpop_scene *scene, const mrpop_r
     chk.scene = scene;
     chk.robots = robots;
     if (mrpop_workspace_create(&chk.ws) != MRPOP_OK) return MRPOP_ERR_CUDA;
-    return mrpop::drrt_run(arms, &GpuChecker::call, &chk, true, start, goals, num_goals, settings, path_out,
+    return mrpop::drrt_run(arms, &GpuChecker::call, nullptr, &chk, true, start, goals, num_goals, settings, path_out,
                            max_waypoints, on_solution, solution_ctx, out);
 }

@@ -69,11 +69,13 @@ constexpr size_t split_scratch_bytes(int64_t n_edges, int g, int A) {
 }
 void set_split_scratch(EdgeParams &p, void *scratch, int64_t n_edges, int g, int A);
 
-// The dRRT / AO-x planner (drrt.cu) with any validator; device_nn: tree
-// searches as a kernel on the current device, else on the host.
-mrpop_status drrt_run(int arms, mrpop_check_fn validate, void *ctx, bool device_nn, const float *start,
-                      const float *goals, int num_goals, const mrpop_drrt_settings *settings, float *path_out,
-                      int64_t max_waypoints, mrpop_drrt_solution_fn on_solution, void *solution_ctx,
+// The dRRT / AO-x planner (drrt.cu) with any validator (validate_many, if
+// not null, takes the groups of checks of the roadmap rounds in one call);
+// device_nn: tree searches as a kernel on the current device, else on the host.
+using check_many_fn = int (*)(void *ctx, const mrpop_check_call *calls, int n_calls);
+mrpop_status drrt_run(int arms, mrpop_check_fn validate, check_many_fn validate_many, void *ctx, bool device_nn,
+                      const float *start, const float *goals, int num_goals, const mrpop_drrt_settings *settings,
+                      float *path_out, int64_t max_waypoints, mrpop_drrt_solution_fn on_solution, void *solution_ctx,
                       mrpop_drrt_result *out);
 
 // Arm count of a robot set (0 for null).

@@ -125,8 +125,8 @@ struct mrpop_session {
     uint8_t *h_valid = nullptr;
     int32_t *h_first = nullptr;
     // guarded by server->mu
-    std::condition_variable done_cv;  // this session's step done
-    bool in_flight = false;
+    std::condition_variable done_cv;  // this session's steps done
+    int in_flight = 0;                // steps submitted and not yet retired
     mrpop_status result = MRPOP_OK;
     std::string error;
 };
@@ -318,8 +318,7 @@ void retire_wave(mrpop_server *s, mrpop_server::Slot &slot, cudaError_t err) {
             st.session->result = MRPOP_ERR_CUDA;
             st.session->error = msg;
         }
-        st.session->in_flight = false;
-        st.session->done_cv.notify_one();
+        if (--st.session->in_flight == 0) st.session->done_cv.notify_one();
     }
     slot.steps.clear();
     slot.busy = false;
@@ -496,7 +495,10 @@ mrpop_status mrpop_session_open(mrpop_server *s, int arms, int64_t max_edges, in
     const int64_t max_chunks = (max_edges + kChunkEdges - 1) / kChunkEdges;
     if (max_chunks > s->cfg.max_wave_chunks || max_edges > INT32_MAX)
         return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_open: max_edges exceeds one wave's chunk table");
-    const size_t bytes = round_up(mrpop::split_scratch_bytes(max_edges, max_granularity, arms));
+    // scratch of max_edges edges at the largest arm count and granularity, and
+    // room for the per-item header and alignment of a multi-item submission
+    const size_t bytes =
+        round_up(mrpop::split_scratch_bytes(max_edges, max_granularity, arms) + 2 * MRPOP_SESSION_MAX_ITEMS * kAlign);
     const size_t qbytes = round_up((size_t)max_edges * 7 * arms * sizeof(float));
     const size_t host_bytes = 2 * qbytes + round_up((size_t)max_edges) + round_up((size_t)max_edges * sizeof(int32_t));
     if ((int64_t)bytes > s->stats.budget_bytes || host_bytes > round_up((size_t)s->cfg.host_bytes))
@@ -540,36 +542,63 @@ mrpop_status mrpop_session_open(mrpop_server *s, int arms, int64_t max_edges, in
     return MRPOP_OK;
 }
 
-mrpop_status mrpop_session_submit(mrpop_session *ss, const mrpop_batch_item *it) {
-    if (!ss || !it) return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_submit: null argument");
+mrpop_status mrpop_session_submit_many(mrpop_session *ss, const mrpop_batch_item *items, int n) {
+    if (!ss || (!items && n)) return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_submit: null argument");
+    if (n < 0 || n > MRPOP_SESSION_MAX_ITEMS)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_submit: at most MRPOP_SESSION_MAX_ITEMS steps at once");
     mrpop_server *s = ss->server;
-    mrpop_server::Step st;
-    st.session = ss;
-    int A = 0;
-    mrpop_status r = mrpop::make_params(it->scene, it->robots, it->q0, it->q1, it->n_edges, it->granularity,
-                                        it->rule, it->range, it->flags, it->arm, it->valid, it->first_hit, nullptr,
-                                        nullptr, st.p, A, st.smem);
-    if (r != MRPOP_OK) return r;
-    if (it->n_edges > ss->max_edges || it->granularity > ss->max_g || A > ss->arms)
-        return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_submit: step larger than the session was opened for");
-    st.arms = A;
-    st.spl = it->granularity > 32 ? 2 : 1;
-    st.seg = it->rule != MRPOP_RULE_PLAIN;
-    st.n_chunks = (int)((it->n_edges + kChunkEdges - 1) / kChunkEdges);
-    mrpop::set_split_scratch(st.p, s->d_arena + ss->offset, it->n_edges, it->granularity, A);
+    mrpop_server::Step steps[MRPOP_SESSION_MAX_ITEMS];
+    int n_steps = 0;
+    int64_t edges = 0;
+    size_t off = 0;  // scratch offset in the session's block
+    for (int k = 0; k < n; k++) {
+        const mrpop_batch_item *it = &items[k];
+        mrpop_server::Step &st = steps[n_steps];
+        st = mrpop_server::Step{};
+        st.session = ss;
+        int A = 0;
+        const mrpop_status r = mrpop::make_params(it->scene, it->robots, it->q0, it->q1, it->n_edges, it->granularity,
+                                                  it->rule, it->range, it->flags, it->arm, it->valid, it->first_hit,
+                                                  nullptr, nullptr, st.p, A, st.smem);
+        if (r != MRPOP_OK) return r;
+        if (it->n_edges > ss->max_edges || it->granularity > ss->max_g || A > ss->arms)
+            return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_submit: step larger than the session was opened for");
+        edges += it->n_edges;
+        if (it->n_edges == 0) continue;
+        const size_t need = mrpop::split_scratch_bytes(it->n_edges, it->granularity, A);
+        if (off + need > ss->bytes)
+            return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_submit: the steps' scratch exceeds the session's");
+        st.arms = A;
+        st.spl = it->granularity > 32 ? 2 : 1;
+        st.seg = it->rule != MRPOP_RULE_PLAIN;
+        st.n_chunks = (int)((it->n_edges + kChunkEdges - 1) / kChunkEdges);
+        mrpop::set_split_scratch(st.p, s->d_arena + ss->offset + off, it->n_edges, it->granularity, A);
+        off = round_up(off + need);
+        n_steps++;
+    }
+    if (edges > ss->max_edges)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_submit: the steps' edges exceed the session's max_edges");
     {
         std::lock_guard<std::mutex> lk(s->mu);
         if (ss->in_flight) return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_submit: the previous step is not done");
         ss->result = MRPOP_OK;
         ss->error.clear();
-        if (it->n_edges == 0) return MRPOP_OK;
-        ss->in_flight = true;
-        st.t_submit = host_ns();
-        s->pending.push_back(st);
+        if (!n_steps) return MRPOP_OK;
+        ss->in_flight = n_steps;
+        const int64_t now = host_ns();
+        for (int k = 0; k < n_steps; k++) {
+            steps[k].t_submit = now;
+            s->pending.push_back(steps[k]);
+        }
         s->n_pending.store((int64_t)s->pending.size(), std::memory_order_relaxed);
     }
     s->work_cv.notify_one();
     return MRPOP_OK;
+}
+
+mrpop_status mrpop_session_submit(mrpop_session *ss, const mrpop_batch_item *it) {
+    if (!it) return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_submit: null argument");
+    return mrpop_session_submit_many(ss, it, 1);
 }
 
 mrpop_status mrpop_session_wait(mrpop_session *ss, int64_t timeout_ms) {
@@ -577,8 +606,8 @@ mrpop_status mrpop_session_wait(mrpop_session *ss, int64_t timeout_ms) {
     mrpop_server *s = ss->server;
     std::unique_lock<std::mutex> lk(s->mu);
     if (timeout_ms < 0) {
-        ss->done_cv.wait(lk, [&] { return !ss->in_flight; });
-    } else if (!ss->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return !ss->in_flight; })) {
+        ss->done_cv.wait(lk, [&] { return ss->in_flight == 0; });
+    } else if (!ss->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return ss->in_flight == 0; })) {
         return fail(MRPOP_ERR_DEVICE_TIMEOUT, "session_wait: the step is still running");
     }
     if (ss->result != MRPOP_OK) return fail(ss->result, ss->error);
@@ -590,7 +619,7 @@ mrpop_status mrpop_session_close(mrpop_session *ss) {
     mrpop_server *s = ss->server;
     {
         std::unique_lock<std::mutex> lk(s->mu);
-        ss->done_cv.wait(lk, [&] { return !ss->in_flight; });
+        ss->done_cv.wait(lk, [&] { return ss->in_flight == 0; });
         arena_give(s->free_blocks, s->in_use, ss->offset, ss->bytes);
         arena_give(s->free_host, s->host_in_use, ss->host_off, ss->host_bytes);
     }
@@ -708,6 +737,64 @@ int session_check(void *ctx, const float *q0, const float *q1, int64_t n, int g,
     return MRPOP_OK;
 }
 
+// A group of the planner's checks: as many as fit the session's buffers
+// (edges, endpoint floats, MRPOP_SESSION_MAX_ITEMS) are packed into them and
+// submitted together; a check larger than the session goes alone, in steps.
+int session_check_many(void *ctx, const mrpop_check_call *calls, int n) {
+    auto *c = static_cast<SessionChecker *>(ctx);
+    mrpop_session *ss = c->ss;
+    const int64_t qcap = ss->max_edges * 7 * ss->arms;
+    int i = 0;
+    while (i < n) {
+        if (calls[i].n_edges > ss->max_edges) {
+            const mrpop_check_call &f = calls[i];
+            const int rc = session_check(ctx, f.q0, f.q1, f.n_edges, f.granularity, f.rule, f.range, f.flags, f.arm,
+                                         f.valid, f.first_hit);
+            if (rc) return rc;
+            i++;
+            continue;
+        }
+        mrpop_batch_item items[MRPOP_SESSION_MAX_ITEMS];
+        int64_t e_off[MRPOP_SESSION_MAX_ITEMS];
+        int64_t e_at = 0, q_at = 0;
+        int k = 0, j = i;
+        for (; j < n && k < MRPOP_SESSION_MAX_ITEMS; j++, k++) {
+            const mrpop_check_call &f = calls[j];
+            const int dof = 7 * (f.arm >= 0 ? 1 : ss->arms);
+            if (f.n_edges > ss->max_edges || e_at + f.n_edges > ss->max_edges || q_at + f.n_edges * dof > qcap) break;
+            std::memcpy(ss->h_q0 + q_at, f.q0, (size_t)f.n_edges * dof * sizeof(float));
+            std::memcpy(ss->h_q1 + q_at, f.q1, (size_t)f.n_edges * dof * sizeof(float));
+            mrpop_batch_item &it = items[k];
+            it = mrpop_batch_item{};
+            it.scene = c->scene;
+            it.robots = c->robots;
+            it.q0 = ss->h_q0 + q_at;
+            it.q1 = ss->h_q1 + q_at;
+            it.n_edges = f.n_edges;
+            it.granularity = f.granularity;
+            it.flags = f.flags;
+            it.arm = f.arm;
+            it.valid = ss->h_valid + e_at;
+            it.first_hit = ss->h_first + e_at;
+            it.rule = f.rule;
+            it.range = f.range;
+            e_off[k] = e_at;
+            e_at += f.n_edges;
+            q_at += f.n_edges * dof;
+        }
+        mrpop_status st = mrpop_session_submit_many(ss, items, k);
+        if (st == MRPOP_OK) st = mrpop_session_wait(ss, -1);
+        if (st != MRPOP_OK) return st;
+        for (int m = 0; m < k; m++) {
+            const mrpop_check_call &f = calls[i + m];
+            std::memcpy(f.valid, ss->h_valid + e_off[m], (size_t)f.n_edges);
+            std::memcpy(f.first_hit, ss->h_first + e_off[m], (size_t)f.n_edges * sizeof(int32_t));
+        }
+        i = j;
+    }
+    return MRPOP_OK;
+}
+
 }  // namespace
 
 extern "C" mrpop_status mrpop_session_drrt(mrpop_session *ss, const mrpop_scene *scene, const mrpop_robotset *robots,
@@ -721,6 +808,6 @@ extern "C" mrpop_status mrpop_session_drrt(mrpop_session *ss, const mrpop_scene 
     if (mrpop::robotset_arms(robots) != ss->arms)
         return fail(MRPOP_ERR_INVALID_ARGUMENT, "session_drrt: the robot set's arm count differs from the session's");
     SessionChecker c{ss, scene, robots};
-    return mrpop::drrt_run(ss->arms, session_check, &c, true, start, goals, num_goals, settings, path_out,
+    return mrpop::drrt_run(ss->arms, session_check, session_check_many, &c, true, start, goals, num_goals, settings, path_out,
                            max_waypoints, on_solution, solution_ctx, out);
 }

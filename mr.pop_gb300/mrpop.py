@@ -35,7 +35,7 @@ EXPORTED = [
     "mrpop_server_get_stats", "mrpop_session_open", "mrpop_session_submit", "mrpop_session_wait",
     "mrpop_session_close", "mrpop_session_host_buffers", "mrpop_plan", "mrpop_session_plan",
     "mrpop_drrt_settings_default", "mrpop_drrt_solve", "mrpop_drrt_solve_with", "mrpop_session_drrt",
-    "mrpop_batch_shapes", "mrpop_batch_set_shape", "mrpop_drrt_release_pool",
+    "mrpop_batch_shapes", "mrpop_batch_set_shape", "mrpop_drrt_release_pool", "mrpop_session_submit_many",
 ]
 KERNEL_KINDS = ("fused", "broad", "narrow")
 NOALLOC_MAX_EDGES = 16384
@@ -170,6 +170,7 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
         "mrpop_server_get_stats": [vp, C.POINTER(ServerStats)],
         "mrpop_session_open": [vp, i32, i64, i32, i64, C.POINTER(vp)],
         "mrpop_session_submit": [vp, C.POINTER(BatchItem)],
+        "mrpop_session_submit_many": [vp, C.POINTER(BatchItem), i32],
         "mrpop_session_wait": [vp, i64],
         "mrpop_session_close": [vp],
         "mrpop_session_host_buffers": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)],
@@ -578,6 +579,29 @@ class Session:
                  range_=0.0):
         self.submit(scene, robots, q0, q1, granularity, flags, arm, rule, range_)
         return self.wait()
+
+    def validate_many(self, scene: Scene, robots: RobotSet, checks: list[tuple]):
+        """Several steps submitted together (mrpop_session_submit_many), packed
+        one after another in the session's buffers; checks: (q0, q1,
+        granularity, flags, arm, rule, range_) tuples.  Returns a (valid,
+        first_hit) pair per check."""
+        items, spans = (BatchItem * max(1, len(checks)))(), []
+        q_at = e_at = 0
+        fq0, fq1 = self.q0.reshape(-1), self.q1.reshape(-1)
+        for k, (q0, q1, g, flags, arm, rule, rg) in enumerate(checks):
+            n, dof = q0.shape
+            if e_at + n > self.max_edges or q_at + n * dof > fq0.size:
+                raise MrpopError(1, "session steps exceed the session's buffers")
+            fq0[q_at:q_at + n * dof] = np.asarray(q0, np.float32).reshape(-1)
+            fq1[q_at:q_at + n * dof] = np.asarray(q1, np.float32).reshape(-1)
+            items[k] = BatchItem(scene.handle, robots.handle, self._ptrs[0] + 4 * q_at, self._ptrs[1] + 4 * q_at, n, g,
+                                 flags, arm, self._ptrs[2] + e_at, self._ptrs[3] + 4 * e_at, rule, float(rg))
+            spans.append((e_at, n))
+            q_at += n * dof
+            e_at += n
+        _check(self.lib, self.lib.mrpop_session_submit_many(self.handle, items, len(checks)))
+        _check(self.lib, self.lib.mrpop_session_wait(self.handle, -1))
+        return [(self.valid[a:a + n].copy(), self.first_hit[a:a + n].copy()) for a, n in spans]
 
     def plan(self, scene: Scene, robots: RobotSet, start: np.ndarray, goal: np.ndarray, settings: PlanSettingsC,
              flags: int = CHECK_ENV | CHECK_SELF, max_waypoints: int = 4096):

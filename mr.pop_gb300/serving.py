@@ -35,7 +35,7 @@ class Served:
         return 1e3 * (self.finish - self.arrival)
 
 
-DRRT_STEP_EDGES = 4096  # a dRRT session's step size: larger checks are cut into steps of this many edges
+DRRT_STEP_EDGES = 8192  # a dRRT session's step size: larger checks are cut into steps of this many edges
 
 
 # The service shape for dRRT clients: wave slots (CUDA streams) and client

@@ -74,6 +74,57 @@ def test_steps_equal_direct_calls(cuda, pkg, fused_edges):
     server.close()
 
 
+def test_multi_item_submissions_equal_direct_calls(cuda, pkg):
+    """mrpop_session_submit_many: a session's several steps (composite and
+    single-arm, plain and segmented, different granularities) submitted
+    together, from concurrent sessions, give the direct calls' verdicts."""
+    W = pkg.workloads
+    insts = W.config4_instances(n_instances=8, seed=5, scale=0.04)
+    rules = [(pkg.RULE_PLAIN, 0.0), (pkg.RULE_CONNECT, 0.6), (pkg.RULE_SHORTCUT, 0.7)]
+    server = pkg.Server(budget_bytes=512 << 20, streams=2)
+    jobs = []
+    for k, wl in enumerate(insts):
+        scene = pkg.Scene(wl.scene)
+        rb = pkg.RobotSet(len(wl.bases), wl.bases)
+        A = len(wl.bases)
+        checks = []
+        for m in range(min(4, A + 1)):
+            arm = -1 if m == 0 else m - 1
+            q0, q1 = wl.q0, wl.q1
+            if arm >= 0:
+                q0 = np.ascontiguousarray(q0[:, 7 * arm:7 * arm + 7])
+                q1 = np.ascontiguousarray(q1[:, 7 * arm:7 * arm + 7])
+            n = max(1, len(q0) // (m + 1))
+            rule, rg = rules[(k + m) % 3]
+            checks.append((q0[:n], q1[:n], [16, 32, 64][(k + m) % 3], wl.flags, arm, rule, rg))
+        jobs.append((scene, rb, A, checks))
+    expect = [[_direct(pkg, cuda, scene, rb, *c) for c in checks] for scene, rb, _, checks in jobs]
+    got, errors = [None] * len(jobs), []
+
+    def client(i):
+        try:
+            scene, rb, A, checks = jobs[i]
+            sess = server.session(A, sum(len(c[0]) for c in checks), 64)
+            got[i] = sess.validate_many(scene, rb, checks)
+            sess.close()
+        except Exception as e:  # noqa: BLE001
+            errors.append((i, e))
+
+    th = [threading.Thread(target=client, args=(i,)) for i in range(len(jobs))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors, errors
+    for i in range(len(jobs)):
+        for (v, f), (ev, ef) in zip(got[i], expect[i]):
+            assert np.array_equal(v, ev), i
+            assert np.array_equal(f, ef), i
+    st = server.stats()
+    assert st["steps"] == sum(len(j[3]) for j in jobs) and st["bytes_in_use"] == 0
+    server.close()
+
+
 def test_admission_waits_for_budget(cuda, pkg):
     W = pkg.workloads
     wl = W.config2(n_edges=256, seed=1)
