@@ -633,7 +633,8 @@ def run_serving(args, world, rank, local, pkg, torch):
                        "isolated_p50_ms": iso["p50_ms"], "isolated_p99_ms": iso["p99_ms"],
                        "isolated_queries": m,
                        "p99_ratio": sv["p99_ms"] / iso["p99_ms"] if iso["p99_ms"] else None},
-           "solve_rate": {"served": sv["solve_rate"], "isolated": iso["solve_rate"]},
+           "solve_rate": {"served": sv["solve_rate"], "isolated": iso["solve_rate"],
+                          "served_same_queries": S.summary(served[:m])["solve_rate"]},
            "mean_cost": {"served": sv["mean_cost"], "isolated": iso["mean_cost"]},
            "same_result_alone_and_mixed": f"{same}/{m}",
            "phase_mean_ms": {"served": sv["phase_mean_ms"], "isolated": iso["phase_mean_ms"]},

@@ -288,13 +288,17 @@ mrpop_status mrpop_batch_destroy(mrpop_batch *batch);
  * plain or segmented, whose buffers are device memory or page-locked host
  * memory and must stay valid until the step is done) and waits for it
  * (mrpop_session_wait; timeout_ms as above, MRPOP_ERR_DEVICE_TIMEOUT if the
- * step is still running).  The worker gathers the steps pending from all
- * sessions, in submission order, into a wave (up to max_wave_steps steps, and
- * up to max_wave_chunks chunks counted at 96 edges each), cuts it into chunks of
- * 6 to 96 edges so that even a small wave spreads over the SMs, and launches it
- * as one set of persistent batch kernels on the next free slot's stream, so
- * waves formed while others run overlap on the device.  Each step's verdicts equal the same
- * mrpop_validate_edges / mrpop_validate_segments call made alone.
+ * step is still running).  The worker (a dispatcher thread) gathers the
+ * steps pending from all sessions, in submission order, into a wave (up to
+ * max_wave_steps steps, and up to max_wave_chunks chunks counted at 96 edges
+ * each), cuts it into chunks of 6 to 96 edges so that even a small wave
+ * spreads over the SMs, and launches it as one set of persistent batch kernels
+ * on the next free slot's stream, so waves formed while others run overlap on
+ * the device.  While waves are in flight the worker polls an event recorded
+ * after each wave (one host core busy) and wakes each session whose steps are
+ * done; with nothing in flight or pending it sleeps.  Each step's verdicts
+ * equal the same mrpop_validate_edges / mrpop_validate_segments call made
+ * alone.
  * mrpop_session_close waits for the session's step and returns its memory to
  * the arena.  Sessions may be used from different host threads; one session
  * is used by one thread at a time.  Close every session before
@@ -556,9 +560,11 @@ mrpop_status mrpop_drrt_solve_with(int arms, mrpop_check_fn validate, void *ctx,
 int64_t mrpop_drrt_release_pool(void);
 /* The same planner with its checks served by a session of the validation
  * service (below): every check becomes steps of at most the session's edge
- * count, co-batched with the steps of the other sessions; the tree searches
- * run on the device on a stream of the call's own.  The session needs the
- * robot set's arm count and a granularity of at least settings->granularity. */
+ * count, co-batched with the steps of the other sessions, and each roadmap
+ * round's checks of all arms go in as one mrpop_session_submit_many group;
+ * the tree searches run on the device on a stream of the call's own.  The
+ * session needs the robot set's arm count and a granularity of at least
+ * settings->granularity. */
 mrpop_status mrpop_session_drrt(mrpop_session *session, const mrpop_scene *scene, const mrpop_robotset *robots,
                                 const float *start, const float *goals, int num_goals,
                                 const mrpop_drrt_settings *settings, float *path_out, int64_t max_waypoints,
