@@ -715,14 +715,19 @@ def run_planner(args, pkg, torch):
         wall = time.perf_counter_ns() - t0
         rows.append({"problem": p, "solved": r.solved, "cost": r.cost, "kernel_ns": r.stats["kernel_ns"],
                      "wall_ns": wall, "iterations": r.stats["iterations"], "edges": r.stats["edges_validated"],
-                     "validate_ns": r.stats["validate_ns"], "nn_ns": r.stats["nn_ns"]})
+                     "validate_ns": r.stats["validate_ns"], "nn_ns": r.stats["nn_ns"],
+                     "roadmap_ns": r.stats["roadmap_ns"], "oracle_ns": r.stats["oracle_ns"],
+                     "validate_calls": r.stats["validate_calls"]})
     clk = clocks.stop()
     edges = sum(r["edges"] for r in rows)
     out = planner_line(args, "mine", rows, {"validated_edges": edges,
                                             "validate_share_of_kernel_ns": sum(r["validate_ns"] for r in rows) /
                                             max(1, sum(r["kernel_ns"] for r in rows)),
                                             "nn_share_of_kernel_ns": sum(r["nn_ns"] for r in rows) /
-                                            max(1, sum(r["kernel_ns"] for r in rows))})
+                                            max(1, sum(r["kernel_ns"] for r in rows)),
+                                            "phase_mean_ms": {k: round(float(np.mean([r[k + "_ns"] for r in rows])) / 1e6, 2)
+                                                              for k in ("kernel", "validate", "nn", "roadmap", "oracle")},
+                                            "validate_calls_mean": float(np.mean([r["validate_calls"] for r in rows]))})
     out["clocks"] = clk
     out["gpu_launches"] = None
     out["per_problem"] = [{k: r[k] for k in ("problem", "solved", "cost", "kernel_ns")} for r in rows]

@@ -123,7 +123,15 @@ mrpop_status mrpop_robotset_destroy(mrpop_robotset *robots);
  * Outputs (device): valid[e] = 1 if collision-free; first_hit[e] = the 1-based
  * sample index of the first sample whose detailed check fired (-1 if valid).
  * Replaces one fkcc_single_buffer* call per edge (see flags above).
+ * Launch form: a call of more than the fused-edge limit runs the split
+ * pipeline (a broad and a narrow kernel; for segmented rules, segment rounds
+ * of both and a fused tail); a smaller call runs as one fused launch (both
+ * phases per edge in one warp, from segment 0), which saves the launches and
+ * the staging that dominate small calls.  Verdicts are the same either way.
+ * mrpop_set_fused_edges sets the limit for the process (0: the default, 2048
+ * edges; -1: every call split) and returns the previous one.
  */
+int64_t mrpop_set_fused_edges(int64_t max_edges);
 mrpop_status mrpop_validate_edges(const mrpop_scene *scene, const mrpop_robotset *robots,
                                   const float *q0, const float *q1, int64_t n_edges,
                                   int granularity, uint32_t flags, int arm, uint8_t *valid,

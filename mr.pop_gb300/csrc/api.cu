@@ -1,4 +1,5 @@
 // api.cu -- C ABI of the GB300 edge validator (declared in include/mrpop.h).
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -479,8 +480,10 @@ mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots,
     return MRPOP_OK;
 }
 
-// 16 bytes of work counters, then per edge: flag words, candidate masks,
-// reference-sphere bounds and segment state.
+// A 128-byte head with the two work counters, then per edge: flag words,
+// candidate masks, reference-sphere bounds and segment state.  The kernels
+// stage the flag words as 32-bit pairs for up to 4 arms, in the first half
+// of their slice (which keeps its 64-bit size).
 int robotset_arms(const mrpop_robotset *robots) { return robots ? robots->n_arms : 0; }
 
 void set_split_scratch(EdgeParams &p, void *scratch, int64_t n_edges, int g, int A) {
@@ -489,7 +492,7 @@ void set_split_scratch(EdgeParams &p, void *scratch, int64_t n_edges, int g, int
     const size_t mask_bytes = (size_t)n_edges * 2 * sizeof(uint64_t);
     const size_t bound_bytes = (size_t)n_edges * A * kRefSpheres * sizeof(float4);
     p.work = (unsigned long long *)scratch;
-    char *b = (char *)scratch + 2 * sizeof(unsigned long long);
+    char *b = (char *)scratch + kSplitScratchHead;
     p.sflags = (uint64_t *)b;
     p.smasks = (uint64_t *)(b + flag_bytes);
     p.sbounds = (float4 *)(b + flag_bytes + mask_bytes);
@@ -500,6 +503,10 @@ void set_split_scratch(EdgeParams &p, void *scratch, int64_t n_edges, int g, int
 // ext_scratch: caller-provided device scratch for the single-segment pipeline
 // (at least split_scratch_bytes(n_edges, g, arms) bytes); nullptr = the
 // library's stream-ordered pool.
+// Calls of at most this many edges run as one fused launch (mrpop_set_fused_edges).
+constexpr int64_t kFusedEdgesDefault = 2048;
+std::atomic<int64_t> g_fused_edges{kFusedEdgesDefault};
+
 mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robots, const float *q0,
                            const float *q1, int64_t n_edges, int g, int rule, float range, uint32_t flags,
                            int arm, uint8_t *valid, int32_t *first_hit, int32_t *n_seg_out, double *flops,
@@ -520,12 +527,21 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
         p.valid = tmp_valid;
         p.first_hit = tmp_first;
     }
+    // a small call: one fused launch from segment 0, no staging
+    cudaError_t err;
+    if (n_edges <= g_fused_edges.load(std::memory_order_relaxed)) {
+        p.seg0 = 0;
+        err = timed_launch(A, kFused, p, smem, stream);
+        if (tmp_valid) cudaFreeAsync(tmp_valid, stream);
+        if (tmp_first) cudaFreeAsync(tmp_first, stream);
+        if (err != cudaSuccess) return cuda_fail(err, "validate: launch");
+        return MRPOP_OK;
+    }
     // split pipeline: staged flags, masks, bounds and segment state in
     // stream-ordered scratch.  Single-segment edges: one broad and one narrow
     // launch.  Segmented rules: segment r of every undecided edge per round
     // (broad + narrow), kSegRounds rounds, then the fused kernel for the edges
     // that still have segments left, from segment kSegRounds on.
-    cudaError_t err;
     void *scratch = ext_scratch;
     if (!scratch) {
         cudaMemPool_t pool;
@@ -556,6 +572,10 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
 }
 
 mrpop_status fail_status(mrpop_status st, const char *msg) { return fail(st, msg); }
+
+int64_t set_fused_edges(int64_t max_edges) {
+    return g_fused_edges.exchange(max_edges == 0 ? kFusedEdgesDefault : max_edges < 0 ? -1 : max_edges);
+}
 
 }  // namespace mrpop
 
@@ -693,6 +713,8 @@ mrpop_status mrpop_debug_row5_table(uint32_t *out, int64_t words, int *n6, int *
     *n7 = mrpop::kRow5N7;
     return MRPOP_OK;
 }
+
+int64_t mrpop_set_fused_edges(int64_t max_edges) { return mrpop::set_fused_edges(max_edges); }
 
 mrpop_status mrpop_kernel_timing(int enable) {
     std::lock_guard<std::mutex> lk(g_timing_mu);

@@ -142,7 +142,7 @@ struct EdgeParams {
     SceneCounts sc;
     unsigned int *status;
     unsigned long long *phase;  // phase timers (MRPOP_PHASE_TIMERS builds only)
-    uint64_t *sflags;           // split pipeline: per-sample {env, self} flag words
+    uint64_t *sflags;           // split pipeline: per-sample {env, self} flag words (32-bit for <= 4 arms)
     uint64_t *smasks;           // split pipeline: per-edge {env, self} candidate masks
     float4 *sbounds;            // split pipeline: per-edge swept reference-sphere bounds [A][kRefSpheres]
     int32_t *snseg;             // segmented rules: per-edge segment count (-1: too many), from segment 0
@@ -1353,6 +1353,26 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
 // instruction cache on its own.  broad_edge / narrow_edge are one warp's work
 // on edge e, shared by the plain kernels and the batch kernels.
 // ---------------------------------------------------------------------------
+// Staged flag words of sample slot o (= edge * 32 * SPL + sample - 1): 8 flag
+// bits per arm, so 32-bit words hold up to 4 arms.
+template <int A>
+__device__ __forceinline__ void store_flags(const EdgeParams &P, long long o, uint64_t env, uint64_t self) {
+    if (A <= 4) reinterpret_cast<uint2 *>(P.sflags)[o] = make_uint2((uint32_t)env, (uint32_t)self);
+    else reinterpret_cast<ulonglong2 *>(P.sflags)[o] = make_ulonglong2(env, self);
+}
+template <int A>
+__device__ __forceinline__ void load_flags(const EdgeParams &P, long long o, uint64_t &env, uint64_t &self) {
+    if (A <= 4) {
+        const uint2 v = reinterpret_cast<const uint2 *>(P.sflags)[o];
+        env = v.x;
+        self = v.y;
+    } else {
+        const ulonglong2 v = reinterpret_cast<const ulonglong2 *>(P.sflags)[o];
+        env = v.x;
+        self = v.y;
+    }
+}
+
 template <int A, int SPL, bool SEG>
 __device__ __forceinline__ void broad_edge(const EdgeParams &P, WarpScratch &W, const float4 *S, const SceneLayout &L,
                                            long long e, int dof, int g, int lane, bool staged) {
@@ -1403,11 +1423,7 @@ __device__ __forceinline__ void broad_edge(const EdgeParams &P, WarpScratch &W, 
     const bool any = broad_decide<A, SPL>(P, W, S, L, r, g, lane, envw, selfw, cand_env, cand_self, tally);
     if (any) {
 #pragma unroll
-        for (int s = 0; s < SPL; s++) {
-            const long long o = (e * (32 * SPL) + lane + 32 * s) * 2;
-            P.sflags[o] = envw[s];
-            P.sflags[o + 1] = selfw[s];
-        }
+        for (int s = 0; s < SPL; s++) store_flags<A>(P, e * (32 * SPL) + lane + 32 * s, envw[s], selfw[s]);
         for (int t = lane; t < A * kRefSpheres; t += 32) P.sbounds[e * (A * kRefSpheres) + t] = (&W.rsw[0][0])[t];
     }
     if (lane == 0) {
@@ -1444,11 +1460,7 @@ __device__ __forceinline__ void narrow_edge(const EdgeParams &P, WarpScratch &W,
     if (SEG && P.rule == kRuleConnect && r > 0) connect_advance(W, dof, r, lane);
     uint64_t envw[SPL], selfw[SPL];
 #pragma unroll
-    for (int s = 0; s < SPL; s++) {
-        const long long o = (e * (32 * SPL) + lane + 32 * s) * 2;
-        envw[s] = P.sflags[o];
-        selfw[s] = P.sflags[o + 1];
-    }
+    for (int s = 0; s < SPL; s++) load_flags<A>(P, e * (32 * SPL) + lane + 32 * s, envw[s], selfw[s]);
     for (int t = lane; t < A * kRefSpheres; t += 32) (&W.rsw[0][0])[t] = P.sbounds[e * (A * kRefSpheres) + t];
     __syncwarp();
     const int fb = narrow_segment<A, SPL>(P, W, S, L, det_tab, r, lane, envw, selfw, cand_env, cand_self);

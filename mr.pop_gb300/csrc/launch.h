@@ -59,11 +59,13 @@ mrpop_status make_params(const mrpop_scene *scene, const mrpop_robotset *robots,
 size_t warp_scratch_bytes();
 
 // Scratch of the single-segment pipeline (staged flags, candidate masks and
-// reference-sphere bounds): its size, and its slices in p.  Two work counters,
-// then per edge: 32 * spl samples x {env, self} flag words, {env, self}
-// candidate masks, A arms' reference-sphere bounds and the segment state.
+// reference-sphere bounds): its size, and its slices in p.  Two work counters
+// in a 128-byte head (every edge's flag words start on an L2 line), then per
+// edge: 32 * spl samples x {env, self} flag words, {env, self} candidate
+// masks, A arms' reference-sphere bounds and the segment state.
+constexpr size_t kSplitScratchHead = 128;
 constexpr size_t split_scratch_bytes(int64_t n_edges, int g, int A) {
-    return 2 * sizeof(unsigned long long) +
+    return kSplitScratchHead +
            (size_t)n_edges * (32 * (g > 32 ? 2 : 1) * 2 * sizeof(uint64_t) + 2 * sizeof(uint64_t) +
                               (size_t)A * kRefSpheres * sizeof(float4) + 2 * sizeof(int32_t));
 }
@@ -83,5 +85,7 @@ int robotset_arms(const mrpop_robotset *robots);
 
 // Records msg as the calling thread's last error and returns st.
 mrpop_status fail_status(mrpop_status st, const char *msg);
+// The fused-edge limit of run_validator (mrpop_set_fused_edges); returns the previous one.
+int64_t set_fused_edges(int64_t max_edges);
 
 }  // namespace mrpop

@@ -36,6 +36,7 @@ EXPORTED = [
     "mrpop_session_close", "mrpop_session_host_buffers", "mrpop_plan", "mrpop_session_plan",
     "mrpop_drrt_settings_default", "mrpop_drrt_solve", "mrpop_drrt_solve_with", "mrpop_session_drrt",
     "mrpop_batch_shapes", "mrpop_batch_set_shape", "mrpop_drrt_release_pool", "mrpop_session_submit_many",
+    "mrpop_set_fused_edges",
 ]
 KERNEL_KINDS = ("fused", "broad", "narrow")
 NOALLOC_MAX_EDGES = 16384
@@ -188,6 +189,8 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = C.c_int
+    lib.mrpop_set_fused_edges.argtypes = [C.c_int64]
+    lib.mrpop_set_fused_edges.restype = C.c_int64
     lib.mrpop_drrt_release_pool.argtypes = []
     lib.mrpop_drrt_release_pool.restype = C.c_int64
     lib.mrpop_last_error.restype = C.c_char_p

@@ -41,6 +41,17 @@ def _workloads(pkg):
     }
 
 
+@pytest.fixture(autouse=True, params=["small-calls-fused", "all-split"])
+def launch_form(request, pkg):
+    """Every test runs twice: with the default launch form (calls of at most
+    2048 edges as one fused launch) and with every call split into the broad
+    and narrow kernels (mrpop_set_fused_edges(-1))."""
+    lib = pkg.library()
+    prev = lib.mrpop_set_fused_edges(0 if request.param == "small-calls-fused" else -1)
+    yield request.param
+    lib.mrpop_set_fused_edges(prev)
+
+
 @pytest.fixture(scope="module")
 def wls(pkg):
     return _workloads(pkg)
