@@ -254,6 +254,27 @@ def committed_profile(kernel: str, workload: str) -> dict:
     return {}
 
 
+def step_traffic(kt: dict, workload: str, algorithmic_bytes: int, steps: int) -> dict:
+    """DRAM bytes of one step (every kernel of the step, from the committed
+    per-launch captures) against the step's algorithmic bytes (endpoints read,
+    verdicts written)."""
+    per = {}
+    for kind, (launches, _) in kt.items():
+        if not launches:
+            continue
+        b = committed_profile(KERNEL_NAMES[kind], workload).get("dram_bytes_per_launch")
+        if b is None:
+            return {"bytes": None, "algorithmic_bytes": algorithmic_bytes,
+                    "basis": f"no committed capture of {KERNEL_NAMES[kind]} on {workload}"}
+        per[KERNEL_NAMES[kind]] = b * launches / steps
+    total = sum(per.values())
+    return {"bytes": total, "per_kernel": per, "algorithmic_bytes": algorithmic_bytes,
+            "ratio": total / algorithmic_bytes,
+            "basis": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch under application replay with "
+                     "--cache-control none (profiles/<kernel>_<workload>.json); the broad kernel's writes include "
+                     "the write-back of the L2-flush buffer's dirty lines that its own lines evict"}
+
+
 def roofline(kt: dict, flops: dict, peak: float, workload: str, arms: int, spl: int, steps: int,
              sm_mhz: float | None = None) -> dict:
     """Roofline of the kernel with the largest share of device time.
@@ -843,6 +864,7 @@ def run_mine(args, world, rank, local):
         "roofline": roofline(kt, flops, peak, args.workload, arms, spl, args.steps, (clk or {}).get("sm_mhz")),
         "clocks": clk,
     }
+    out["roofline"]["step_traffic"] = step_traffic(kt, args.workload, wl.q0.nbytes + wl.q1.nbytes + n * 5, args.steps)
     if not args.no_e2e:
         ws = pkg.Workspace()
         hq0 = torch.from_numpy(wl.q0).pin_memory()
