@@ -82,8 +82,9 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, util: bool = False):
         self.gpu = gpu_index
+        self.util = util  # also report the median GPU utilisation (long runs)
         self.rows = []
         self.proc = None
 
@@ -120,9 +121,11 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({n for r in self.rows for n, v in zip(names, r[5:9]) if v.lower().startswith("active")})
         util = [float(r[9]) for r in self.rows if len(r) > 9 and r[9].replace(".", "").isdigit()]
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows),
-                "gpu_util_pct_median": statistics.median(util) if util else None}
+        out = {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+               "reasons": reasons, "samples": len(self.rows)}
+        if self.util:
+            out["gpu_util_pct_median"] = statistics.median(util) if util else None
+        return out
 
 
 def host_cpu_times() -> tuple[int, int] | None:
@@ -624,7 +627,7 @@ def run_serving(args, world, rank, local, pkg, torch):
     alone = S.isolated(server, queries[:m], settings)
     before = server.stats()
     barrier(world)
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(local, util=True)
     clocks.start()
     cpu0 = host_cpu_times()
     t0 = time.perf_counter()
