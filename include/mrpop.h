@@ -615,6 +615,15 @@ mrpop_status mrpop_kernel_times(int64_t *launches, double *ms);
  * out needs n6 * n7 / 32 words; 3072 today. */
 mrpop_status mrpop_debug_row5_table(uint32_t *out, int64_t words, int *n6, int *n7);
 
+/* The kernels' bounded wait on a bulk copy, run out on purpose: one CTA waits
+ * on an mbarrier whose bytes no copy will deliver, with limit_ns (at most 2 s)
+ * in place of the kernels' 1 s.  The wait gives up, sets bit 0 of the status
+ * word and returns: *status_out receives the word, *elapsed_ns_out the time
+ * from the wait's start to its giving up (both waits).  Synchronous; the
+ * context stays usable.  Tests the failure path that reports a scene status
+ * (mrpop_scene_status) without a fault or a hang. */
+mrpop_status mrpop_debug_wait_timeout(int64_t limit_ns, uint32_t *status_out, int64_t *elapsed_ns_out);
+
 /* The __cosf/__sinf values the validator uses for inputs x (device arrays). */
 mrpop_status mrpop_debug_trig(const float *x, int64_t n, float *cos_out, float *sin_out,
                               void *stream);

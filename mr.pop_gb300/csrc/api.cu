@@ -619,6 +619,24 @@ __global__ void fk_spheres_kernel(const float *q, long long n, int detailed, con
     }
 }
 
+// One CTA waits, with the kernels' bounded copy wait, on an mbarrier whose
+// expected bytes no copy will deliver: the wait runs out after limit_ns,
+// sets the status bit and returns.
+__global__ void wait_timeout_kernel(unsigned long long limit_ns, unsigned int *status, unsigned long long *elapsed) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mrpop::smem_u32(&bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mrpop::smem_u32(&bar)), "r"(16u)
+                     : "memory");
+    const unsigned long long t0 = mrpop::global_ns();
+    const bool ok = mrpop::copy_wait(&bar, 0, status, limit_ns);
+    if (threadIdx.x == 0) *elapsed = ok ? 0ull : mrpop::global_ns() - t0;
+}
+
 __global__ void trig_kernel(const float *x, long long n, float *c, float *s) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -762,6 +780,30 @@ mrpop_status mrpop_fk_spheres(const mrpop_robotset *robots, int arm, const float
     fk_spheres_kernel<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, (cudaStream_t)stream>>>(q, n, detailed, b, out);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return cuda_fail(err, "fk_spheres: launch");
+    return MRPOP_OK;
+}
+
+mrpop_status mrpop_debug_wait_timeout(int64_t limit_ns, uint32_t *status_out, int64_t *elapsed_ns_out) {
+    if (!status_out || !elapsed_ns_out || limit_ns <= 0 || limit_ns > 2000000000ll)
+        return fail(MRPOP_ERR_INVALID_ARGUMENT, "debug_wait_timeout: limit 1 ns .. 2 s, non-null outputs");
+    unsigned int *d_status = nullptr;
+    unsigned long long *d_elapsed = nullptr;
+    MRPOP_CUDA(cudaMalloc(&d_status, sizeof(unsigned int)), "debug_wait_timeout: status");
+    cudaError_t e = cudaMalloc(&d_elapsed, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(d_status, 0, sizeof(unsigned int));
+    if (e == cudaSuccess) {
+        wait_timeout_kernel<<<1, 32>>>((unsigned long long)limit_ns, d_status, d_elapsed);
+        e = cudaGetLastError();
+    }
+    unsigned int st = 0;
+    unsigned long long el = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&st, d_status, sizeof(st), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&el, d_elapsed, sizeof(el), cudaMemcpyDeviceToHost);
+    cudaFree(d_status);
+    cudaFree(d_elapsed);
+    MRPOP_CUDA(e, "debug_wait_timeout: run");
+    *status_out = st;
+    *elapsed_ns_out = (int64_t)el;
     return MRPOP_OK;
 }
 

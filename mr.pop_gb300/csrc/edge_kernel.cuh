@@ -196,9 +196,45 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
+// The global nanosecond timer.
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Every wait on an mbarrier is bounded in time: a copy that has not completed
+// after kWaitLimitNs is reported (scene status bit) instead of waited for.
+constexpr uint64_t kWaitLimitNs = 1000000000ull;
+
+// Wait for phase `parity` of mbarrier `bar`: true once it has completed,
+// false after limit_ns of global time without it.
+__device__ __forceinline__ bool bar_wait(uint64_t *bar, uint32_t parity, uint64_t limit_ns) {
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
+}
+
+// The wait of a bulk copy into shared memory.  If it runs out, the status bit
+// is set and the copy, which may still be writing this CTA's shared memory,
+// gets a second bounded wait before the caller reports its edges and leaves.
+__device__ __forceinline__ bool copy_wait(uint64_t *bar, uint32_t parity, unsigned int *status, uint64_t limit_ns) {
+    if (bar_wait(bar, parity, limit_ns)) return true;
+    atomicOr(status, 1u);
+    bar_wait(bar, parity, limit_ns);
+    return false;
+}
+
 __device__ __forceinline__ bool stage_scene(float4 *dst, const float4 *src, uint32_t bytes, uint64_t *bar,
                                             unsigned int *status) {
-    bool ok = true;
     if (bytes == 0) return true;
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
@@ -214,28 +250,7 @@ __device__ __forceinline__ bool stage_scene(float4 *dst, const float4 *src, uint
             "l"(src), "r"(bytes), "r"(smem_u32(bar))
             : "memory");
     }
-    uint32_t done = 0;
-    for (int it = 0; it < (1 << 22) && !done; it++) {
-        asm volatile(
-            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
-            : "=r"(done)
-            : "r"(smem_u32(bar))
-            : "memory");
-    }
-    if (!done) {
-        atomicOr(status, 1u);
-        ok = false;
-        // the bulk copy may still be writing this CTA's shared memory: give it
-        // a second bounded wait before the CTA reports its edges and leaves
-        for (int it = 0; it < (1 << 22) && !done; it++) {
-            asm volatile(
-                "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
-                : "=r"(done)
-                : "r"(smem_u32(bar))
-                : "memory");
-        }
-    }
-    return __syncthreads_and(ok);
+    return __syncthreads_and(copy_wait(bar, 0, status, kWaitLimitNs));
 }
 
 __device__ __forceinline__ bool near3(float x, float y, float z, float4 b, float r) {
@@ -1552,29 +1567,7 @@ __device__ __forceinline__ bool stage_bulk(float4 *dst, const float4 *src, uint3
             "l"(src), "r"(bytes), "r"(smem_u32(bar))
             : "memory");
     }
-    uint32_t done = 0;
-    for (int it = 0; it < (1 << 22) && !done; it++) {
-        asm volatile(
-            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-            : "=r"(done)
-            : "r"(smem_u32(bar)), "r"(parity)
-            : "memory");
-    }
-    bool ok = true;
-    if (!done) {
-        atomicOr(status, 1u);
-        ok = false;
-        // the bulk copy may still be writing this CTA's shared memory: give it
-        // a second bounded wait before the CTA reports its edges and leaves
-        for (int it = 0; it < (1 << 22) && !done; it++) {
-            asm volatile(
-                "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-                : "=r"(done)
-                : "r"(smem_u32(bar)), "r"(parity)
-                : "memory");
-        }
-    }
-    return __syncthreads_and(ok);
+    return __syncthreads_and(copy_wait(bar, parity, status, kWaitLimitNs));
 }
 
 template <int A, int SPL, int MODE, bool SEG>

@@ -36,7 +36,7 @@ EXPORTED = [
     "mrpop_session_close", "mrpop_session_host_buffers", "mrpop_plan", "mrpop_session_plan",
     "mrpop_drrt_settings_default", "mrpop_drrt_solve", "mrpop_drrt_solve_with", "mrpop_session_drrt",
     "mrpop_batch_shapes", "mrpop_batch_set_shape", "mrpop_drrt_release_pool", "mrpop_session_submit_many",
-    "mrpop_set_fused_edges",
+    "mrpop_set_fused_edges", "mrpop_debug_wait_timeout",
 ]
 KERNEL_KINDS = ("fused", "broad", "narrow")
 NOALLOC_MAX_EDGES = 16384
@@ -172,6 +172,7 @@ def library(variant: str = "", path: str | Path | None = None) -> C.CDLL:
         "mrpop_session_open": [vp, i32, i64, i32, i64, C.POINTER(vp)],
         "mrpop_session_submit": [vp, C.POINTER(BatchItem)],
         "mrpop_session_submit_many": [vp, C.POINTER(BatchItem), i32],
+        "mrpop_debug_wait_timeout": [i64, C.POINTER(C.c_uint32), C.POINTER(C.c_int64)],
         "mrpop_session_wait": [vp, i64],
         "mrpop_session_close": [vp],
         "mrpop_session_host_buffers": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)],
