@@ -369,8 +369,13 @@ struct GpuChecker {
     uint8_t *valid = nullptr;
     int32_t *first = nullptr;
     size_t cap_f = 0, cap_e = 0;
+    std::vector<cudaStream_t> group_streams;  // one per check of a group (call_many)
 
     ~GpuChecker() {
+        for (cudaStream_t st : group_streams) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
         if (q0) cudaFreeHost(q0);
         if (q1) cudaFreeHost(q1);
         if (valid) cudaFreeHost(valid);
@@ -382,29 +387,8 @@ struct GpuChecker {
         GpuChecker &c = *static_cast<GpuChecker *>(ctx);
         const int dof = 7 * (arm >= 0 ? 1 : mrpop::robotset_arms(c.robots));
         const size_t nf = (size_t)n * dof;
-        if (nf > c.cap_f) {
-            cudaFreeHost(c.q0);
-            cudaFreeHost(c.q1);
-            c.q0 = c.q1 = nullptr;
-            c.cap_f = 0;
-            const size_t cap = std::max(nf, (size_t)1 << 16) * 2;
-            if (cudaHostAlloc(&c.q0, cap * sizeof(float), cudaHostAllocDefault) != cudaSuccess ||
-                cudaHostAlloc(&c.q1, cap * sizeof(float), cudaHostAllocDefault) != cudaSuccess)
-                return mrpop::fail_status(MRPOP_ERR_OUT_OF_MEMORY, "drrt: page-locked staging buffers");
-            c.cap_f = cap;
-        }
-        if ((size_t)n > c.cap_e) {
-            cudaFreeHost(c.valid);
-            cudaFreeHost(c.first);
-            c.valid = nullptr;
-            c.first = nullptr;
-            c.cap_e = 0;
-            const size_t cap = std::max((size_t)n, (size_t)1 << 12) * 2;
-            if (cudaHostAlloc(&c.valid, cap, cudaHostAllocDefault) != cudaSuccess ||
-                cudaHostAlloc(&c.first, cap * sizeof(int32_t), cudaHostAllocDefault) != cudaSuccess)
-                return mrpop::fail_status(MRPOP_ERR_OUT_OF_MEMORY, "drrt: page-locked staging buffers");
-            c.cap_e = cap;
-        }
+        const int rc = c.reserve(nf, (size_t)n);
+        if (rc) return rc;
         std::memcpy(c.q0, a, nf * sizeof(float));
         std::memcpy(c.q1, b, nf * sizeof(float));
         const mrpop_status st = mrpop_validate_edges_host(c.ws, c.scene, c.robots, c.q0, c.q1, n, g, flags, arm, rule,
@@ -412,6 +396,92 @@ struct GpuChecker {
         if (st != MRPOP_OK) return st;
         std::memcpy(valid_out, c.valid, (size_t)n);
         std::memcpy(first_out, c.first, (size_t)n * sizeof(int32_t));
+        return 0;
+    }
+
+    // Page-locked staging of at least nf floats per endpoint array and ne edges.
+    int reserve(size_t nf, size_t ne) {
+        if (nf > cap_f) {
+            cudaFreeHost(q0);
+            cudaFreeHost(q1);
+            q0 = q1 = nullptr;
+            cap_f = 0;
+            const size_t cap = std::max(nf, (size_t)1 << 16) * 2;
+            if (cudaHostAlloc(&q0, cap * sizeof(float), cudaHostAllocDefault) != cudaSuccess ||
+                cudaHostAlloc(&q1, cap * sizeof(float), cudaHostAllocDefault) != cudaSuccess)
+                return mrpop::fail_status(MRPOP_ERR_OUT_OF_MEMORY, "drrt: page-locked staging buffers");
+            cap_f = cap;
+        }
+        if (ne > cap_e) {
+            cudaFreeHost(valid);
+            cudaFreeHost(first);
+            valid = nullptr;
+            first = nullptr;
+            cap_e = 0;
+            const size_t cap = std::max(ne, (size_t)1 << 12) * 2;
+            if (cudaHostAlloc(&valid, cap, cudaHostAllocDefault) != cudaSuccess ||
+                cudaHostAlloc(&first, cap * sizeof(int32_t), cudaHostAllocDefault) != cudaSuccess)
+                return mrpop::fail_status(MRPOP_ERR_OUT_OF_MEMORY, "drrt: page-locked staging buffers");
+            cap_e = cap;
+        }
+        return 0;
+    }
+
+    // A group of checks (a roadmap round's checks of every arm): each is
+    // enqueued on a stream of its own before one wait for all, so that they
+    // run side by side on the device instead of one call after another.  The
+    // kernels read the staged endpoints and write the verdicts in place.
+    static int call_many(void *ctx, const mrpop_check_call *calls, int n) {
+        GpuChecker &c = *static_cast<GpuChecker *>(ctx);
+        const int arms = mrpop::robotset_arms(c.robots);
+        size_t nf = 0, ne = 0;
+        for (int i = 0; i < n; i++) {
+            nf += (size_t)calls[i].n_edges * 7 * (calls[i].arm >= 0 ? 1 : arms);
+            ne += (size_t)calls[i].n_edges;
+        }
+        int rc = c.reserve(nf, ne);
+        if (rc) return rc;
+        const int ns = std::min(n, MRPOP_MAX_ARMS);
+        while ((int)c.group_streams.size() < ns) {
+            cudaStream_t st = nullptr;
+            if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+                return mrpop::fail_status(MRPOP_ERR_CUDA, "drrt: check streams");
+            c.group_streams.push_back(st);
+        }
+        float *d0 = nullptr, *d1 = nullptr;
+        uint8_t *dv = nullptr;
+        int32_t *df = nullptr;
+        if (cudaHostGetDevicePointer((void **)&d0, c.q0, 0) != cudaSuccess ||
+            cudaHostGetDevicePointer((void **)&d1, c.q1, 0) != cudaSuccess ||
+            cudaHostGetDevicePointer((void **)&dv, c.valid, 0) != cudaSuccess ||
+            cudaHostGetDevicePointer((void **)&df, c.first, 0) != cudaSuccess)
+            return mrpop::fail_status(MRPOP_ERR_CUDA, "drrt: staging device pointers");
+        size_t fo = 0, eo = 0;
+        mrpop_status st = MRPOP_OK;
+        for (int i = 0; i < n && st == MRPOP_OK; i++) {
+            const mrpop_check_call &k = calls[i];
+            const size_t f = (size_t)k.n_edges * 7 * (k.arm >= 0 ? 1 : arms);
+            std::memcpy(c.q0 + fo, k.q0, f * sizeof(float));
+            std::memcpy(c.q1 + fo, k.q1, f * sizeof(float));
+            st = mrpop::run_validator(c.scene, c.robots, d0 + fo, d1 + fo, k.n_edges, k.granularity, k.rule, k.range,
+                                      k.flags, k.arm, dv + eo, df + eo, nullptr, nullptr, c.group_streams[i % ns],
+                                      nullptr);
+            fo += f;
+            eo += (size_t)k.n_edges;
+        }
+        cudaError_t e = cudaSuccess;
+        for (int i = 0; i < ns; i++) {
+            const cudaError_t ei = cudaStreamSynchronize(c.group_streams[i]);
+            if (e == cudaSuccess) e = ei;
+        }
+        if (st != MRPOP_OK) return st;
+        if (e != cudaSuccess) return mrpop::fail_status(MRPOP_ERR_CUDA, "drrt: grouped checks");
+        eo = 0;
+        for (int i = 0; i < n; i++) {
+            std::memcpy(calls[i].valid, c.valid + eo, (size_t)calls[i].n_edges);
+            std::memcpy(calls[i].first_hit, c.first + eo, (size_t)calls[i].n_edges * sizeof(int32_t));
+            eo += (size_t)calls[i].n_edges;
+        }
         return 0;
     }
 };
@@ -1593,6 +1663,6 @@ extern "C" mrpop_status mrpop_drrt_solve(const mrpop_scene *scene, const mrpop_r
     chk.scene = scene;
     chk.robots = robots;
     if (mrpop_workspace_create(&chk.ws) != MRPOP_OK) return MRPOP_ERR_CUDA;
-    return mrpop::drrt_run(arms, &GpuChecker::call, nullptr, &chk, true, start, goals, num_goals, settings, path_out,
+    return mrpop::drrt_run(arms, &GpuChecker::call, &GpuChecker::call_many, &chk, true, start, goals, num_goals, settings, path_out,
                            max_waypoints, on_solution, solution_ctx, out);
 }
