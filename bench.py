@@ -741,7 +741,8 @@ def run_planner(args, pkg, torch):
                      "wall_ns": wall, "iterations": r.stats["iterations"], "edges": r.stats["edges_validated"],
                      "validate_ns": r.stats["validate_ns"], "nn_ns": r.stats["nn_ns"],
                      "roadmap_ns": r.stats["roadmap_ns"], "oracle_ns": r.stats["oracle_ns"],
-                     "validate_calls": r.stats["validate_calls"]})
+                     "validate_calls": r.stats["validate_calls"], "check_ns": r.stats["check_ns"],
+                     "check_calls": r.stats["check_calls"]})
     clk = clocks.stop()
     edges = sum(r["edges"] for r in rows)
     out = planner_line(args, "mine", rows, {"validated_edges": edges,
@@ -751,7 +752,11 @@ def run_planner(args, pkg, torch):
                                             max(1, sum(r["kernel_ns"] for r in rows)),
                                             "phase_mean_ms": {k: round(float(np.mean([r[k + "_ns"] for r in rows])) / 1e6, 2)
                                                               for k in ("kernel", "validate", "nn", "roadmap", "oracle")},
-                                            "validate_calls_mean": float(np.mean([r["validate_calls"] for r in rows]))})
+                                            "validate_calls_mean": float(np.mean([r["validate_calls"] for r in rows])),
+                                            "check_ms_mean": {k: round(float(np.mean([r["check_ns"][k] for r in rows])) / 1e6, 2)
+                                                              for k in pkg.drrt.CHECK_KINDS},
+                                            "check_calls_mean": {k: float(np.mean([r["check_calls"][k] for r in rows]))
+                                                                 for k in pkg.drrt.CHECK_KINDS}})
     out["clocks"] = clk
     out["gpu_launches"] = None
     out["per_problem"] = [{k: r[k] for k in ("problem", "solved", "cost", "kernel_ns")} for r in rows]

@@ -548,6 +548,8 @@ typedef struct {
     int64_t nn_ns;            /* inside nearest-neighbour searches                        */
     int64_t oracle_ns;        /* direction oracle and prunes of the attempts (host)       */
     int64_t roadmap_ns;       /* roadmap neighbour searches (host)                        */
+    int64_t check_ns[5];      /* validate time by kind of check: roadmap (single-arm),    */
+    int64_t check_calls[5];   /* extend (composite plain), connect, B-spline, shortcut    */
 } mrpop_drrt_result;
 
 mrpop_status mrpop_drrt_settings_default(mrpop_drrt_settings *out);

@@ -664,13 +664,20 @@ struct Solver {
         give_work(std::move(w));
     }
 
+    // Kind of a check for the statistics: roadmap (single-arm), extend
+    // (composite plain), connect, B-spline, shortcut.
+    static int check_kind(int rule, int arm) { return arm >= 0 ? 0 : rule == MRPOP_RULE_PLAIN ? 1 : 1 + rule; }
+
     int check(int64_t n, int rule, float range, uint32_t flags, int arm, int gran) {
         if (n == 0) return 0;
         ok.resize((size_t)n);
         fh.resize((size_t)n);
         const auto t0 = Clock::now();
         const int rc = validate(vctx, a0.data(), a1.data(), n, gran, rule, range, flags, arm, ok.data(), fh.data());
-        R->validate_ns += ns_since(t0);
+        const int64_t dt = ns_since(t0);
+        R->validate_ns += dt;
+        R->check_ns[check_kind(rule, arm)] += dt;
+        R->check_calls[check_kind(rule, arm)]++;
         R->validate_calls++;
         R->edges_validated += n;
         return rc;
@@ -693,8 +700,11 @@ struct Solver {
                 if (rc) break;
             }
         }
-        R->validate_ns += ns_since(t0);
+        const int64_t dt = ns_since(t0);
+        R->validate_ns += dt;
+        R->check_ns[check_kind(calls[0].rule, calls[0].arm)] += dt;  // a group is of one kind
         for (const auto &c : calls) {
+            R->check_calls[check_kind(c.rule, c.arm)]++;
             R->validate_calls++;
             R->edges_validated += c.n_edges;
         }

@@ -60,10 +60,17 @@ def settings_dict(s: M.DrrtSettingsC) -> dict:
     return {name: getattr(s, name) for name, _ in s._fields_}
 
 
+CHECK_KINDS = ("roadmap", "extend", "connect", "bspline", "shortcut")
+
+
 def _stats(r: M.DrrtResultC, arms: int) -> dict:
-    out = {name: getattr(r, name) for name, _ in r._fields_ if name not in ("roadmap_nodes", "roadmap_edges")}
+    arrays = ("roadmap_nodes", "roadmap_edges", "check_ns", "check_calls")
+    out = {name: getattr(r, name) for name, _ in r._fields_ if name not in arrays}
     out["roadmap_nodes"] = list(r.roadmap_nodes)[:arms]
     out["roadmap_edges"] = list(r.roadmap_edges)[:arms]
+    # validate time and calls by kind of check
+    for key in ("check_ns", "check_calls"):
+        out[key] = dict(zip(CHECK_KINDS, list(getattr(r, key))))
     return out
 
 

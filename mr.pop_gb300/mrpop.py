@@ -109,7 +109,7 @@ class DrrtResultC(C.Structure):
                 ("roadmap_edges", C.c_int64 * 5), ("validate_calls", C.c_int64), ("edges_validated", C.c_int64),
                 ("iterations", C.c_int64), ("wall_ns", C.c_int64), ("kernel_ns", C.c_int64),
                 ("validate_ns", C.c_int64), ("nn_ns", C.c_int64), ("oracle_ns", C.c_int64),
-                ("roadmap_ns", C.c_int64)]
+                ("roadmap_ns", C.c_int64), ("check_ns", C.c_int64 * 5), ("check_calls", C.c_int64 * 5)]
 
 
 CHECK_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_float,
