@@ -1250,12 +1250,13 @@ __device__ __forceinline__ bool broad_decide(const EdgeParams &P, WarpScratch &W
 }
 
 // Detailed phase of one segment: every candidate sample in parallel, one lane
-// each.  Returns the 0-based index of the first colliding sample, or 64.
+// each (samples k0 + 1 ..; k0 = 32 for the second warp of a pair).  Returns
+// the 0-based index (from k0) of the first colliding sample, or 64.
 template <int A, int SPL>
 __device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &W, const float4 *S,
                                               const SceneLayout &L, const float4 *det_tab, int seg, int lane,
                                               const uint64_t (&envw)[SPL], const uint64_t (&selfw)[SPL],
-                                              uint64_t cand_env, uint64_t cand_self) {
+                                              uint64_t cand_env, uint64_t cand_self, int k0 = 0) {
     MRPOP_PHASE_START();
     // sub-group bounds over the segment's samples, from the reference-sphere bounds
     for (int t = lane; t < A * kNumGroups; t += 32) {
@@ -1274,7 +1275,7 @@ __device__ __forceinline__ int narrow_segment(const EdgeParams &P, WarpScratch &
         // every lane walks the arms (warp-wide screening inside); lanes
         // without a candidate sample keep the others company on sample
         // min(k, g), so that the warp's merged bounds stay on real samples
-        const int k = bit + 1 <= P.g ? bit + 1 : P.g;
+        const int k = k0 + bit + 1 <= P.g ? k0 + bit + 1 : P.g;
         bool h = narrow_lane<A>(P, W, S, L, det_tab, seg, k, ew, sw, dE, dS);
         MRPOP_PHASE(P, 5);
         MRPOP_COUNT_LANES(14, dE || dS);
@@ -1358,6 +1359,143 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
     MRPOP_KERNEL_PROLOGUE()
     for (long long e = (long long)blockIdx.x * kWarpsPerBlock + warp; e < P.n_edges; e += nwarps)
         fused_edge<A, SPL>(P, W, S, L, det_tab, e, dof, g, lane, staged);
+}
+
+// ---------------------------------------------------------------------------
+// fused kernel, two warps per edge (granularity above 32, small calls): warp
+// `half` of a pair takes samples 32 * half + 1 .. 32 * half + 32 of every
+// segment, so an edge takes the time of one 32-sample slot instead of two.
+// The thread split's totals and shares are summed over the pair (integers,
+// so in any order), the segment's swept bounds merged with the single-warp
+// kernel's formula, and both warps leave a segment together at its first
+// hit: the verdicts are those of the one-warp kernels.
+// ---------------------------------------------------------------------------
+struct PairShare {
+    int tot[2][2];  // [half] env, self flag totals of the slot
+    int sum[2][2];  // [half] env, self thread shares of the slot
+    int fb[2];      // [half] first colliding sample of the slot (from its k0), or 64
+};
+
+__device__ __forceinline__ void pair_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+
+template <int A>
+__device__ __forceinline__ void fused_edge_pair(const EdgeParams &P, WarpScratch &W, const WarpScratch &Wo,
+                                                const float4 *S, const SceneLayout &L, const float4 *det_tab,
+                                                long long e, int dof, int g, int lane, int half, PairShare &X,
+                                                int bar_id, bool staged) {
+    if (!staged) {
+        if (half == 0 && lane == 0) {
+            P.valid[e] = 0;
+            P.first_hit[e] = -2;
+        }
+        return;
+    }
+    bool too_many;
+    const int nseg = edge_setup(P, W, e, dof, g, lane, too_many);
+    const int nseg_run = too_many ? 0 : nseg;
+    const int k = lane + 1 + 32 * half;
+    int first = 0;
+    for (int seg = 0; seg < nseg_run && first == 0; seg++) {
+        uint64_t ew, sw;
+        broad_sample<A>(P, W, S, L, seg, k <= g ? k : g, false, ew, sw);
+        if (k > g) ew = sw = 0;
+        const int ec = flag_count(ew), sc = flag_count(sw);
+        int te = ec, ts = sc;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            te += __shfl_xor_sync(kFull, te, o);
+            ts += __shfl_xor_sync(kFull, ts, o);
+        }
+        if (lane == 0) {
+            X.tot[half][0] = te;
+            X.tot[half][1] = ts;
+        }
+        pair_sync(bar_id);  // A: both slots' totals and swept bounds written
+        const int tot_env = X.tot[0][0] + X.tot[1][0], tot_self = X.tot[0][1] + X.tot[1][1];
+        if (tot_env > 0 || tot_self > 0) {
+            // the segment's bounds: slot 0's grown by slot 1's (fk_approx_lane's merge)
+            const WarpScratch &W0 = half == 0 ? W : Wo, &W1 = half == 0 ? Wo : W;
+            float4 mg[2];
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int t = lane + 32 * r;
+                if (t < A * kRefSpheres) {
+                    const float4 o = (&W0.rsw[0][0])[t], sv = (&W1.rsw[0][0])[t];
+                    const float ex = sv.x - o.x, ey = sv.y - o.y, ez = sv.z - o.z;
+                    const float d = sqrtf(ex * ex + ey * ey + ez * ez) * 1.0001f;
+                    mg[r] = make_float4(o.x, o.y, o.z, fmaxf(o.w, d + sv.w) + 1e-6f);
+                }
+            }
+            bool cE, cS;
+            if (P.flags & kExactBit) {
+                cE = ec > 0;
+                cS = sc > 0;
+                pair_sync(bar_id);  // B (both warps read the bounds)
+            } else {
+                int de = k <= g ? ref_share(ec, tot_env, g) : 0, ds = k <= g ? ref_share(sc, tot_self, g) : 0;
+                int se = de, ss = ds;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    se += __shfl_xor_sync(kFull, se, o);
+                    ss += __shfl_xor_sync(kFull, ss, o);
+                }
+                if (lane == 0) {
+                    X.sum[half][0] = se;
+                    X.sum[half][1] = ss;
+                }
+                pair_sync(bar_id);  // B: shares written, bounds read
+                if (k == g) {  // the remainder goes to the last sample
+                    de += 4 * g - (X.sum[0][0] + X.sum[1][0]);
+                    ds += 4 * g - (X.sum[0][1] + X.sum[1][1]);
+                }
+                cE = tot_env > 0 && de > 0;
+                cS = tot_self > 0 && ds > 0;
+            }
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int t = lane + 32 * r;
+                if (t < A * kRefSpheres) (&W.rsw[0][0])[t] = mg[r];
+            }
+            const uint64_t cand_env = __ballot_sync(kFull, cE), cand_self = __ballot_sync(kFull, cS);
+            __syncwarp();
+            const uint64_t envw[1] = {ew}, selfw[1] = {sw};
+            const int fb = (cand_env | cand_self)
+                               ? narrow_segment<A, 1>(P, W, S, L, det_tab, seg, lane, envw, selfw, cand_env, cand_self,
+                                                      32 * half)
+                               : 64;
+            if (lane == 0) X.fb[half] = fb;
+            pair_sync(bar_id);  // C: both slots' first hits written
+            const int f0 = X.fb[0], f1 = X.fb[1];
+            if (f0 < 64) first = seg * g + f0 + 1;
+            else if (f1 < 64) first = seg * g + 32 + f1 + 1;
+        }
+        if (P.rule == kRuleConnect) {
+            __syncwarp();
+            for (int d = lane; d < dof; d += 32) W.base[d] = __fadd_rn(W.base[d], W.delta[d]);
+            __syncwarp();
+        }
+        pair_sync(bar_id);  // D: the pair's shared words are read before the next segment writes them
+    }
+    if (half == 0 && lane == 0) {
+        P.valid[e] = (first == 0 && !too_many) ? 1 : 0;
+        P.first_hit[e] = too_many ? -2 : (first ? first : -1);
+        if (P.n_seg_out) P.n_seg_out[e] = nseg;
+    }
+    __syncwarp();
+}
+
+template <int A>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
+    pair_kernel(const __grid_constant__ EdgeParams P) {
+    MRPOP_KERNEL_PROLOGUE()
+    static_assert(kWarpsPerBlock % 2 == 0, "warps come in pairs");
+    __shared__ PairShare X[kWarpsPerBlock / 2];
+    const WarpScratch &Wo = Wall[warp ^ 1];
+    const int pair = warp >> 1, half = warp & 1;
+    (void)nwarps;
+    for (long long e = (long long)blockIdx.x * (kWarpsPerBlock / 2) + pair; e < P.n_edges;
+         e += (long long)gridDim.x * (kWarpsPerBlock / 2))
+        fused_edge_pair<A>(P, W, Wo, S, L, det_tab, e, dof, g, lane, half, X[pair], 1 + pair, staged);
 }
 
 // ---------------------------------------------------------------------------

@@ -8,7 +8,9 @@
 namespace mrpop {
 
 // Which kernel to launch.
-enum KernelKind { kFused = 0, kBroad = 1, kNarrow = 2 };
+// kFusedPair: the fused kernel with two warps per edge (granularity above 32);
+// timed as kFused.
+enum KernelKind { kFused = 0, kBroad = 1, kNarrow = 2, kFusedPair = 3 };
 
 // Launch a validator kernel for `arms` arms (1..5).  smem_bytes: dynamic
 // shared memory (staged scene + per-warp scratch).  Returns the launch error.

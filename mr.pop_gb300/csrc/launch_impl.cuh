@@ -69,6 +69,7 @@ const void *kernel_fn(KernelKind kind, bool seg) {
     switch (kind) {
     case kBroad: return seg ? (const void *)broad_kernel<A, SPL, true> : (const void *)broad_kernel<A, SPL, false>;
     case kNarrow: return seg ? (const void *)narrow_kernel<A, SPL, true> : (const void *)narrow_kernel<A, SPL, false>;
+    case kFusedPair: return (const void *)pair_kernel<A>;
     default: return (const void *)validate_kernel<A, SPL>;
     }
 }
@@ -102,7 +103,8 @@ cudaError_t launch_validate_impl(KernelKind kind, const EdgeParams &p, size_t sm
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long need = (p.n_edges + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    const int per_cta = kind == kFusedPair ? kWarpsPerBlock / 2 : kWarpsPerBlock;  // edges in flight per CTA
+    const long long need = (p.n_edges + per_cta - 1) / per_cta;
     long long grid = (long long)sms * per_sm;
     if (need < grid) grid = need;
     if (grid < 1) grid = 1;
