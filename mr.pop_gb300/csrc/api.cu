@@ -106,7 +106,8 @@ cudaError_t timed_launch(int arms, mrpop::KernelKind kind, const mrpop::EdgePara
         on = g_timing_on;
     }
     if (!on) return mrpop::launch_validate(arms, kind, p, smem, stream);
-    TimedLaunch t{nullptr, nullptr, (int)(kind == mrpop::kFusedPair ? mrpop::kFused : kind)};
+    TimedLaunch t{nullptr, nullptr,
+                  (int)(kind == mrpop::kFusedPair || kind == mrpop::kArmwise ? mrpop::kFused : kind)};
     cudaError_t e = cudaEventCreate(&t.start);
     if (e == cudaSuccess) e = cudaEventCreate(&t.stop);
     if (e == cudaSuccess) e = cudaEventRecord(t.start, stream);
@@ -527,13 +528,13 @@ mrpop_status run_validator(const mrpop_scene *scene, const mrpop_robotset *robot
         p.valid = tmp_valid;
         p.first_hit = tmp_first;
     }
-    // a small call: one fused launch from segment 0, no staging; above 32
-    // samples per segment, two warps per edge (one per 32-sample slot) unless
-    // the flop tally is wanted
+    // a small call: one fused launch from segment 0, no staging; with 3 or
+    // more arms one warp per arm, else above 32 samples per segment two warps
+    // per edge (one per 32-sample slot), unless the flop tally is wanted
     cudaError_t err;
     if (n_edges <= g_fused_edges.load(std::memory_order_relaxed)) {
         p.seg0 = 0;
-        err = timed_launch(A, g > 32 && !flops ? kFusedPair : kFused, p, smem, stream);
+        err = timed_launch(A, flops ? kFused : A >= 3 ? kArmwise : g > 32 ? kFusedPair : kFused, p, smem, stream);
         if (tmp_valid) cudaFreeAsync(tmp_valid, stream);
         if (tmp_first) cudaFreeAsync(tmp_first, stream);
         if (err != cudaSuccess) return cuda_fail(err, "validate: launch");

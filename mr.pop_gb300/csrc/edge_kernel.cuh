@@ -923,17 +923,18 @@ __device__ __forceinline__ void lane_rows(int j, const EdgeParams &P, const Xf &
 // (screened warp-wide per sub-group) and the intra-arm rows of self-flagged
 // joints run as the frames stream by (the first sphere of each row is stashed
 // until its targets come).  Returns true if a test fired.
-template <int A>
+// ONE: only arm one_arm's chain (the arm-per-warp kernel).
+template <int A, bool ONE = false>
 __device__ __forceinline__ bool narrow_lane(const EdgeParams &P, WarpScratch &W, const float4 *S,
                                                 const SceneLayout &L, const float4 *det_tab, int seg, int k,
-                                                uint64_t envw, uint64_t selfw, bool de, bool ds) {
+                                                uint64_t envw, uint64_t selfw, bool de, bool ds, int one_arm = 0) {
     const int lane = threadIdx.x & 31;
     LaneCtx c;
     c.quirk = (!P.single && !(P.flags & kExactBit)) ? 1 : 0;
     c.hit = false;
     MRPOP_PHASE_START();
 #pragma unroll 1
-    for (int a = 0; a < A; a++) {
+    for (int a = ONE ? one_arm : 0; a < (ONE ? one_arm + 1 : A); a++) {
         if (__all_sync(kFull, c.hit || !(de || ds))) break;
         c.em = de ? (uint32_t)(envw >> (8 * a)) & 0xffu : 0u;
         const uint32_t sm = ds ? (uint32_t)(selfw >> (8 * a)) & 0xffu : 0u;
@@ -1029,6 +1030,12 @@ __host__ __device__ __forceinline__ constexpr int grp_ref(int g) {
     return g < 5 ? g : g < 8 ? 5 : g < 9 ? 6 : g < 10 ? 7 : 8;
 }
 
+// Arm pairs (a < b) in order: pair index of (a, b), and the count.
+__host__ __device__ __forceinline__ constexpr int pair_index(int a, int b, int A) {
+    return a * (2 * A - a - 1) / 2 + (b - a - 1);
+}
+__host__ __device__ __forceinline__ constexpr int num_pairs(int A) { return A * (A - 1) / 2; }
+
 // Arm-vs-arm detailed test (panda_four.cuh:415-453) of this lane's sample;
 // every lane of the warp calls it, lanes with act set take part.  For each arm
 // pair (a, b) the 121 sub-group pairs are screened warp-wide, one per lane,
@@ -1039,9 +1046,10 @@ __host__ __device__ __forceinline__ constexpr int grp_ref(int g) {
 // lane stashes arm a's flagged spheres of the surviving groups that can reach
 // arm b's bound (chunks of kCrossStash) and streams arm b's surviving groups
 // against them.  Returns true if a test fired.
-template <int A>
+// SEL: only the arm pairs whose bit (pair_index) is set in `pairs`.
+template <int A, bool SEL = false>
 __device__ __forceinline__ bool cross_swept(const EdgeParams &P, WarpScratch &W, int seg, int k, uint64_t selfw,
-                                            bool act) {
+                                            bool act, uint32_t pairs = 0) {
     const int lane = threadIdx.x & 31;
     bool hit = false;
 #pragma unroll 1
@@ -1051,6 +1059,7 @@ __device__ __forceinline__ bool cross_swept(const EdgeParams &P, WarpScratch &W,
         if (!uj) continue;
 #pragma unroll 1
         for (int b = a + 1; b < A; b++) {
+            if (SEL && !(pairs >> pair_index(a, b, A) & 1u)) continue;
             uint32_t qa = 0, qb = 0;
 #pragma unroll
             for (int r = 0; r < 4; r++) {
@@ -1496,6 +1505,235 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
     for (long long e = (long long)blockIdx.x * (kWarpsPerBlock / 2) + pair; e < P.n_edges;
          e += (long long)gridDim.x * (kWarpsPerBlock / 2))
         fused_edge_pair<A>(P, W, Wo, S, L, det_tab, e, dof, g, lane, half, X[pair], 1 + pair, staged);
+}
+
+// ---------------------------------------------------------------------------
+// fused kernel, one warp per arm (small calls of 2 to 5 arms): a CTA of A
+// warps takes one edge at a time and warp a does arm a's share of it -- its
+// forward kinematics, env and intra-arm screens and exact tests, its detailed
+// chain walk -- and every A-th arm pair of the arm-vs-arm screens and tests,
+// each over every slot of the segment.  Flag words are ORed together in
+// shared memory, the thread split is evaluated from them by every warp (the
+// same integers), and a sample collides when any warp's tests fire: the
+// verdicts are those of the one-warp kernels.  The lower arm's spheres of a
+// pair are read from the warp that placed them instead of being placed again.
+// ---------------------------------------------------------------------------
+struct ArmShare {
+    unsigned long long env[2][32], self[2][32];  // [slot][lane] flag words of the segment
+    unsigned int hits[2];                        // [slot] lanes whose sample collided
+};
+
+template <int A, int SPL>
+__device__ __forceinline__ void armwise_edge(const EdgeParams &P, unsigned char *wbase, const float4 *S,
+                                             const SceneLayout &L, const float4 *det_tab, long long e, int dof,
+                                             int g, int lane, int arm, ArmShare &X, bool staged) {
+    WarpScratch &W = reinterpret_cast<WarpScratch *>(wbase)[arm];
+    if (!staged) {
+        if (arm == 0 && lane == 0) {
+            P.valid[e] = 0;
+            P.first_hit[e] = -2;
+        }
+        return;
+    }
+    bool too_many;
+    const int nseg = edge_setup(P, W, e, dof, g, lane, too_many);
+    const int nseg_run = too_many ? 0 : nseg;
+    const bool do_env = P.flags & kEnvBit, do_self = P.flags & kSelfBit;
+    int first = 0;
+    for (int seg = 0; seg < nseg_run && first == 0; seg++) {
+        if (arm == 0) {
+#pragma unroll
+            for (int t = 0; t < 2; t++) X.env[t][lane] = X.self[t][lane] = 0;
+            if (lane < 2) X.hits[lane] = 0;
+        }
+        __syncthreads();
+        // this arm: placement, swept bounds, env and intra-arm screens (the
+        // slots' spheres stay in broad.cur / broad.low for the pair tests)
+#pragma unroll 1
+        for (int s = 0; s < SPL; s++) {
+            const int k = lane + 1 + 32 * s;
+            float(*sp)[3][32] = s == 0 ? W.broad.cur : W.broad.low;
+            float4 *sw = W.broad.swept[s];
+            fk_approx_lane(P.base[arm], W, P.rule, seg, P.single ? 0 : arm, k <= g ? k : g, sp, lane, sw, W.rsw[arm],
+                           s > 0);
+            uint32_t em = 0, im = 0;
+            if (do_env) {
+                const uint32_t m = env_mask_approx(S, L, P.sc, sp, lane, sw);
+#pragma unroll
+                for (int i = 1; i < kNumApprox; i++)
+                    if (m >> i & 1u) em |= 1u << approx_joint(i);
+            }
+            if (do_self) {
+                const int p1 = lane < 6 ? 0 : lane < 12 ? 1 : lane < 17 ? 2 : 5;
+                const int p2 = lane < 12 ? 5 + lane % 6 : lane == 12 ? 5 : lane < 17 ? lane - 6 : lane - 10;
+                const float4 u1 = sw[p1];
+                const bool c = lane < 21 && near3(u1.x, u1.y, u1.z, sw[p2], u1.w);
+                uint32_t bal = __ballot_sync(kFull, c);
+                while (bal) {
+                    const int t = __ffs(bal) - 1;
+                    bal &= bal - 1;
+                    const int s1 = c_intra_pairs[t][0], s2 = c_intra_pairs[t][1];
+                    if (hit_sphere_sphere(sp[s1][0][lane], sp[s1][1][lane], sp[s1][2][lane], c_approx[s1].w,
+                                          sp[s2][0][lane], sp[s2][1][lane], sp[s2][2][lane], c_approx[s2].w))
+                        im |= 1u << approx_joint(s1);
+                }
+            }
+            if (k <= g) {
+                if (em) atomicOr(&X.env[s][lane], (unsigned long long)em << (8 * arm));
+                if (im) atomicOr(&X.self[s][lane], (unsigned long long)im << (8 * arm));
+            }
+        }
+        __syncthreads();
+        // arm pairs (a, b), a < b, pair index = arm mod A: flags go to arm a
+        // (panda_four.cuh:178-214); screened by the slot's swept bounds
+        if (A > 1 && do_self) {
+            const WarpScratch *Wa = reinterpret_cast<const WarpScratch *>(wbase);
+#pragma unroll 1
+            for (int a = 0; a < A - 1; a++)
+#pragma unroll 1
+                for (int b = a + 1; b < A; b++) {
+                    if (pair_index(a, b, A) % A != arm) continue;
+#pragma unroll 1
+                    for (int s = 0; s < SPL; s++) {
+                        const int k = lane + 1 + 32 * s;
+                        const float4 *swa = Wa[a].broad.swept[s], *swb = Wa[b].broad.swept[s];
+                        uint32_t bal[4];
+#pragma unroll
+                        for (int r = 0; r < 4; r++) {
+                            const int t = 32 * r + lane;
+                            const int i = t / kNumApprox, j = t - kNumApprox * i;
+                            bal[r] = __ballot_sync(kFull, t < kNumApprox * kNumApprox &&
+                                                              near3(swa[i].x, swa[i].y, swa[i].z, swb[j], swa[i].w));
+                        }
+                        if (!(bal[0] | bal[1] | bal[2] | bal[3])) continue;
+                        const float(*low)[3][32] = s == 0 ? Wa[a].broad.cur : Wa[a].broad.low;
+                        const float(*cur)[3][32] = s == 0 ? Wa[b].broad.cur : Wa[b].broad.low;
+                        uint32_t am = 0;
+#pragma unroll
+                        for (int r = 0; r < 4; r++) {
+                            uint32_t q = bal[r];
+                            while (q) {
+                                const int t = 32 * r + __ffs(q) - 1;
+                                q &= q - 1;
+                                const int i = t / kNumApprox, j = t - kNumApprox * i;
+                                if (hit_sphere_sphere(low[i][0][lane], low[i][1][lane], low[i][2][lane],
+                                                      c_approx[i].w, cur[j][0][lane], cur[j][1][lane],
+                                                      cur[j][2][lane], c_approx[j].w))
+                                    am |= 1u << approx_joint(i);
+                            }
+                        }
+                        if (am && k <= g) atomicOr(&X.self[s][lane], (unsigned long long)am << (8 * a));
+                    }
+                }
+        }
+        __syncthreads();
+        // the thread split, from the ORed words (every warp alike)
+        uint64_t envw[SPL], selfw[SPL];
+        int envc[SPL], selfc[SPL], tot_env = 0, tot_self = 0;
+#pragma unroll
+        for (int s = 0; s < SPL; s++) {
+            envw[s] = X.env[s][lane];
+            selfw[s] = X.self[s][lane];
+            envc[s] = flag_count(envw[s]);
+            selfc[s] = flag_count(selfw[s]);
+            tot_env += envc[s];
+            tot_self += selfc[s];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            tot_env += __shfl_xor_sync(kFull, tot_env, o);
+            tot_self += __shfl_xor_sync(kFull, tot_self, o);
+        }
+        if (tot_env > 0 || tot_self > 0) {
+            uint64_t cand_env = 0, cand_self = 0;
+            if (P.flags & kExactBit) {
+#pragma unroll
+                for (int s = 0; s < SPL; s++) {
+                    cand_env |= (uint64_t)__ballot_sync(kFull, envc[s] > 0) << (32 * s);
+                    cand_self |= (uint64_t)__ballot_sync(kFull, selfc[s] > 0) << (32 * s);
+                }
+            } else {
+                int de[SPL], ds[SPL], sum_e = 0, sum_s = 0;
+#pragma unroll
+                for (int s = 0; s < SPL; s++) {
+                    const int k = lane + 1 + 32 * s;
+                    de[s] = k <= g ? ref_share(envc[s], tot_env, g) : 0;
+                    ds[s] = k <= g ? ref_share(selfc[s], tot_self, g) : 0;
+                    sum_e += de[s];
+                    sum_s += ds[s];
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    sum_e += __shfl_xor_sync(kFull, sum_e, o);
+                    sum_s += __shfl_xor_sync(kFull, sum_s, o);
+                }
+#pragma unroll
+                for (int s = 0; s < SPL; s++) {
+                    const int k = lane + 1 + 32 * s;
+                    if (k == g) {  // the remainder goes to the last sample
+                        de[s] += 4 * g - sum_e;
+                        ds[s] += 4 * g - sum_s;
+                    }
+                    cand_env |= (uint64_t)__ballot_sync(kFull, tot_env > 0 && de[s] > 0) << (32 * s);
+                    cand_self |= (uint64_t)__ballot_sync(kFull, tot_self > 0 && ds[s] > 0) << (32 * s);
+                }
+            }
+            // the segment's sub-group bounds for the arm-vs-arm screens, from
+            // every arm's reference-sphere bounds (each warp's own row)
+            const WarpScratch *Wa = reinterpret_cast<const WarpScratch *>(wbase);
+            for (int t = lane; t < A * kNumGroups; t += 32) {
+                const int a = t / kNumGroups, gg = t - kNumGroups * a;
+                const float4 u = Wa[a].rsw[a][grp_ref(gg)];
+                W.gbd[a][gg] = make_float4(u.x, u.y, u.z, u.w + P.gofs[gg]);
+            }
+            __syncwarp();
+            uint32_t my_pairs = 0;
+            for (int pp = arm; pp < num_pairs(A); pp += A) my_pairs |= 1u << pp;
+#pragma unroll 1
+            for (int s = 0; s < SPL; s++) {
+                const int bit = lane + 32 * s;
+                const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
+                const int k = bit + 1 <= g ? bit + 1 : g;
+                bool h = narrow_lane<A, true>(P, W, S, L, det_tab, seg, k, envw[s], selfw[s], dE, dS, arm);
+                if (A > 1 && my_pairs && __any_sync(kFull, dS && !h))
+                    h |= cross_swept<A, true>(P, W, seg, k, selfw[s], dS && !h, my_pairs);
+                const unsigned int hb = __ballot_sync(kFull, h);
+                if (lane == 0 && hb) atomicOr(&X.hits[s], hb);
+            }
+            __syncthreads();
+            const uint64_t hits = (uint64_t)X.hits[0] | (SPL > 1 ? (uint64_t)X.hits[1] << 32 : 0ull);
+            if (hits) first = seg * g + __ffsll((long long)hits);
+        }
+        if (P.rule == kRuleConnect) {
+            __syncwarp();
+            for (int d = lane; d < dof; d += 32) W.base[d] = __fadd_rn(W.base[d], W.delta[d]);
+            __syncwarp();
+        }
+        __syncthreads();  // the shared words are read before the next segment clears them
+    }
+    if (arm == 0 && lane == 0) {
+        P.valid[e] = (first == 0 && !too_many) ? 1 : 0;
+        P.first_hit[e] = too_many ? -2 : (first ? first : -1);
+        if (P.n_seg_out) P.n_seg_out[e] = nseg;
+    }
+}
+
+template <int A, int SPL>
+__global__ void __launch_bounds__(32 * A) armwise_kernel(const __grid_constant__ EdgeParams P) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ float4 det_tab[kNumDet];
+    __shared__ ArmShare X;
+    const SceneLayout L = scene_layout(P.sc);
+    const float4 *S = reinterpret_cast<const float4 *>(smem_raw);
+    const int arm = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < kNumDet; i += blockDim.x) det_tab[i] = c_det[i];
+    const bool staged = stage_scene(reinterpret_cast<float4 *>(smem_raw), P.scene,
+                                    (uint32_t)(L.total * sizeof(float4)), &bar, P.status);
+    unsigned char *wbase = smem_raw + (size_t)L.total * sizeof(float4);
+    const int dof = 7 * (P.single ? 1 : A);
+    for (long long e = blockIdx.x; e < P.n_edges; e += gridDim.x)
+        armwise_edge<A, SPL>(P, wbase, S, L, det_tab, e, dof, P.g, lane, arm, X, staged);
 }
 
 // ---------------------------------------------------------------------------

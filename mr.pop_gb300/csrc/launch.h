@@ -10,7 +10,8 @@ namespace mrpop {
 // Which kernel to launch.
 // kFusedPair: the fused kernel with two warps per edge (granularity above 32);
 // timed as kFused.
-enum KernelKind { kFused = 0, kBroad = 1, kNarrow = 2, kFusedPair = 3 };
+// kArmwise: the fused kernel with one warp per arm; timed as kFused.
+enum KernelKind { kFused = 0, kBroad = 1, kNarrow = 2, kFusedPair = 3, kArmwise = 4 };
 
 // Launch a validator kernel for `arms` arms (1..5).  smem_bytes: dynamic
 // shared memory (staged scene + per-warp scratch).  Returns the launch error.

@@ -37,7 +37,7 @@ LaunchState *launch_state(const void *fn) {
 // Raises the kernel's dynamic shared-memory attribute to smem_bytes if it is
 // lower (it only grows, so launches racing on other threads stay valid), and
 // returns the resident CTAs per SM at that size when blocks_per_sm is given.
-cudaError_t prepare_kernel(const void *fn, size_t smem_bytes, int *blocks_per_sm) {
+cudaError_t prepare_kernel(const void *fn, size_t smem_bytes, int *blocks_per_sm, int threads = 32 * kWarpsPerBlock) {
     std::lock_guard<std::mutex> lk(launch_mu);
     LaunchState *st = launch_state(fn);
     if (!st || smem_bytes > st->attr_bytes) {
@@ -48,7 +48,7 @@ cudaError_t prepare_kernel(const void *fn, size_t smem_bytes, int *blocks_per_sm
     if (!blocks_per_sm) return cudaSuccess;
     if (!st || st->occ_bytes != smem_bytes || st->occ_blocks == 0) {
         int nb = 0;
-        const cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * kWarpsPerBlock, smem_bytes);
+        const cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem_bytes);
         if (err != cudaSuccess) return err;
         *blocks_per_sm = nb > 0 ? nb : 1;
         if (st) {
@@ -70,6 +70,7 @@ const void *kernel_fn(KernelKind kind, bool seg) {
     case kBroad: return seg ? (const void *)broad_kernel<A, SPL, true> : (const void *)broad_kernel<A, SPL, false>;
     case kNarrow: return seg ? (const void *)narrow_kernel<A, SPL, true> : (const void *)narrow_kernel<A, SPL, false>;
     case kFusedPair: return (const void *)pair_kernel<A>;
+    case kArmwise: return (const void *)armwise_kernel<A, SPL>;
     default: return (const void *)validate_kernel<A, SPL>;
     }
 }
@@ -94,6 +95,26 @@ const void *batch_fn(int mode, bool seg) {
 // CTAs than edges / kWarpsPerBlock.
 template <int A>
 cudaError_t launch_validate_impl(KernelKind kind, const EdgeParams &p, size_t smem_bytes, cudaStream_t stream) {
+    if (kind == kArmwise) {
+        // A warps per CTA, one edge per CTA at a time; only while every edge
+        // of the call has a CTA of its own (a second round of edges would
+        // double the call's time: then the pair or one-warp kernel)
+        const size_t arm_smem =
+            smem_bytes - (size_t)kWarpsPerBlock * sizeof(WarpScratch) + (size_t)A * sizeof(WarpScratch);
+        const void *fn = p.g > 32 ? (const void *)armwise_kernel<A, 2> : (const void *)armwise_kernel<A, 1>;
+        int per_sm = 0, dev = 0, sms = 0;
+        const cudaError_t err = prepare_kernel(fn, arm_smem, &per_sm, 32 * A);
+        if (err != cudaSuccess) return err;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const long long resident = (long long)sms * (per_sm > 0 ? per_sm : 1);
+        if (p.n_edges <= resident) {
+            void *args[] = {(void *)&p};
+            return cudaLaunchKernel(fn, dim3((unsigned)(p.n_edges > 0 ? p.n_edges : 1)), dim3(32 * A), args, arm_smem,
+                                    stream);
+        }
+        kind = p.g > 32 ? kFusedPair : kFused;
+    }
     const int spl = p.g > 32 ? 2 : 1;
     const bool seg = p.rule != 0;
     const void *fn = spl == 2 ? kernel_fn<A, 2>(kind, seg) : kernel_fn<A, 1>(kind, seg);
