@@ -59,7 +59,7 @@ constexpr int kRoadmapIters = 230;        // ROADMAP_BUILD_ITER (roadmap_interio
 constexpr int kMaxRoadmap = 100000;       // MAX_ROADMAP_SIZE (roadmap_interior.cuh:21)
 constexpr float kExistSq = 1e-5f;         // a node "already exists" within this squared distance (:526)
 constexpr int kShortcutSpan = 16;         // the simplify kernel's 16 blocks (pop_planner.cu:911)
-constexpr int kNNChunk = 128;             // queries per nearest-neighbour launch
+constexpr int kNNChunk = 32;              // queries per nearest-neighbour job (one grid row of blocks)
 
 // splitmix64 (Steele, Lea, Flood 2014) streams; uniform() is in (0, 1).
 struct Rng {
@@ -243,7 +243,7 @@ struct Tree {
 //   mode 1 (connect search): sqrt(distance) < bound (pop_planner.cu:642)
 // One thread per node (held in registers); queries in shared memory.
 // ---------------------------------------------------------------------------
-constexpr int kNNMaxJobs = 8;
+constexpr int kNNMaxJobs = 64;
 
 // One launch for the query chunks of both trees: job j = (tree, first query,
 // queries); blockIdx.y is the job, blockIdx.x a block of 256 nodes.
@@ -256,37 +256,69 @@ struct NNLaunch {
     int tree[kNNMaxJobs], q0[kNNMaxJobs], nq[kNNMaxJobs];
 };
 
+// A thread holds kNNNodes nodes; the query rows are read from shared memory as
+// float4.  The searches are latency-bound (trees of a few thousand nodes leave
+// most of the device idle), so queries go in jobs of kNNChunk, each job a row
+// of blocks: more blocks, fewer queries per thread.
+constexpr int kNNNodes = 1;
+
 template <int DIM>
 __global__ void __launch_bounds__(256) tree_nn_kernel(const __grid_constant__ NNLaunch L) {
-    __shared__ float sx[kNNChunk * DIM];
+    constexpr int DIMP = (DIM + 3) / 4 * 4;  // query row stride (float4 loads)
+    __shared__ __align__(16) float sx[kNNChunk * DIMP];
     __shared__ float sb[kNNChunk];
     __shared__ unsigned long long red[8][kNNChunk];
     const int job = blockIdx.y, t = L.tree[job], nq = L.nq[job];
     const long long n = L.n[t];
-    if ((long long)blockIdx.x * blockDim.x >= n) return;  // whole block past this tree's nodes
+    const long long i0 = (long long)blockIdx.x * blockDim.x * kNNNodes + threadIdx.x;
+    if ((long long)blockIdx.x * blockDim.x * kNNNodes >= n) return;  // whole block past this tree's nodes
     const float *qx = L.qx + (size_t)L.q0[job] * DIM, *qb = L.qb + L.q0[job];
-    for (int i = threadIdx.x; i < nq * DIM; i += blockDim.x) sx[i] = qx[i];
-    for (int i = threadIdx.x; i < nq; i += blockDim.x) sb[i] = qb[i];
+    for (int j = threadIdx.x; j < nq * DIMP; j += blockDim.x) {
+        const int q = j / DIMP, d = j - q * DIMP;
+        sx[j] = d < DIM ? qx[q * DIM + d] : 0.0f;
+    }
+    for (int j = threadIdx.x; j < nq; j += blockDim.x) sb[j] = qb[j];
     __syncthreads();
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool have = i < n;
-    const float *row = L.rows[t] + (size_t)(have ? i : 0) * (DIM + 1);
-    float x[DIM];
+    float x[kNNNodes][DIM], c[kNNNodes];
+    bool have[kNNNodes];
 #pragma unroll
-    for (int d = 0; d < DIM; d++) x[d] = have ? row[d] : 0.0f;
-    const float c = have ? row[DIM] : 0.0f;
+    for (int m = 0; m < kNNNodes; m++) {
+        const long long i = i0 + (long long)m * blockDim.x;
+        have[m] = i < n;
+        const float *row = L.rows[t] + (size_t)(have[m] ? i : 0) * (DIM + 1);
+#pragma unroll
+        for (int d = 0; d < DIM; d++) x[m][d] = have[m] ? row[d] : 0.0f;
+        c[m] = have[m] ? row[DIM] : 0.0f;
+    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const float4 *sx4 = reinterpret_cast<const float4 *>(sx);
     for (int q = 0; q < nq; q++) {
-        unsigned long long key = ~0ull;
-        if (have) {
-            float s = 0.0f;
+        float s[kNNNodes];
 #pragma unroll
-            for (int d = 0; d < DIM; d++) {
-                const float u = x[d] - sx[q * DIM + d];
-                s = __fmaf_rn(u, u, s);
+        for (int m = 0; m < kNNNodes; m++) s[m] = 0.0f;
+#pragma unroll
+        for (int d4 = 0; d4 < DIMP / 4; d4++) {
+            const float4 v = sx4[q * (DIMP / 4) + d4];
+            const float qv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                const int d = 4 * d4 + r;
+                if (d < DIM) {
+#pragma unroll
+                    for (int m = 0; m < kNNNodes; m++) {
+                        const float u = x[m][d] - qv[r];
+                        s[m] = __fmaf_rn(u, u, s[m]);
+                    }
+                }
             }
-            const bool ok = (L.mode == 0 ? c < sb[q] : sqrtf(s) < sb[q]) && s < FLT_MAX;
-            if (ok) key = ((unsigned long long)__float_as_uint(s) << 32) | (unsigned long long)(unsigned)i;
+        }
+        unsigned long long key = ~0ull;
+#pragma unroll
+        for (int m = 0; m < kNNNodes; m++) {
+            const bool ok = have[m] && (L.mode == 0 ? c[m] < sb[q] : sqrtf(s[m]) < sb[q]) && s[m] < FLT_MAX;
+            const unsigned long long k = ((unsigned long long)__float_as_uint(s[m]) << 32) |
+                                         (unsigned long long)(unsigned)(i0 + (long long)m * blockDim.x);
+            if (ok && k < key) key = k;
         }
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
@@ -305,7 +337,8 @@ __global__ void __launch_bounds__(256) tree_nn_kernel(const __grid_constant__ NN
 }
 
 cudaError_t launch_tree_nn(int dim, const NNLaunch &L, int njobs, long long max_n, cudaStream_t s) {
-    const dim3 grid((unsigned)std::max<long long>(1, (max_n + 255) / 256), (unsigned)njobs);
+    const long long per_block = 256LL * kNNNodes;
+    const dim3 grid((unsigned)std::max<long long>(1, (max_n + per_block - 1) / per_block), (unsigned)njobs);
     switch (dim) {
         case 7: tree_nn_kernel<7><<<grid, 256, 0, s>>>(L); break;
         case 14: tree_nn_kernel<14><<<grid, 256, 0, s>>>(L); break;
@@ -730,7 +763,7 @@ struct Solver {
     // For both trees at once: idx[t][q] = the node of tree t nearest to
     // x[t][q] that passes the filter (lowest squared distance, then lowest
     // index), or -1; sqd[t][q] = its squared distance.  One upload, one launch
-    // per tree and chunk of 128 queries, one read-back.
+    // for every job of 32 queries of both trees, one read-back.
     struct NNJob {
         std::vector<float> x, bound;
         std::vector<int> who, idx;
