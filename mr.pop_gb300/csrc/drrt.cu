@@ -59,7 +59,7 @@ constexpr int kRoadmapIters = 230;        // ROADMAP_BUILD_ITER (roadmap_interio
 constexpr int kMaxRoadmap = 100000;       // MAX_ROADMAP_SIZE (roadmap_interior.cuh:21)
 constexpr float kExistSq = 1e-5f;         // a node "already exists" within this squared distance (:526)
 constexpr int kShortcutSpan = 16;         // the simplify kernel's 16 blocks (pop_planner.cu:911)
-constexpr int kNNChunk = 32;              // queries per nearest-neighbour job (one grid row of blocks)
+constexpr int kNNChunk = 16;              // queries per nearest-neighbour job (one grid row of blocks)
 
 // splitmix64 (Steele, Lea, Flood 2014) streams; uniform() is in (0, 1).
 struct Rng {
