@@ -763,7 +763,7 @@ struct Solver {
     // For both trees at once: idx[t][q] = the node of tree t nearest to
     // x[t][q] that passes the filter (lowest squared distance, then lowest
     // index), or -1; sqd[t][q] = its squared distance.  One upload, one launch
-    // for every job of 32 queries of both trees, one read-back.
+    // for every job of kNNChunk queries of both trees, one read-back.
     struct NNJob {
         std::vector<float> x, bound;
         std::vector<int> who, idx;
