@@ -1925,6 +1925,9 @@ struct BatchParams {
 // Batch kernel modes: the split pipeline's two kernels, and the fused kernel
 // that finishes segmented edges after the split rounds.
 constexpr int kBatchBroad = 0, kBatchNarrow = 1, kBatchFused = 2;
+// Batch mode of the arm-per-warp kernel (whole edges from segment 0, a CTA of
+// A warps per edge): batch_armwise_kernel.
+constexpr int kBatchArmwise = 3;
 
 // One bulk copy of `bytes` from global to shared memory, completed on `bar`
 // in phase `parity`; bounded wait.  Every thread of the CTA calls it after a
@@ -2009,6 +2012,56 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
             else fused_edge<A, SPL>(P, W, S, L, det_tab, e, dof, P.g, lane, staged);
         }
         __syncthreads(); // every warp is done with this chunk (and instance)
+    }
+}
+
+// Batch form of armwise_kernel: the CTA takes chunks (of single edges) from the
+// launch's counter, stages each instance's parameters and scene as
+// batch_kernel does, and runs the arm-per-warp body on every edge of the chunk.
+template <int A, int SPL>
+__global__ void __launch_bounds__(32 * A) batch_armwise_kernel(const __grid_constant__ BatchParams B) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ float4 det_tab[kNumDet];
+    __shared__ __align__(16) EdgeParams Ps;
+    __shared__ ArmShare X;
+    __shared__ int s_chunk;
+    const int arm = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < kNumDet; i += blockDim.x) det_tab[i] = c_det[i];
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int item = -1;
+    uint32_t parity = 0;
+    bool staged = false;
+    for (;;) {
+        if (threadIdx.x == 0) s_chunk = (int)atomicAdd(B.work, 1ull);
+        __syncthreads();
+        const int c = s_chunk;
+        if (c >= B.n_chunks) break;
+        const int4 ch = B.chunks[c];
+        if (ch.x != item) {
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(B.items + ch.x);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&Ps);
+            for (int i = threadIdx.x; i < (int)(sizeof(EdgeParams) / 4); i += blockDim.x) dst[i] = src[i];
+            __syncthreads();
+            const uint32_t bytes = (uint32_t)(scene_layout(Ps.sc).total * sizeof(float4));
+            staged = true;
+            if (bytes) {
+                staged = stage_bulk(reinterpret_cast<float4 *>(smem_raw), Ps.scene, bytes, &bar, parity, Ps.status);
+                parity ^= 1u;
+            }
+            item = ch.x;
+        }
+        const SceneLayout L = scene_layout(Ps.sc);
+        const float4 *S = reinterpret_cast<const float4 *>(smem_raw);
+        unsigned char *wbase = smem_raw + (size_t)L.total * sizeof(float4);
+        const int dof = 7 * (Ps.single ? 1 : A);
+        for (int k = 0; k < ch.z; k++)
+            armwise_edge<A, SPL>(Ps, wbase, S, L, det_tab, (long long)ch.y + k, dof, Ps.g, lane, arm, X, staged);
+        __syncthreads();  // every warp is done with this chunk (and instance)
     }
 }
 

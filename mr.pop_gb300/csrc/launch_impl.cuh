@@ -77,6 +77,7 @@ const void *kernel_fn(KernelKind kind, bool seg) {
 
 template <int A, int SPL>
 const void *batch_fn(int mode, bool seg) {
+    if (mode == kBatchArmwise) return (const void *)batch_armwise_kernel<A, SPL>;
     if (!seg) {
         switch (mode) {
         case kBatchBroad: return (const void *)batch_kernel<A, SPL, kBatchBroad, false>;
@@ -151,8 +152,16 @@ cudaError_t launch_validate_impl(KernelKind kind, const EdgeParams &p, size_t sm
 // Batch kernels: the attribute is raised when a batch is created (or tuned),
 // so launches (and graph capture) do not touch it.  A CTA may have fewer warps
 // than kWarpsPerBlock (the kernel indexes its per-warp scratch by warp).
+// The arm-per-warp batch kernel runs A warps per CTA whatever `warps` says:
+// its CTA size and shared memory (callers give the size for `warps` warps).
+inline void armwise_shape(int A, size_t &smem_bytes, int &warps) {
+    smem_bytes = smem_bytes - (size_t)warps * sizeof(WarpScratch) + (size_t)A * sizeof(WarpScratch);
+    warps = A;
+}
+
 template <int A>
 cudaError_t batch_occupancy_impl(int mode, bool seg, int spl, size_t smem_bytes, int warps, int *blocks_per_sm) {
+    if (mode == kBatchArmwise) armwise_shape(A, smem_bytes, warps);
     const void *fn = spl == 2 ? batch_fn<A, 2>(mode, seg) : batch_fn<A, 1>(mode, seg);
     cudaError_t err = prepare_kernel(fn, smem_bytes, nullptr);
     if (err != cudaSuccess) return err;
@@ -165,6 +174,7 @@ cudaError_t batch_occupancy_impl(int mode, bool seg, int spl, size_t smem_bytes,
 template <int A>
 cudaError_t launch_batch_impl(int mode, bool seg, int spl, const BatchParams &b, size_t smem_bytes, int grid,
                               int warps, cudaStream_t stream) {
+    if (mode == kBatchArmwise) armwise_shape(A, smem_bytes, warps);
     const void *fn = spl == 2 ? batch_fn<A, 2>(mode, seg) : batch_fn<A, 1>(mode, seg);
     void *args[] = {(void *)&b};
     return cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(32 * warps), args, smem_bytes, stream);

@@ -48,6 +48,10 @@ constexpr int kWaveCtasPerSm = 3;
 // 2 * kSegRounds + 1 for segmented rules): launch latency and the serial
 // dependency between the split kernels dominate small waves.
 constexpr int64_t kFusedEdgesDefault = 4096;
+// Groups of 3 to 5 arms with at most this many edges in a wave run the
+// arm-per-warp kernel (a CTA of A warps per edge; about as many edges as its
+// CTAs resident on the device at 5 arms).
+constexpr int64_t kArmwiseEdges = 456;
 // Work counters per group and wave: one per launch (split rounds + fused
 // tail), zeroed together with the parameter upload so that no launch needs a
 // memset of its own.
@@ -217,6 +221,7 @@ cudaError_t launch_wave(mrpop_server *s, mrpop_server::Slot &slot) {
         int p0 = 0, np = 0, c0 = 0, nc = 0;
         int64_t edges = 0;
         size_t smem = 0;
+        bool armwise = false;
     };
     // chunk size of this wave (a multiple of the warps per CTA)
     int64_t total = 0;
@@ -230,6 +235,9 @@ cudaError_t launch_wave(mrpop_server *s, mrpop_server::Slot &slot) {
         if (n <= s->cfg.max_wave_chunks || chunk >= kChunkEdges) break;
         chunk = std::min(kChunkEdges, chunk + mrpop::kWarpsPerBlock);
     }
+    // chunks of every group at the wave's chunk size (they fit the table)
+    int64_t left = 0;
+    for (const auto &st : slot.steps) left += (st.p.n_edges + chunk - 1) / chunk;
     Range ranges[kGroupKeys];
     int np = 0, nc = 0;
     for (int key = 0; key < kGroupKeys; key++) {
@@ -238,12 +246,24 @@ cudaError_t launch_wave(mrpop_server *s, mrpop_server::Slot &slot) {
         Range &r = ranges[key];
         r.p0 = np;
         r.c0 = nc;
+        int64_t edges = 0, at_chunk = 0;
+        for (const auto &st : slot.steps)
+            if (st.arms == arms && st.spl == spl && st.seg == seg) {
+                edges += st.p.n_edges;
+                at_chunk += (st.p.n_edges + chunk - 1) / chunk;
+            }
+        left -= at_chunk;
+        // a small group of 3 to 5 arms runs one warp per arm, one edge per
+        // CTA: its chunks are single edges, if the table has room for them
+        r.armwise = arms >= 3 && edges <= kArmwiseEdges && edges <= s->cfg.fused_edges &&
+                    nc + edges + left <= s->cfg.max_wave_chunks;
+        const int cs = r.armwise ? 1 : chunk;
         for (const auto &st : slot.steps) {
             if (st.arms != arms || st.spl != spl || st.seg != seg) continue;
             const int item = np - r.p0;
             h_params[np++] = st.p;
-            for (int64_t e0 = 0; e0 < st.p.n_edges; e0 += chunk)
-                h_chunks[nc++] = make_int4(item, (int)e0, (int)std::min<int64_t>(chunk, st.p.n_edges - e0), 0);
+            for (int64_t e0 = 0; e0 < st.p.n_edges; e0 += cs)
+                h_chunks[nc++] = make_int4(item, (int)e0, (int)std::min<int64_t>(cs, st.p.n_edges - e0), 0);
             r.smem = std::max(r.smem, st.smem);
             r.edges += st.p.n_edges;
         }
@@ -264,6 +284,10 @@ cudaError_t launch_wave(mrpop_server *s, mrpop_server::Slot &slot) {
         unsigned long long *work = d_work + (size_t)kCountersPerGroup * key;
         const mrpop::EdgeParams *items = d_params + r.p0;
         const int4 *chunks = d_chunks + r.c0;
+        if (r.armwise) {
+            err = launch_one(s, arms, seg, spl, r.smem, mrpop::kBatchArmwise, 0, items, chunks, r.nc, work, slot.stream);
+            continue;
+        }
         if (r.edges <= s->cfg.fused_edges) {
             err = launch_one(s, arms, seg, spl, r.smem, mrpop::kBatchFused, 0, items, chunks, r.nc, work, slot.stream);
             continue;
