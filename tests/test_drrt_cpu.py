@@ -87,6 +87,13 @@ def test_oracle_driven_solve_follows_the_reference_structure(pkg, lib_path, orc)
     assert (False, 3, 3, False) in kinds
     assert r.stats["validate_calls"] == len(calls)
     assert all(n > 0 for n in r.stats["roadmap_nodes"]) and all(e > 0 for e in r.stats["roadmap_edges"])
+    # calls by kind: roadmap (single-arm), extend (composite plain), connect, B-spline, shortcut
+    by_kind = r.stats["check_calls"]
+    assert sum(by_kind.values()) == len(calls)
+    assert by_kind["roadmap"] == sum(1 for _, _, _, _, arm in calls if arm >= 0)
+    assert by_kind["extend"] == sum(1 for _, _, rule, _, arm in calls if arm < 0 and rule == 0)
+    assert by_kind["connect"] == sum(1 for _, _, rule, _, arm in calls if arm < 0 and rule == 1)
+    assert all(r.stats["check_ns"][k] >= 0 for k in by_kind)
 
 
 def test_oracle_driven_solve_is_deterministic(pkg, lib_path, orc):
