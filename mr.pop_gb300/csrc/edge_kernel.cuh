@@ -1521,7 +1521,26 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, MRPOP_MIN_BLOCKS)
 struct ArmShare {
     unsigned long long env[2][32], self[2][32];  // [slot][lane] flag words of the segment
     unsigned int hits[2];                        // [slot] lanes whose sample collided
+    unsigned int next[3];                        // arm pairs handed out: broad, narrow slot 0, slot 1
 };
+
+// The next arm pair for this warp from counter *c (lane 0 takes it).
+__device__ __forceinline__ int take_pair(unsigned int *c, int lane) {
+    unsigned int p = 0;
+    if (lane == 0) p = atomicAdd(c, 1u);
+    return (int)__shfl_sync(kFull, p, 0);
+}
+
+// Arm pair p (pair_index order): its lower and upper arm.
+template <int A>
+__device__ __forceinline__ void pair_arms(int p, int &a, int &b) {
+    a = 0;
+    while (p >= A - 1 - a) {
+        p -= A - 1 - a;
+        a++;
+    }
+    b = a + 1 + p;
+}
 
 template <int A, int SPL>
 __device__ __forceinline__ void armwise_edge(const EdgeParams &P, unsigned char *wbase, const float4 *S,
@@ -1545,6 +1564,7 @@ __device__ __forceinline__ void armwise_edge(const EdgeParams &P, unsigned char 
 #pragma unroll
             for (int t = 0; t < 2; t++) X.env[t][lane] = X.self[t][lane] = 0;
             if (lane < 2) X.hits[lane] = 0;
+            if (lane < 3) X.next[lane] = 0;
         }
         __syncthreads();
         // this arm: placement, swept bounds, env and intra-arm screens (the
@@ -1584,46 +1604,46 @@ __device__ __forceinline__ void armwise_edge(const EdgeParams &P, unsigned char 
             }
         }
         __syncthreads();
-        // arm pairs (a, b), a < b, pair index = arm mod A: flags go to arm a
+        // arm pairs (a, b), a < b, handed out one at a time to the warps as
+        // they finish (their costs differ): flags go to arm a
         // (panda_four.cuh:178-214); screened by the slot's swept bounds
         if (A > 1 && do_self) {
             const WarpScratch *Wa = reinterpret_cast<const WarpScratch *>(wbase);
 #pragma unroll 1
-            for (int a = 0; a < A - 1; a++)
+            for (int p = take_pair(&X.next[0], lane); p < num_pairs(A); p = take_pair(&X.next[0], lane)) {
+                int a, b;
+                pair_arms<A>(p, a, b);
 #pragma unroll 1
-                for (int b = a + 1; b < A; b++) {
-                    if (pair_index(a, b, A) % A != arm) continue;
-#pragma unroll 1
-                    for (int s = 0; s < SPL; s++) {
-                        const int k = lane + 1 + 32 * s;
-                        const float4 *swa = Wa[a].broad.swept[s], *swb = Wa[b].broad.swept[s];
-                        uint32_t bal[4];
+                for (int s = 0; s < SPL; s++) {
+                    const int k = lane + 1 + 32 * s;
+                    const float4 *swa = Wa[a].broad.swept[s], *swb = Wa[b].broad.swept[s];
+                    uint32_t bal[4];
 #pragma unroll
-                        for (int r = 0; r < 4; r++) {
-                            const int t = 32 * r + lane;
-                            const int i = t / kNumApprox, j = t - kNumApprox * i;
-                            bal[r] = __ballot_sync(kFull, t < kNumApprox * kNumApprox &&
-                                                              near3(swa[i].x, swa[i].y, swa[i].z, swb[j], swa[i].w));
-                        }
-                        if (!(bal[0] | bal[1] | bal[2] | bal[3])) continue;
-                        const float(*low)[3][32] = s == 0 ? Wa[a].broad.cur : Wa[a].broad.low;
-                        const float(*cur)[3][32] = s == 0 ? Wa[b].broad.cur : Wa[b].broad.low;
-                        uint32_t am = 0;
-#pragma unroll
-                        for (int r = 0; r < 4; r++) {
-                            uint32_t q = bal[r];
-                            while (q) {
-                                const int t = 32 * r + __ffs(q) - 1;
-                                q &= q - 1;
-                                const int i = t / kNumApprox, j = t - kNumApprox * i;
-                                if (hit_sphere_sphere(low[i][0][lane], low[i][1][lane], low[i][2][lane],
-                                                      c_approx[i].w, cur[j][0][lane], cur[j][1][lane],
-                                                      cur[j][2][lane], c_approx[j].w))
-                                    am |= 1u << approx_joint(i);
-                            }
-                        }
-                        if (am && k <= g) atomicOr(&X.self[s][lane], (unsigned long long)am << (8 * a));
+                    for (int r = 0; r < 4; r++) {
+                        const int t = 32 * r + lane;
+                        const int i = t / kNumApprox, j = t - kNumApprox * i;
+                        bal[r] = __ballot_sync(kFull, t < kNumApprox * kNumApprox &&
+                                                          near3(swa[i].x, swa[i].y, swa[i].z, swb[j], swa[i].w));
                     }
+                    if (!(bal[0] | bal[1] | bal[2] | bal[3])) continue;
+                    const float(*low)[3][32] = s == 0 ? Wa[a].broad.cur : Wa[a].broad.low;
+                    const float(*cur)[3][32] = s == 0 ? Wa[b].broad.cur : Wa[b].broad.low;
+                    uint32_t am = 0;
+#pragma unroll
+                    for (int r = 0; r < 4; r++) {
+                        uint32_t q = bal[r];
+                        while (q) {
+                            const int t = 32 * r + __ffs(q) - 1;
+                            q &= q - 1;
+                            const int i = t / kNumApprox, j = t - kNumApprox * i;
+                            if (hit_sphere_sphere(low[i][0][lane], low[i][1][lane], low[i][2][lane],
+                                                  c_approx[i].w, cur[j][0][lane], cur[j][1][lane],
+                                                  cur[j][2][lane], c_approx[j].w))
+                                am |= 1u << approx_joint(i);
+                        }
+                    }
+                    if (am && k <= g) atomicOr(&X.self[s][lane], (unsigned long long)am << (8 * a));
+                }
                 }
         }
         __syncthreads();
@@ -1687,16 +1707,19 @@ __device__ __forceinline__ void armwise_edge(const EdgeParams &P, unsigned char 
                 W.gbd[a][gg] = make_float4(u.x, u.y, u.z, u.w + P.gofs[gg]);
             }
             __syncwarp();
-            uint32_t my_pairs = 0;
-            for (int pp = arm; pp < num_pairs(A); pp += A) my_pairs |= 1u << pp;
 #pragma unroll 1
             for (int s = 0; s < SPL; s++) {
                 const int bit = lane + 32 * s;
                 const bool dE = cand_env >> bit & 1ull, dS = cand_self >> bit & 1ull;
                 const int k = bit + 1 <= g ? bit + 1 : g;
                 bool h = narrow_lane<A, true>(P, W, S, L, det_tab, seg, k, envw[s], selfw[s], dE, dS, arm);
-                if (A > 1 && my_pairs && __any_sync(kFull, dS && !h))
-                    h |= cross_swept<A, true>(P, W, seg, k, selfw[s], dS && !h, my_pairs);
+                // the slot's arm pairs, one at a time to whichever warp is free
+                if (A > 1 && __any_sync(kFull, dS)) {
+                    unsigned int *next = &X.next[1 + s];
+                    for (int p = take_pair(next, lane); p < num_pairs(A); p = take_pair(next, lane))
+                        if (__any_sync(kFull, dS && !h))
+                            h |= cross_swept<A, true>(P, W, seg, k, selfw[s], dS && !h, 1u << p);
+                }
                 const unsigned int hb = __ballot_sync(kFull, h);
                 if (lane == 0 && hb) atomicOr(&X.hits[s], hb);
             }
