@@ -42,7 +42,7 @@ DRRT_STEP_EDGES = 8192  # a dRRT session's step size: larger checks are cut into
 # threads.  Each dRRT query issues a short device call per tree search, so a
 # few clients per slot keep the GPU fed without the host's cores spinning.
 SERVED_DRRT_STREAMS = 8
-SERVED_DRRT_CLIENTS = 12
+SERVED_DRRT_CLIENTS = 16
 
 
 def served_drrt_settings(**overrides):
