@@ -1165,6 +1165,52 @@ __device__ __forceinline__ void connect_advance(WarpScratch &W, int dof, int seg
 // Broad phase of one segment for this lane's samples plus the decision: which
 // samples get the detailed check (the reference's thread split, or every
 // flagged sample in EXACT mode).  Returns false when no sample is flagged.
+// The candidate masks of a segment from its samples' flag counts (totals over
+// the segment given): every flagged sample in EXACT mode, else the samples the
+// reference's proportional 4g-thread split gives at least one thread
+// (utils.cuh:476-517), the remainder going to the last sample.
+template <int SPL>
+__device__ __forceinline__ void thread_split(bool exact, int g, int lane, const int (&envc)[SPL],
+                                             const int (&selfc)[SPL], int tot_env, int tot_self, uint64_t &cand_env,
+                                             uint64_t &cand_self) {
+    if (exact) {
+#pragma unroll
+        for (int s = 0; s < SPL; s++) {
+            const uint64_t be = __ballot_sync(kFull, envc[s] > 0);
+            const uint64_t bs = __ballot_sync(kFull, selfc[s] > 0);
+            cand_env |= be << (32 * s);
+            cand_self |= bs << (32 * s);
+        }
+        return;
+    }
+    int de[SPL], ds[SPL], sum_e = 0, sum_s = 0;
+#pragma unroll
+    for (int s = 0; s < SPL; s++) {
+        const int k = lane + 1 + 32 * s;
+        de[s] = k <= g ? ref_share(envc[s], tot_env, g) : 0;
+        ds[s] = k <= g ? ref_share(selfc[s], tot_self, g) : 0;
+        sum_e += de[s];
+        sum_s += ds[s];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sum_e += __shfl_xor_sync(kFull, sum_e, o);
+        sum_s += __shfl_xor_sync(kFull, sum_s, o);
+    }
+#pragma unroll
+    for (int s = 0; s < SPL; s++) {
+        const int k = lane + 1 + 32 * s;
+        if (k == g) { // the remainder goes to the last sample
+            de[s] += 4 * g - sum_e;
+            ds[s] += 4 * g - sum_s;
+        }
+        const uint64_t be = __ballot_sync(kFull, tot_env > 0 && de[s] > 0);
+        const uint64_t bs = __ballot_sync(kFull, tot_self > 0 && ds[s] > 0);
+        cand_env |= be << (32 * s);
+        cand_self |= bs << (32 * s);
+    }
+}
+
 template <int A, int SPL>
 __device__ __forceinline__ bool broad_decide(const EdgeParams &P, WarpScratch &W, const float4 *S,
                                              const SceneLayout &L, int seg, int g, int lane, uint64_t (&envw)[SPL],
@@ -1206,42 +1252,7 @@ __device__ __forceinline__ bool broad_decide(const EdgeParams &P, WarpScratch &W
     cand_env = cand_self = 0;
     if (tot_env == 0 && tot_self == 0) return false;
     MRPOP_PHASE(P, 7);
-    if (P.flags & kExactBit) {
-#pragma unroll
-        for (int s = 0; s < SPL; s++) {
-            const uint64_t be = __ballot_sync(kFull, envc[s] > 0);
-            const uint64_t bs = __ballot_sync(kFull, selfc[s] > 0);
-            cand_env |= be << (32 * s);
-            cand_self |= bs << (32 * s);
-        }
-    } else {
-        int de[SPL], ds[SPL], sum_e = 0, sum_s = 0;
-#pragma unroll
-        for (int s = 0; s < SPL; s++) {
-            const int k = lane + 1 + 32 * s;
-            de[s] = k <= g ? ref_share(envc[s], tot_env, g) : 0;
-            ds[s] = k <= g ? ref_share(selfc[s], tot_self, g) : 0;
-            sum_e += de[s];
-            sum_s += ds[s];
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            sum_e += __shfl_xor_sync(kFull, sum_e, o);
-            sum_s += __shfl_xor_sync(kFull, sum_s, o);
-        }
-#pragma unroll
-        for (int s = 0; s < SPL; s++) {
-            const int k = lane + 1 + 32 * s;
-            if (k == g) { // the remainder goes to the last sample
-                de[s] += 4 * g - sum_e;
-                ds[s] += 4 * g - sum_s;
-            }
-            const uint64_t be = __ballot_sync(kFull, tot_env > 0 && de[s] > 0);
-            const uint64_t bs = __ballot_sync(kFull, tot_self > 0 && ds[s] > 0);
-            cand_env |= be << (32 * s);
-            cand_self |= bs << (32 * s);
-        }
-    }
+    thread_split<SPL>((P.flags & kExactBit) != 0, g, lane, envc, selfc, tot_env, tot_self, cand_env, cand_self);
     if (P.flops) {
         double f = 0.0;
 #pragma unroll
@@ -1666,38 +1677,8 @@ __device__ __forceinline__ void armwise_edge(const EdgeParams &P, unsigned char 
         }
         if (tot_env > 0 || tot_self > 0) {
             uint64_t cand_env = 0, cand_self = 0;
-            if (P.flags & kExactBit) {
-#pragma unroll
-                for (int s = 0; s < SPL; s++) {
-                    cand_env |= (uint64_t)__ballot_sync(kFull, envc[s] > 0) << (32 * s);
-                    cand_self |= (uint64_t)__ballot_sync(kFull, selfc[s] > 0) << (32 * s);
-                }
-            } else {
-                int de[SPL], ds[SPL], sum_e = 0, sum_s = 0;
-#pragma unroll
-                for (int s = 0; s < SPL; s++) {
-                    const int k = lane + 1 + 32 * s;
-                    de[s] = k <= g ? ref_share(envc[s], tot_env, g) : 0;
-                    ds[s] = k <= g ? ref_share(selfc[s], tot_self, g) : 0;
-                    sum_e += de[s];
-                    sum_s += ds[s];
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    sum_e += __shfl_xor_sync(kFull, sum_e, o);
-                    sum_s += __shfl_xor_sync(kFull, sum_s, o);
-                }
-#pragma unroll
-                for (int s = 0; s < SPL; s++) {
-                    const int k = lane + 1 + 32 * s;
-                    if (k == g) {  // the remainder goes to the last sample
-                        de[s] += 4 * g - sum_e;
-                        ds[s] += 4 * g - sum_s;
-                    }
-                    cand_env |= (uint64_t)__ballot_sync(kFull, tot_env > 0 && de[s] > 0) << (32 * s);
-                    cand_self |= (uint64_t)__ballot_sync(kFull, tot_self > 0 && ds[s] > 0) << (32 * s);
-                }
-            }
+            thread_split<SPL>((P.flags & kExactBit) != 0, g, lane, envc, selfc, tot_env, tot_self, cand_env,
+                              cand_self);
             // the segment's sub-group bounds for the arm-vs-arm screens, from
             // every arm's reference-sphere bounds (each warp's own row)
             const WarpScratch *Wa = reinterpret_cast<const WarpScratch *>(wbase);
