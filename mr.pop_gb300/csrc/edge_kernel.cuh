@@ -497,6 +497,29 @@ static __constant__ uint8_t c_intra_pairs[21][2] = {
 
 // Broad phase of one sample (every lane of the warp calls it; lanes past the
 // segment's last sample evaluate sample g and discard the result).
+// Intra-arm pairs of one arm (panda_four.cuh:140-176): the 21 approx sphere
+// pairs, one per lane, screened by the swept bounds sw of the warp's samples;
+// exact per-sample tests for the survivors.  Returns the lane's flag bits (by
+// joint of the pair's first sphere).
+__device__ __forceinline__ uint32_t intra_flags(const float (*sp)[3][32], const float4 *sw, int lane) {
+    // pair `lane` of c_intra_pairs, computed rather than read per lane
+    const int p1 = lane < 6 ? 0 : lane < 12 ? 1 : lane < 17 ? 2 : 5;
+    const int p2 = lane < 12 ? 5 + lane % 6 : lane == 12 ? 5 : lane < 17 ? lane - 6 : lane - 10;
+    const float4 u1 = sw[p1];
+    const bool c = lane < 21 && near3(u1.x, u1.y, u1.z, sw[p2], u1.w);
+    uint32_t bal = __ballot_sync(kFull, c);
+    uint32_t jm = 0;
+    while (bal) {
+        const int t = __ffs(bal) - 1;
+        bal &= bal - 1;
+        const int s1 = c_intra_pairs[t][0], s2 = c_intra_pairs[t][1];
+        if (hit_sphere_sphere(sp[s1][0][lane], sp[s1][1][lane], sp[s1][2][lane], c_approx[s1].w, sp[s2][0][lane],
+                              sp[s2][1][lane], sp[s2][2][lane], c_approx[s2].w))
+            jm |= 1u << approx_joint(s1);
+    }
+    return jm;
+}
+
 template <int A>
 __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W, const float4 *S,
                                              const SceneLayout &L, int seg, int k, bool merge, uint64_t &envw,
@@ -525,23 +548,7 @@ __device__ __forceinline__ void broad_sample(const EdgeParams &P, WarpScratch &W
         if (!do_self) continue;
         // intra-arm pairs: one pair per lane screened by swept bounds, exact
         // per-sample tests for the survivors
-        uint32_t jm = 0;
-        {
-            // pair `lane` of c_intra_pairs, computed rather than read per lane
-            const int p1 = lane < 6 ? 0 : lane < 12 ? 1 : lane < 17 ? 2 : 5;
-            const int p2 = lane < 12 ? 5 + lane % 6 : lane == 12 ? 5 : lane < 17 ? lane - 6 : lane - 10;
-            const float4 u1 = sw[p1];
-            const bool c = lane < 21 && near3(u1.x, u1.y, u1.z, sw[p2], u1.w);
-            uint32_t bal = __ballot_sync(kFull, c);
-            while (bal) {
-                const int t = __ffs(bal) - 1;
-                bal &= bal - 1;
-                const int s1 = c_intra_pairs[t][0], s2 = c_intra_pairs[t][1];
-                if (hit_sphere_sphere(cur[s1][0][lane], cur[s1][1][lane], cur[s1][2][lane], c_approx[s1].w,
-                                      cur[s2][0][lane], cur[s2][1][lane], cur[s2][2][lane], c_approx[s2].w))
-                    jm |= 1u << approx_joint(s1);
-            }
-        }
+        const uint32_t jm = intra_flags(cur, sw, lane);
         selfw |= (uint64_t)jm << (8 * b);
         MRPOP_PHASE(P, 2);
         if (A == 1) continue;
@@ -1594,21 +1601,7 @@ __device__ __forceinline__ void armwise_edge(const EdgeParams &P, unsigned char 
                 for (int i = 1; i < kNumApprox; i++)
                     if (m >> i & 1u) em |= 1u << approx_joint(i);
             }
-            if (do_self) {
-                const int p1 = lane < 6 ? 0 : lane < 12 ? 1 : lane < 17 ? 2 : 5;
-                const int p2 = lane < 12 ? 5 + lane % 6 : lane == 12 ? 5 : lane < 17 ? lane - 6 : lane - 10;
-                const float4 u1 = sw[p1];
-                const bool c = lane < 21 && near3(u1.x, u1.y, u1.z, sw[p2], u1.w);
-                uint32_t bal = __ballot_sync(kFull, c);
-                while (bal) {
-                    const int t = __ffs(bal) - 1;
-                    bal &= bal - 1;
-                    const int s1 = c_intra_pairs[t][0], s2 = c_intra_pairs[t][1];
-                    if (hit_sphere_sphere(sp[s1][0][lane], sp[s1][1][lane], sp[s1][2][lane], c_approx[s1].w,
-                                          sp[s2][0][lane], sp[s2][1][lane], sp[s2][2][lane], c_approx[s2].w))
-                        im |= 1u << approx_joint(s1);
-                }
-            }
+            if (do_self) im = intra_flags(sp, sw, lane);
             if (k <= g) {
                 if (em) atomicOr(&X.env[s][lane], (unsigned long long)em << (8 * arm));
                 if (im) atomicOr(&X.self[s][lane], (unsigned long long)im << (8 * arm));
