@@ -153,6 +153,36 @@ def test_every_arm_count_and_single_arm_forms(cuda, pkg, orc, arms):
         assert np.array_equal(got[0], ref["valid"]) and np.array_equal(got[1], ref["first_hit"])
 
 
+@pytest.mark.parametrize("arms,g", [(1, 64), (2, 48), (2, 64)])
+def test_one_and_two_arms_above_32_samples(cuda, pkg, orc, arms, g):
+    """Small calls of 1 and 2 arms above 32 samples per segment run two warps
+    per edge in the fused form (pair_kernel): composite and single-arm forms,
+    plain and connect rules."""
+    W = pkg.workloads
+    rng = np.random.default_rng(200 + 10 * arms + g)
+    bases = W.bases_facing_centre(arms, 0.71)
+    q0, q1 = W.random_edges(rng, 128, arms, 1.5)
+    scene_arrays = W.scene_config2(arms)
+    scene = pkg.Scene(scene_arrays)
+    rb = pkg.RobotSet(arms, bases)
+    for rule, rg in ((0, 0.0), (1, 0.6)):
+        trig = _edge_trig(cuda, pkg, orc, q0, q1, g, rule, rg)
+        for flags in (pkg.CHECK_ENV | pkg.CHECK_SELF, pkg.CHECK_SELF):
+            wl = W.Workload("t", scene_arrays, bases, q0, q1, g, flags, rule=rule, range_=rg)
+            got = _run(cuda, pkg, scene, rb, wl)
+            ref = orc.validate(scene_arrays, bases, q0, q1, g, flags, -1, rule, rg, trig=trig)
+            assert np.array_equal(got[0], ref["valid"]) and np.array_equal(got[1], ref["first_hit"])
+        for a in range(arms):
+            qa0, qa1 = np.ascontiguousarray(q0[:, 7 * a:7 * a + 7]), np.ascontiguousarray(q1[:, 7 * a:7 * a + 7])
+            ta = _edge_trig(cuda, pkg, orc, qa0, qa1, g, rule, rg)
+            wl = W.Workload("t", scene_arrays, bases, qa0, qa1, g, pkg.CHECK_ENV | pkg.CHECK_SELF, arm=a, rule=rule,
+                            range_=rg)
+            got = _run(cuda, pkg, scene, rb, wl)
+            ref = orc.validate(scene_arrays, bases, qa0, qa1, g, wl.flags, a, rule, rg, trig=ta)
+            assert np.array_equal(got[0], ref["valid"]) and np.array_equal(got[1], ref["first_hit"])
+    assert scene.status() == 0
+
+
 def test_all_obstacle_classes(cuda, pkg, orc):
     """Spheres, capsules, z-capsules, boxes and z-boxes in one scene; cylinders ignored."""
     W = pkg.workloads
