@@ -1551,7 +1551,7 @@ __device__ __forceinline__ int take_pair(unsigned int *c, int lane) {
 
 // Arm pair p (pair_index order): its lower and upper arm.
 template <int A>
-__device__ __forceinline__ void pair_arms(int p, int &a, int &b) {
+__host__ __device__ __forceinline__ constexpr void pair_arms(int p, int &a, int &b) {
     a = 0;
     while (p >= A - 1 - a) {
         p -= A - 1 - a;
@@ -1559,6 +1559,20 @@ __device__ __forceinline__ void pair_arms(int p, int &a, int &b) {
     }
     b = a + 1 + p;
 }
+
+// pair_arms inverts pair_index for every pair of up to 5 arms
+template <int A>
+constexpr bool pair_order_round_trips() {
+    for (int p = 0; p < num_pairs(A); p++) {
+        int a = 0, b = 0;
+        pair_arms<A>(p, a, b);
+        if (!(0 <= a && a < b && b < A) || pair_index(a, b, A) != p) return false;
+    }
+    return true;
+}
+static_assert(pair_order_round_trips<2>() && pair_order_round_trips<3>() && pair_order_round_trips<4>() &&
+                  pair_order_round_trips<5>(),
+              "arm pair order");
 
 template <int A, int SPL>
 __device__ __forceinline__ void armwise_edge(const EdgeParams &P, unsigned char *wbase, const float4 *S,
